@@ -1,0 +1,171 @@
+/*
+ * include/jmm_gpu.h -- the C ABI of libjmmgpu.so, the GB300 (sm_103a)
+ * implementation of jmmOneDMC's Monte Carlo move loop.
+ *
+ * Plain C: plain pointers and sizes, no CUDA or C++ types in any signature.
+ * Every entry point returns a status (JMM_OK = 0); jmm_last_error() gives the
+ * message of the last failure on the calling thread.  There is no CPU
+ * fallback: without a usable CUDA device every compute call fails with
+ * JMM_ERR_CUDA.
+ *
+ * Two forms of the same Metropolis chain:
+ *
+ *  - jmm_plain_*  : one chain, FP64, the reference's algorithm step for step
+ *                   (pair-state arrays, incremental separations, summation
+ *                   order, random-draw conditions).  It is the drop-in behind
+ *                   the reference's C++ API (src/jmmMCState.h:6-48) and, fed
+ *                   the same uniforms, reproduces its accept/reject sequence.
+ *  - jmm_batch_*  : thousands of independent chains in one persistent kernel
+ *                   (declared further down).
+ *
+ * Quantity order of every 9-vector (the reference's phi[] layout,
+ * src/pot.cpp:90-100): E, Vir, E12, Vir12, E6, Vir6, HV, HV12, HV6.
+ * Thermo accumulator order (src/jmmMCState.cpp:1941-1961): rhoSysA,
+ * rhoSysSA, lA, lSA, EA, ESA, lEA, VirA, VirSA, EVirA, HVA, HVSA.
+ */
+#ifndef JMM_GPU_H
+#define JMM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define JMM_OK 0
+#define JMM_ERR_INVALID 1     /* bad argument or unsupported combination     */
+#define JMM_ERR_CUDA 2        /* no device, launch failure, driver error     */
+#define JMM_ERR_NOMEM 3       /* device or host allocation failed            */
+#define JMM_ERR_TIMEOUT 4     /* a bounded device wait ran out               */
+#define JMM_ERR_NUMERIC 5     /* NaN/Inf energy or position seen by a kernel */
+#define JMM_ERR_STATE 6       /* call out of order (e.g. steps before fad)   */
+
+/* ---- enums ------------------------------------------------------------- */
+#define JMM_NLT 0             /* ENSEMBLE NLT (src/jmmMCState.cpp:412-421)   */
+#define JMM_NPT 1             /* ENSEMBLE NPT (src/jmmMCState.cpp:402-411)   */
+
+#define JMM_POT_LJCUT 0       /* POT LJcut <rc>: phiLJcut, src/pot.cpp:19-101 */
+#define JMM_POT_LJ 1          /* POT LJ: phiLJinfcutoff, src/pot.cpp:104-108  */
+#define JMM_POT_HARMONIC 2    /* POT HARMONIC [rc]: src/pot.cpp:110-141       */
+#define JMM_POT_SOFTSPHERE 3  /* eps (sigma/r)^12, batched form only          */
+#define JMM_POT_GAUSS 4       /* eps exp(-(r/sigma)^2), batched form only     */
+
+/* Quantity indices of the 9-vectors. */
+#define JMM_Q_E 0
+#define JMM_Q_VIR 1
+#define JMM_Q_E12 2
+#define JMM_Q_VIR12 3
+#define JMM_Q_E6 4
+#define JMM_Q_VIR6 5
+#define JMM_Q_HV 6
+#define JMM_Q_HV12 7
+#define JMM_Q_HV6 8
+
+/* ---- plain form: one FP64 chain ---------------------------------------- */
+
+/* The INPUT keywords that reach the move loop (src/jmmMCState.h:50-85). */
+typedef struct jmm_params {
+  uint64_t n;          /* N                                                   */
+  int32_t ensemble;    /* JMM_NLT | JMM_NPT                                   */
+  int32_t potential;   /* JMM_POT_LJCUT | JMM_POT_LJ | JMM_POT_HARMONIC       */
+  double p;            /* P (NPT)                                             */
+  double l;            /* L (NLT); NPT starts from L = N                      */
+  double t;            /* T                                                   */
+  double cutoff;       /* POT cut-off; INFINITY for POT LJ                    */
+  int32_t nbn;         /* NBN, -1 = no neighbour-number limit                 */
+  int32_t reserved0;
+  double max_step;     /* MAXSTEP                                             */
+  double max_dl;       /* MAXDV                                               */
+  uint64_t seed;       /* SEED                                                */
+  uint64_t eci;        /* ENGCHECK interval, 0 = never                        */
+} jmm_params;
+
+typedef struct jmm_state {
+  uint64_t sn;             /* step number                                     */
+  uint64_t rng_block;      /* Philox blocks opened since set-up               */
+  uint32_t rng_slot;       /* next word of the open block (4 = exhausted)     */
+  uint32_t error;          /* sticky JMM_ERR_* seen by a kernel, 0 = none     */
+  double l;                /* box length                                      */
+  double tot[9];           /* E, Vir, E12, Vir12, E6, Vir6, HV, HV12, HV6     */
+  uint64_t d_acc[2];       /* displacements accepted / rejected               */
+  uint64_t v_acc[2];       /* volume changes accepted / rejected              */
+  double max_step;
+  double max_dl;
+  double thermo[12];       /* block accumulators, order in the file header    */
+  uint64_t echeck_count;   /* energy checks run                               */
+  uint64_t echeck_resets;  /* energy checks that found |dE| > 1e-4            */
+  double echeck_e;         /* ETest of the last energy check                  */
+  double echeck_e_before;  /* running E just before the last energy check     */
+} jmm_state;
+
+/* Replay input: the values the reference consumed at one step. */
+typedef struct jmm_draw {
+  uint64_t nm;   /* trial type: particle index, or N for a volume move        */
+  double rn;     /* trial magnitude uniform                                   */
+  double ran;    /* Metropolis uniform, read only when the step draws one     */
+} jmm_draw;
+
+#define JMM_KIND_DISPLACEMENT 0
+#define JMM_KIND_VOLUME 1
+#define JMM_OUT_REJECT_WALL 0     /* |r_trial| > L/2: no energy work          */
+#define JMM_OUT_REJECT 1          /* Metropolis rejection                      */
+#define JMM_OUT_ACCEPT 2
+
+typedef struct jmm_step_record {
+  uint64_t sn;
+  uint64_t nm;
+  double rn;
+  double ran;      /* NaN when the step drew no Metropolis uniform            */
+  double bf;       /* Boltzmann factor when one was formed, else NaN          */
+  double e;
+  double vir;
+  double hv;
+  double l;
+  int32_t kind;    /* JMM_KIND_*                                               */
+  int32_t outcome; /* JMM_OUT_*                                                */
+} jmm_step_record;
+
+typedef struct jmm_plain jmm_plain;
+
+/* setupMCS (src/jmmMCState.cpp:261-790), fresh start: lattice
+ * r_i = ((i+0.5)/N - 0.5) L, separations, E = Vir = HV = 1e11 until fad. */
+int jmm_plain_create(const jmm_params *params, jmm_plain **out);
+/* Restart branch of setupMCS (src/jmmMCState.cpp:572-769): positions, box
+ * length and step number from a saved frame; energies back to 1e11. */
+int jmm_plain_set_config(jmm_plain *h, const double *r, uint64_t n, double l,
+                         uint64_t sn);
+/* fad (src/jmmMCState.cpp:853-1003) with explicit particle and uniform;
+ * the driver's step 0 is jmm_plain_fad(h, 0, 0.5) (src/Main.cpp:66-68). */
+int jmm_plain_fad(jmm_plain *h, uint64_t nm, double d);
+/* n_steps x (incrementStep + Step) (src/jmmMCState.cpp:1734-1811): draw,
+ * qad2 / fav / qavLJ, ECheck when sn % ENGCHECK == 0, updateThermo.
+ * replay: NULL to draw from the Philox stream, else n_steps draws.
+ * log: NULL, or room for n_steps records. */
+int jmm_plain_steps(jmm_plain *h, uint64_t n_steps, const jmm_draw *replay,
+                    jmm_step_record *log);
+/* updateThermo on its own (the driver's step-0 call, src/Main.cpp:95). */
+int jmm_plain_update_thermo(jmm_plain *h);
+/* Zero the 12 thermo accumulators (what printThermo does after printing,
+ * src/jmmMCState.cpp:1922-1934). */
+int jmm_plain_reset_thermo(jmm_plain *h);
+/* ECheck on its own (src/jmmMCState.cpp:1965-2095). */
+int jmm_plain_echeck(jmm_plain *h, double *e_test, int32_t *reset);
+/* maxDisAdjust / maxDVAdjust results written back (src/jmmMCState.cpp:2100-2139). */
+int jmm_plain_set_step_sizes(jmm_plain *h, double max_step, double max_dl);
+int jmm_plain_get_state(jmm_plain *h, jmm_state *out);
+int jmm_plain_get_positions(jmm_plain *h, double *r, uint64_t n);
+/* Stored pair separations r_j - r_i (i < j), row-major over i, N*(N-1)/2. */
+int jmm_plain_get_separations(jmm_plain *h, double *rij, uint64_t n_pairs);
+int jmm_plain_destroy(jmm_plain *h);
+
+const char *jmm_last_error(void);
+/* 1 when a CUDA device can be used by this library, else 0. */
+int jmm_device_available(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JMM_GPU_H */

@@ -1,0 +1,128 @@
+"""ctypes mirror of the public C ABI in include/jmm_gpu.h.
+
+Every structure here has the exact field order and types of its C
+counterpart; ``tests/test_abi.py`` checks the sizes against the header.
+"""
+import ctypes as C
+
+JMM_OK = 0
+JMM_ERR_INVALID = 1
+JMM_ERR_CUDA = 2
+JMM_ERR_NOMEM = 3
+JMM_ERR_TIMEOUT = 4
+JMM_ERR_NUMERIC = 5
+JMM_ERR_STATE = 6
+
+ERROR_NAMES = {
+    JMM_OK: "ok",
+    JMM_ERR_INVALID: "invalid argument",
+    JMM_ERR_CUDA: "CUDA error",
+    JMM_ERR_NOMEM: "out of memory",
+    JMM_ERR_TIMEOUT: "device wait timed out",
+    JMM_ERR_NUMERIC: "non-finite value",
+    JMM_ERR_STATE: "call out of order",
+}
+
+JMM_NLT = 0
+JMM_NPT = 1
+
+JMM_POT_LJCUT = 0
+JMM_POT_LJ = 1
+JMM_POT_HARMONIC = 2
+JMM_POT_SOFTSPHERE = 3
+JMM_POT_GAUSS = 4
+
+Q_NAMES = ("e", "vir", "e12", "vir12", "e6", "vir6", "hv", "hv12", "hv6")
+THERMO_NAMES = ("rhoSysA", "rhoSysSA", "lA", "lSA", "EA", "ESA", "lEA",
+                "VirA", "VirSA", "EVirA", "HVA", "HVSA")
+
+JMM_KIND_DISPLACEMENT = 0
+JMM_KIND_VOLUME = 1
+JMM_OUT_REJECT_WALL = 0
+JMM_OUT_REJECT = 1
+JMM_OUT_ACCEPT = 2
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("n", C.c_uint64),
+        ("ensemble", C.c_int32),
+        ("potential", C.c_int32),
+        ("p", C.c_double),
+        ("l", C.c_double),
+        ("t", C.c_double),
+        ("cutoff", C.c_double),
+        ("nbn", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("max_step", C.c_double),
+        ("max_dl", C.c_double),
+        ("seed", C.c_uint64),
+        ("eci", C.c_uint64),
+    ]
+
+
+class State(C.Structure):
+    _fields_ = [
+        ("sn", C.c_uint64),
+        ("rng_block", C.c_uint64),
+        ("rng_slot", C.c_uint32),
+        ("error", C.c_uint32),
+        ("l", C.c_double),
+        ("tot", C.c_double * 9),
+        ("d_acc", C.c_uint64 * 2),
+        ("v_acc", C.c_uint64 * 2),
+        ("max_step", C.c_double),
+        ("max_dl", C.c_double),
+        ("thermo", C.c_double * 12),
+        ("echeck_count", C.c_uint64),
+        ("echeck_resets", C.c_uint64),
+        ("echeck_e", C.c_double),
+        ("echeck_e_before", C.c_double),
+    ]
+
+
+class Draw(C.Structure):
+    _fields_ = [("nm", C.c_uint64), ("rn", C.c_double), ("ran", C.c_double)]
+
+
+class StepRecord(C.Structure):
+    _fields_ = [
+        ("sn", C.c_uint64),
+        ("nm", C.c_uint64),
+        ("rn", C.c_double),
+        ("ran", C.c_double),
+        ("bf", C.c_double),
+        ("e", C.c_double),
+        ("vir", C.c_double),
+        ("hv", C.c_double),
+        ("l", C.c_double),
+        ("kind", C.c_int32),
+        ("outcome", C.c_int32),
+    ]
+
+
+STEP_RECORD_DTYPE = [
+    ("sn", "<u8"), ("nm", "<u8"), ("rn", "<f8"), ("ran", "<f8"), ("bf", "<f8"),
+    ("e", "<f8"), ("vir", "<f8"), ("hv", "<f8"), ("l", "<f8"),
+    ("kind", "<i4"), ("outcome", "<i4"),
+]
+
+
+def make_params(n, ensemble=JMM_NLT, potential=JMM_POT_LJCUT, p=1.0, l=None,
+                t=1.0, cutoff=3.0, nbn=-1, max_step=0.3, max_dl=1.0, seed=1,
+                eci=0):
+    """Build a Params with the INPUT keyword meanings of src/readInput.cpp."""
+    prm = Params()
+    prm.n = n
+    prm.ensemble = ensemble
+    prm.potential = potential
+    prm.p = p
+    prm.l = float(n) if l is None else l
+    prm.t = t
+    prm.cutoff = float("inf") if potential == JMM_POT_LJ else cutoff
+    prm.nbn = nbn
+    prm.max_step = max_step
+    prm.max_dl = max_dl
+    prm.seed = seed
+    prm.eci = eci
+    return prm

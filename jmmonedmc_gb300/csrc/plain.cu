@@ -1,0 +1,939 @@
+// plain.cu -- the plain one-chain FP64 form of jmmOneDMC's move loop on one
+// GB300, behind the jmm_plain_* entry points of include/jmm_gpu.h.
+//
+// This is the reference's algorithm step for step, so that, fed the same
+// uniforms, it reproduces the reference's accept/reject sequence and its
+// FP64 totals bit for bit:
+//   phiLJcut / phiLJinfcutoff / phiHarmoniccut   src/pot.cpp:19-141
+//   fad                                          src/jmmMCState.cpp:853-1003
+//   qad2 (incremental separations, two partial   src/jmmMCState.cpp:1160-1464
+//         sums i<nm then i>nm, in index order)
+//   qavLJ                                        src/jmmMCState.cpp:1648-1730
+//   Step / incrementStep                         src/jmmMCState.cpp:1734-1811
+//   updateThermo                                 src/jmmMCState.cpp:1941-1961
+//   ECheck                                       src/jmmMCState.cpp:1965-2095
+//   fav                                          src/jmmMCState.cpp:2161-2293
+//
+// GB300 mapping: one persistent 1024-thread block runs many steps per launch.
+// Pair terms of a step are evaluated in parallel; the FP64 sums that decide
+// acceptance are formed by nine lanes of warp 0 (one per quantity) in the
+// reference's index order, because a reordered FP64 sum would not round the
+// same.  Per-pair state (separations and nine quantities) stays in HBM,
+// (i<j) at i*N+j; a step touches N-1 pairs, a volume move or energy check
+// all N(N-1)/2.  This TU is compiled with -fmad=false: no FP64 expression is
+// contracted into a fused multiply-add, matching the reference's x86-64 build.
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <new>
+
+#include "common.cuh"
+#include "philox.cuh"
+
+namespace jmm {
+namespace plain {
+
+constexpr int kThreads = 1024;
+constexpr uint64_t kMaxN = 2900;  // partner terms of one step must fit in shared memory
+
+struct Scalars {
+  uint64_t sn;
+  uint64_t rng_block;
+  uint32_t rng_slot;
+  uint32_t error;
+  uint32_t words[4];
+  double l, max_step, max_dl;
+  double bf, ran;  // persist between steps like mcs->bf and the file-static ran
+  double tot[9];
+  uint64_t d_acc[2], v_acc[2];
+  double thermo[12];
+  uint64_t echeck_count, echeck_resets;
+  double echeck_e, echeck_e_before;
+};
+
+struct Args {
+  Scalars *s;
+  double *r;        // N positions
+  double *r_trial;  // N trial positions (volume move, fad)
+  double *rij;      // N*N, stored separation r_j - r_i at i*N+j (i<j)
+  double *q;        // 9*N*N stored pair quantities
+  double *scratch;  // 9*P pair terms of a full sum, packed row-major over (i<j)
+  uint64_t n, nn, npairs, num_trial_types;
+  int32_t potential, nbn;
+  int32_t use_qavlj;
+  int32_t pad;
+  double cutoff, t, p;
+  uint64_t seed, eci;
+};
+
+struct Ctl {
+  uint64_t nm;
+  double rn, md, rt;
+  double dl, lnew, lrat1;
+  double ran, bf;
+  double sum[9];
+  int32_t wall, accept, kind, outcome, reset, pad;
+};
+
+// ---- pair potentials (FP64, the reference's operand order) --------------
+
+__device__ __forceinline__ void phi_lj(double d, double cut, bool virial, double *phi) {
+  double d3 = __dmul_rn(__dmul_rn(d, d), d);
+  double r6 = __ddiv_rn(1.0, __dmul_rn(d3, d3));
+  double r12 = __dmul_rn(r6, r6);
+  double phitot = 0, phi6 = 0, phi12 = 0, vir6 = 0, vir12 = 0, virtot = 0;
+  double hv6 = 0, hv12 = 0, hvtot = 0;
+  if (d <= cut) {
+    phi6 = __dmul_rn(4.0, r6);
+    phi12 = __dmul_rn(4.0, r12);
+    phitot = __dsub_rn(phi12, phi6);
+    if (virial) {
+      vir6 = __dmul_rn(24.0, r6);
+      vir12 = __dmul_rn(48.0, r12);
+      virtot = __dsub_rn(vir12, vir6);
+      hv6 = __dmul_rn(144.0, r6);
+      hv12 = __dmul_rn(576.0, r12);
+      hvtot = __dsub_rn(hv12, hv6);
+    }
+  }
+  phi[0] = phitot;
+  phi[1] = virtot;
+  phi[2] = phi12;
+  phi[3] = vir12;
+  phi[4] = phi6;
+  phi[5] = vir6;
+  phi[6] = hvtot;
+  phi[7] = hv12;
+  phi[8] = hv6;
+}
+
+// phiHarmoniccut leaves phi[2..8] unwritten (and phi[1] undefined without the
+// virial flag); they are 0 here.
+__device__ __forceinline__ void phi_harmonic(double d, double cut, bool virial, double l,
+                                             double *phi) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) phi[k] = 0.0;
+  if (d <= 0) {
+    phi[0] = 10E10;
+    phi[1] = 10E10;
+  } else if (d < cut) {
+    double rijm = __dsub_rn(d, 1.0);
+    phi[0] = __dmul_rn(rijm, rijm);
+    phi[1] = virial ? __dmul_rn(__dmul_rn(__ddiv_rn(2.0, l), d), rijm) : 0.0;
+  }
+}
+
+__device__ __forceinline__ void phi_eval(const Args &a, double d, bool virial, double l,
+                                         double *phi) {
+  if (a.potential == JMM_POT_HARMONIC)
+    phi_harmonic(d, a.cutoff, virial, l, phi);
+  else
+    phi_lj(d, a.potential == JMM_POT_LJ ? (double)INFINITY : a.cutoff, virial, phi);
+}
+
+__device__ __forceinline__ bool pair_cut(const Args &a, uint64_t i, uint64_t j) {
+  return a.nbn >= 0 && (j - i) > (uint64_t)a.nbn;
+}
+
+__device__ __forceinline__ uint64_t packed_index(uint64_t i, uint64_t j, uint64_t n) {
+  return i * (n - 1) - (i * (i + 1)) / 2 + j - 1;
+}
+
+// ---- the stream the reference consumes (thread 0 only) ----------------
+
+__device__ void open_block(Scalars *S, uint64_t seed) {
+  S->rng_block += 1;
+  Words4 w = step_words(seed, S->rng_block, 0u);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) S->words[k] = w.w[k];
+  S->rng_slot = 0;
+}
+
+__device__ uint64_t draw_int(Scalars *S, uint64_t seed, uint64_t n) {
+  open_block(S, seed);
+  S->rng_slot = 1;
+  return word_to_index(S->words[0], n);
+}
+
+__device__ double draw_uniform(Scalars *S, uint64_t seed) {
+  if (S->rng_slot >= 4) {
+    open_block(S, seed);
+    S->rng_slot = 1;
+  }
+  uint32_t w = S->words[S->rng_slot];
+  S->rng_slot += 1;
+  return word_to_unit(w);
+}
+
+// ---- block-wide pieces ----------------------------------------------------
+
+// Pair terms of every pair at positions `x` (box length `l` for HARMONIC's
+// virial) into scratch[k*9 + q]; pairs beyond NBN get zeros.
+__device__ void full_terms(const Args &a, const double *x, bool virial, double l) {
+  const uint64_t n = a.n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (uint64_t i = warp; i < n; i += nwarps) {
+    const uint64_t row = packed_index(i, i + 1, n);
+    for (uint64_t j = i + 1 + lane; j < n; j += 32) {
+      double phi[9];
+      if (pair_cut(a, i, j)) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) phi[k] = 0.0;
+      } else {
+        phi_eval(a, __dsub_rn(x[j], x[i]), virial, l, phi);
+      }
+      double *dst = a.scratch + (row + (j - i - 1)) * 9;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) dst[k] = phi[k];
+    }
+  }
+}
+
+// Lanes 0..8 of warp 0: sequential sums of the scratch terms in pair order.
+__device__ void full_sums(const Args &a, Ctl &ctl) {
+  if (threadIdx.x < 9) {
+    const int k = threadIdx.x;
+    double s = 0.0;
+#pragma unroll 8
+    for (uint64_t p = 0; p < a.npairs; ++p) s = __dadd_rn(s, a.scratch[p * 9 + k]);
+    ctl.sum[k] = s;
+  }
+}
+
+// Scratch terms into the stored pair arrays, with separations from `x`.
+__device__ void commit_all(const Args &a, const double *x) {
+  const uint64_t n = a.n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (uint64_t i = warp; i < n; i += nwarps) {
+    const uint64_t row = packed_index(i, i + 1, n);
+    for (uint64_t j = i + 1 + lane; j < n; j += 32) {
+      const uint64_t ind = i * n + j;
+      const double *src = a.scratch + (row + (j - i - 1)) * 9;
+      a.rij[ind] = __dsub_rn(x[j], x[i]);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) a.q[k * a.nn + ind] = src[k];
+    }
+  }
+}
+
+__device__ void update_thermo(Scalars *S, uint64_t n) {
+  double *acc = S->thermo;
+  const double l = S->l, e = S->tot[JMM_Q_E], vir = S->tot[JMM_Q_VIR], hv = S->tot[JMM_Q_HV];
+  const double rho = __ddiv_rn((double)n, l);
+  acc[0] = __dadd_rn(acc[0], rho);
+  acc[1] = __dadd_rn(acc[1], __dmul_rn(rho, rho));
+  acc[2] = __dadd_rn(acc[2], l);
+  acc[3] = __dadd_rn(acc[3], __dmul_rn(l, l));
+  acc[4] = __dadd_rn(acc[4], e);
+  acc[5] = __dadd_rn(acc[5], __dmul_rn(e, e));
+  acc[6] = __dadd_rn(acc[6], __dmul_rn(l, e));
+  acc[7] = __dadd_rn(acc[7], vir);
+  acc[8] = __dadd_rn(acc[8], __dmul_rn(vir, vir));
+  acc[9] = __dadd_rn(acc[9], __dmul_rn(e, vir));
+  acc[10] = __dadd_rn(acc[10], hv);
+  acc[11] = __dadd_rn(acc[11], __dmul_rn(hv, hv));
+}
+
+// ---- the moves --------------------------------------------------------------
+
+// qad2: displacement of particle ctl.nm by (rn - 0.5) * 2 * maxStep.
+__device__ void qad2(const Args &a, Ctl &ctl, double *s_new, double *s_rij, const jmm_draw *rp) {
+  Scalars *S = a.s;
+  const uint64_t n = a.n, nm = ctl.nm, nm1 = n - 1;
+  if (threadIdx.x == 0) {
+    const double md = __dmul_rn(__dmul_rn(__dsub_rn(ctl.rn, 0.5), 2.0), S->max_step);
+    const double rt = __dadd_rn(a.r[nm], md);
+    ctl.md = md;
+    ctl.rt = rt;
+    ctl.kind = JMM_KIND_DISPLACEMENT;
+    ctl.ran = NAN;
+    ctl.bf = NAN;
+    ctl.wall = fabs(rt) > __ddiv_rn(S->l, 2.0);
+    if (ctl.wall) {
+      S->d_acc[1] += 1;
+      ctl.outcome = JMM_OUT_REJECT_WALL;
+    }
+  }
+  __syncthreads();
+  if (ctl.wall) return;
+  const double md = ctl.md, l = S->l;
+  for (uint64_t p = threadIdx.x; p < nm1; p += blockDim.x) {
+    const uint64_t i = p < nm ? p : p + 1;
+    const uint64_t lo = i < nm ? i : nm, hi = i < nm ? nm : i;
+    const uint64_t ind = lo * n + hi;
+    const double rt = (i < nm) ? __dadd_rn(a.rij[ind], md) : __dsub_rn(a.rij[ind], md);
+    double phi[9];
+    if (pair_cut(a, lo, hi)) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) phi[k] = 0.0;
+    } else {
+      phi_eval(a, rt, true, l, phi);
+    }
+    s_rij[p] = rt;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) s_new[k * nm1 + p] = phi[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 9) {
+    const int k = threadIdx.x;
+    const double *old = a.q + (uint64_t)k * a.nn;
+    const double *nw = s_new + (uint64_t)k * nm1;
+    double sa = 0.0, sb = 0.0;
+#pragma unroll 4
+    for (uint64_t p = 0; p < nm; ++p) sa = __dadd_rn(__dsub_rn(sa, old[p * n + nm]), nw[p]);
+#pragma unroll 4
+    for (uint64_t p = nm; p < nm1; ++p)
+      sb = __dadd_rn(__dsub_rn(sb, old[nm * n + p + 1]), nw[p]);
+    ctl.sum[k] = __dadd_rn(sa, sb);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double de = ctl.sum[JMM_Q_E];
+    if (de > 0) {
+      S->ran = rp ? rp->ran : draw_uniform(S, a.seed);
+      S->bf = exp(__ddiv_rn(-de, a.t));
+      ctl.ran = S->ran;
+      ctl.bf = S->bf;
+    }
+    const bool acc = (de <= 0) || (S->bf > S->ran);
+    if (acc) {
+      S->d_acc[0] += 1;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) S->tot[k] = __dadd_rn(S->tot[k], ctl.sum[k]);
+      a.r[nm] = ctl.rt;
+      ctl.outcome = JMM_OUT_ACCEPT;
+    } else {
+      S->d_acc[1] += 1;
+      ctl.outcome = JMM_OUT_REJECT;
+    }
+    ctl.accept = acc;
+  }
+  __syncthreads();
+  if (ctl.accept) {
+    for (uint64_t p = threadIdx.x; p < nm1; p += blockDim.x) {
+      const uint64_t i = p < nm ? p : p + 1;
+      const uint64_t ind = i < nm ? i * n + nm : nm * n + i;
+      a.rij[ind] = s_rij[p];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) a.q[k * a.nn + ind] = s_new[k * nm1 + p];
+    }
+  }
+  __syncthreads();
+}
+
+// fav: full-energy volume move, linear dl uniform in +-maxdl.
+__device__ void fav(const Args &a, Ctl &ctl, const jmm_draw *rp) {
+  Scalars *S = a.s;
+  const uint64_t n = a.n;
+  if (threadIdx.x == 0) {
+    const double dl = __dmul_rn(__dmul_rn(__dsub_rn(ctl.rn, 0.5), 2.0), S->max_dl);
+    const double lnew = __dadd_rn(S->l, dl);
+    ctl.dl = dl;
+    ctl.lnew = lnew;
+    ctl.lrat1 = __ddiv_rn(lnew, S->l);
+    ctl.kind = JMM_KIND_VOLUME;
+    ctl.ran = NAN;
+  }
+  __syncthreads();
+  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) a.r_trial[i] = __dmul_rn(a.r[i], ctl.lrat1);
+  __syncthreads();
+  full_terms(a, a.r_trial, true, ctl.lnew);
+  __syncthreads();
+  full_sums(a, ctl);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double arg = __dadd_rn(
+        __ddiv_rn(-__dadd_rn(__dsub_rn(ctl.sum[JMM_Q_E], S->tot[JMM_Q_E]), __dmul_rn(a.p, ctl.dl)),
+                  a.t),
+        __dmul_rn((double)n, log(ctl.lrat1)));
+    S->bf = exp(arg);
+    ctl.bf = S->bf;
+    if (S->bf < 1.0) {
+      S->ran = rp ? rp->ran : draw_uniform(S, a.seed);
+      ctl.ran = S->ran;
+    }
+    const bool acc = (S->bf >= 1.0) || (S->bf > S->ran);
+    if (acc) {
+      S->v_acc[0] += 1;
+      S->l = __dadd_rn(S->l, ctl.dl);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) S->tot[k] = ctl.sum[k];
+      ctl.outcome = JMM_OUT_ACCEPT;
+    } else {
+      S->v_acc[1] += 1;
+      ctl.outcome = JMM_OUT_REJECT;
+    }
+    ctl.accept = acc;
+  }
+  __syncthreads();
+  if (ctl.accept) {
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) a.r[i] = a.r_trial[i];
+    commit_all(a, a.r_trial);
+  }
+  __syncthreads();
+}
+
+// qavLJ with a nine-entry phi buffer.  The reference's six-entry buffer
+// (src/jmmMCState.cpp:1651) overflows and aborts there; nothing here is
+// pinned to it.
+__device__ void qav_lj(const Args &a, Ctl &ctl, const jmm_draw *rp) {
+  Scalars *S = a.s;
+  const uint64_t n = a.n;
+  __shared__ double lrat1_s;
+  if (threadIdx.x == 0) {
+    const double dl = __dmul_rn(__dmul_rn(__dsub_rn(ctl.rn, 0.5), 2.0), S->max_dl);
+    const double lrat1 = __ddiv_rn(__dadd_rn(S->l, dl), S->l);
+    const double lrat3 = __dmul_rn(__dmul_rn(lrat1, lrat1), lrat1);
+    const double lrat6 = __ddiv_rn(1.0, __dmul_rn(lrat3, lrat3));
+    const double lrat12 = __dmul_rn(lrat6, lrat6);
+    const double e12t = __dmul_rn(lrat12, S->tot[JMM_Q_E12]);
+    const double e6t = __dmul_rn(lrat6, S->tot[JMM_Q_E6]);
+    const double de = __dsub_rn(__dsub_rn(e12t, e6t), S->tot[JMM_Q_E]);
+    const double arg =
+        __dadd_rn(__ddiv_rn(-__dadd_rn(de, __dmul_rn(a.p, dl)), a.t), __dmul_rn((double)n, log(lrat1)));
+    S->bf = exp(arg);
+    ctl.kind = JMM_KIND_VOLUME;
+    ctl.bf = S->bf;
+    ctl.ran = NAN;
+    if (S->bf < 1.0) {
+      S->ran = rp ? rp->ran : draw_uniform(S, a.seed);
+      ctl.ran = S->ran;
+    }
+    const bool acc = (S->bf >= 1.0) || (S->bf > S->ran);
+    if (acc) {
+      S->v_acc[0] += 1;
+      S->tot[JMM_Q_E] = __dadd_rn(S->tot[JMM_Q_E], de);
+      S->tot[JMM_Q_E12] = e12t;
+      S->tot[JMM_Q_E6] = e6t;
+      S->l = __dadd_rn(S->l, dl);
+      const double lrat7 = __ddiv_rn(lrat6, lrat1);
+      const double lrat13 = __ddiv_rn(lrat12, lrat1);
+      S->tot[JMM_Q_VIR6] = __dmul_rn(lrat7, S->tot[JMM_Q_VIR6]);
+      S->tot[JMM_Q_VIR12] = __dmul_rn(lrat13, S->tot[JMM_Q_VIR12]);
+      S->tot[JMM_Q_VIR] = __dsub_rn(
+          __dadd_rn(__ddiv_rn(__dmul_rn((double)n, a.t), S->l), S->tot[JMM_Q_VIR12]),
+          S->tot[JMM_Q_VIR6]);
+      ctl.outcome = JMM_OUT_ACCEPT;
+    } else {
+      S->v_acc[1] += 1;
+      ctl.outcome = JMM_OUT_REJECT;
+    }
+    ctl.accept = acc;
+    lrat1_s = lrat1;
+  }
+  __syncthreads();
+  if (ctl.accept) {
+    const double lrat1 = lrat1_s, l = S->l;
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) a.r[i] = __dmul_rn(lrat1, a.r[i]);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    for (uint64_t i = warp; i < n; i += nwarps) {
+      for (uint64_t j = i + 1 + lane; j < n; j += 32) {
+        const uint64_t ind = i * n + j;
+        const double rij = __dmul_rn(lrat1, a.rij[ind]);
+        a.rij[ind] = rij;
+        double phi[9];
+        phi_eval(a, rij, true, l, phi);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) a.q[k * a.nn + ind] = phi[k];
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// ECheck: full FP64 re-sum of E from the positions; on |dE| > 1e-4 rebuild
+// every pair and total.
+__device__ void echeck(const Args &a, Ctl &ctl) {
+  Scalars *S = a.s;
+  const uint64_t n = a.n;
+  full_terms(a, a.r, false, S->l);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (uint64_t p = 0; p < a.npairs; ++p) s = __dadd_rn(s, a.scratch[p * 9]);
+    S->echeck_count += 1;
+    S->echeck_e = s;
+    S->echeck_e_before = S->tot[JMM_Q_E];
+    ctl.reset = fabs(__dsub_rn(s, S->tot[JMM_Q_E])) > 0.0001;
+    if (ctl.reset) S->echeck_resets += 1;
+  }
+  __syncthreads();
+  if (!ctl.reset) return;
+  const double l = S->l;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (uint64_t i = warp; i < n; i += nwarps) {
+    const uint64_t row = packed_index(i, i + 1, n);
+    for (uint64_t j = i + 1 + lane; j < n; j += 32) {
+      const uint64_t ind = i * n + j;
+      double phi[9];
+      if (pair_cut(a, i, j)) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) phi[k] = 0.0;
+      } else {
+        const double rij = __dsub_rn(a.r[j], a.r[i]);
+        a.rij[ind] = rij;
+        phi_eval(a, rij, true, l, phi);
+      }
+      double *dst = a.scratch + (row + (j - i - 1)) * 9;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        a.q[k * a.nn + ind] = phi[k];
+        dst[k] = phi[k];
+      }
+    }
+  }
+  __syncthreads();
+  full_sums(a, ctl);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) S->tot[k] = ctl.sum[k];
+  }
+  __syncthreads();
+}
+
+// ---- kernels ------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kThreads, 1)
+    steps_kernel(Args a, uint64_t n_steps, const jmm_draw *replay, jmm_step_record *log) {
+  extern __shared__ double smem[];
+  __shared__ Ctl ctl;
+  Scalars *S = a.s;
+  const uint64_t nm1 = a.n - 1;
+  double *s_new = smem;
+  double *s_rij = smem + 9 * nm1;
+  for (uint64_t step = 0; step < n_steps; ++step) {
+    const jmm_draw *rp = replay ? replay + step : nullptr;
+    if (threadIdx.x == 0) {
+      S->sn += 1;
+      if (rp) {
+        ctl.nm = rp->nm;
+        ctl.rn = rp->rn;
+      } else {
+        ctl.nm = draw_int(S, a.seed, a.num_trial_types);
+        ctl.rn = draw_uniform(S, a.seed);
+      }
+      ctl.outcome = JMM_OUT_REJECT;
+      ctl.kind = JMM_KIND_DISPLACEMENT;
+      ctl.ran = NAN;
+      ctl.bf = NAN;
+    }
+    __syncthreads();
+    if (ctl.nm < a.n) {
+      qad2(a, ctl, s_new, s_rij, rp);
+    } else if (ctl.nm == a.n) {
+      if (a.use_qavlj)
+        qav_lj(a, ctl, rp);
+      else
+        fav(a, ctl, rp);
+    } else if (threadIdx.x == 0) {
+      S->error = JMM_ERR_INVALID;  // trial type beyond N: "unknown trial type"
+    }
+    __syncthreads();
+    if (a.eci && (S->sn % a.eci) == 0) echeck(a, ctl);
+    if (threadIdx.x == 0) {
+      update_thermo(S, a.n);
+      if (log) {
+        jmm_step_record rec;
+        rec.sn = S->sn;
+        rec.nm = ctl.nm;
+        rec.rn = ctl.rn;
+        rec.ran = ctl.ran;
+        rec.bf = ctl.bf;
+        rec.e = S->tot[JMM_Q_E];
+        rec.vir = S->tot[JMM_Q_VIR];
+        rec.hv = S->tot[JMM_Q_HV];
+        rec.l = S->l;
+        rec.kind = ctl.kind;
+        rec.outcome = ctl.outcome;
+        log[step] = rec;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) fad_kernel(Args a, uint64_t nm, double d) {
+  __shared__ Ctl ctl;
+  Scalars *S = a.s;
+  const uint64_t n = a.n;
+  if (threadIdx.x == 0) {
+    const double md = __dmul_rn(__dmul_rn(__dsub_rn(d, 0.5), 2.0), S->max_step);
+    ctl.rt = __dadd_rn(a.r[nm], md);
+    ctl.wall = fabs(ctl.rt) > __ddiv_rn(S->l, 2.0);
+    if (ctl.wall) S->d_acc[1] += 1;
+  }
+  __syncthreads();
+  if (ctl.wall) return;
+  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) a.r_trial[i] = (i == nm) ? ctl.rt : a.r[i];
+  __syncthreads();
+  full_terms(a, a.r_trial, true, S->l);
+  __syncthreads();
+  full_sums(a, ctl);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double et = ctl.sum[JMM_Q_E], e = S->tot[JMM_Q_E];
+    if (et > e) {
+      S->ran = draw_uniform(S, a.seed);
+      S->bf = exp(__ddiv_rn(__dsub_rn(e, et), a.t));
+    }
+    const bool acc = (et < e) || (S->bf > S->ran);
+    if (acc) {
+      S->d_acc[0] += 1;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) S->tot[k] = ctl.sum[k];
+      a.r[nm] = ctl.rt;
+    } else {
+      S->d_acc[1] += 1;
+    }
+    ctl.accept = acc;
+  }
+  __syncthreads();
+  if (ctl.accept) commit_all(a, a.r_trial);
+}
+
+__global__ void __launch_bounds__(kThreads, 1) echeck_kernel(Args a) {
+  __shared__ Ctl ctl;
+  echeck(a, ctl);
+}
+
+__global__ void separations_kernel(Args a) {
+  const uint64_t n = a.n;
+  for (uint64_t ind = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; ind < a.nn;
+       ind += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = ind / n, j = ind % n;
+    if (j > i) a.rij[ind] = __dsub_rn(a.r[j], a.r[i]);
+  }
+}
+
+__global__ void update_thermo_kernel(Args a) { update_thermo(a.s, a.n); }
+
+}  // namespace plain
+}  // namespace jmm
+
+using namespace jmm;
+using namespace jmm::plain;
+
+struct jmm_plain {
+  jmm_params prm;
+  Args a;
+  size_t smem_bytes;
+  jmm_draw *d_replay;
+  uint64_t replay_cap;
+  jmm_step_record *d_log;
+  uint64_t log_cap;
+  bool initialised;  // fad has run since set-up
+};
+
+static void plain_free(jmm_plain *h) {
+  if (!h) return;
+  cudaFree(h->a.s);
+  cudaFree(h->a.r);
+  cudaFree(h->a.r_trial);
+  cudaFree(h->a.rij);
+  cudaFree(h->a.q);
+  cudaFree(h->a.scratch);
+  cudaFree(h->d_replay);
+  cudaFree(h->d_log);
+  delete h;
+}
+
+static int plain_sync(const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_status(e, what, __FILE__, __LINE__);
+  return JMM_OK;
+}
+
+static int plain_reset_separations(jmm_plain *h) {
+  const uint64_t nn = h->a.nn;
+  int blocks = (int)((nn + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  separations_kernel<<<blocks, 256>>>(h->a);
+  return plain_sync("separations_kernel");
+}
+
+extern "C" int jmm_plain_create(const jmm_params *prm, jmm_plain **out) {
+  clear_error();
+  JMM_CHECK_ARG(prm && out, "null argument");
+  *out = nullptr;
+  JMM_CHECK_ARG(prm->n >= 2 && prm->n <= kMaxN, "N must be in [2, 2900] for the plain form");
+  JMM_CHECK_ARG(prm->ensemble == JMM_NLT || prm->ensemble == JMM_NPT, "unknown ensemble");
+  JMM_CHECK_ARG(prm->potential == JMM_POT_LJCUT || prm->potential == JMM_POT_LJ ||
+                    prm->potential == JMM_POT_HARMONIC,
+                "the plain form runs the reference's potentials LJcut, LJ and HARMONIC");
+  JMM_CHECK_ARG(prm->t > 0, "T must be positive");
+  JMM_CHECK_ARG(prm->ensemble == JMM_NPT || prm->l > 0, "L must be positive");
+  if (!jmm_device_available()) return fail(JMM_ERR_CUDA, "jmm_plain_create: no CUDA device");
+
+  jmm_plain *h = new (std::nothrow) jmm_plain();
+  if (!h) return fail(JMM_ERR_NOMEM, "jmm_plain_create: host allocation failed");
+  h->prm = *prm;
+  const uint64_t n = prm->n;
+  Args &a = h->a;
+  a.n = n;
+  a.nn = n * n;
+  a.npairs = n * (n - 1) / 2;
+  a.num_trial_types = prm->ensemble == JMM_NPT ? n + 1 : n;
+  a.potential = prm->potential;
+  a.nbn = prm->nbn;
+  a.use_qavlj = (prm->potential == JMM_POT_LJ && prm->nbn < 0) ? 1 : 0;
+  a.cutoff = prm->potential == JMM_POT_LJ ? INFINITY : prm->cutoff;
+  a.t = prm->t;
+  a.p = prm->p;
+  a.seed = prm->seed;
+  a.eci = prm->eci;
+  h->smem_bytes = 10 * (n - 1) * sizeof(double);
+
+  int rc = JMM_OK;
+#define ALLOC(ptr, bytes)                                               \
+  do {                                                                  \
+    cudaError_t e_ = cudaMalloc((void **)&(ptr), (bytes));              \
+    if (e_ != cudaSuccess) {                                            \
+      rc = cuda_status(e_, "cudaMalloc " #ptr, __FILE__, __LINE__);     \
+      plain_free(h);                                                    \
+      return rc;                                                        \
+    }                                                                   \
+  } while (0)
+  ALLOC(a.s, sizeof(Scalars));
+  ALLOC(a.r, n * sizeof(double));
+  ALLOC(a.r_trial, n * sizeof(double));
+  ALLOC(a.rij, a.nn * sizeof(double));
+  ALLOC(a.q, 9 * a.nn * sizeof(double));
+  ALLOC(a.scratch, 9 * a.npairs * sizeof(double));
+#undef ALLOC
+
+  Scalars s;
+  memset(&s, 0, sizeof(s));
+  s.rng_slot = 4;
+  s.l = prm->ensemble == JMM_NPT ? (double)n : prm->l;
+  s.max_step = prm->max_step;
+  s.max_dl = prm->max_dl;
+  s.tot[JMM_Q_E] = 10E10;
+  s.tot[JMM_Q_VIR] = 10E10;
+  s.tot[JMM_Q_HV] = 10E10;
+  s.tot[JMM_Q_E6] = -5E10;
+  s.tot[JMM_Q_E12] = 5E10;
+  s.tot[JMM_Q_VIR6] = -5E10;
+  s.tot[JMM_Q_VIR12] = 5E10;
+  s.tot[JMM_Q_HV6] = -5E10;
+  s.tot[JMM_Q_HV12] = 5E10;
+  double *r = (double *)malloc(n * sizeof(double));
+  if (!r) {
+    plain_free(h);
+    return fail(JMM_ERR_NOMEM, "jmm_plain_create: host allocation failed");
+  }
+  for (uint64_t i = 0; i < n; ++i) r[i] = ((i + 0.5) / n - 0.5) * s.l;
+  cudaError_t e = cudaMemcpy(a.r, r, n * sizeof(double), cudaMemcpyHostToDevice);
+  free(r);
+  if (e == cudaSuccess) e = cudaMemcpy(a.s, &s, sizeof(s), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(a.q, 0, 9 * a.nn * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemset(a.rij, 0, a.nn * sizeof(double));
+  if (e == cudaSuccess && h->smem_bytes > 48 * 1024)
+    e = cudaFuncSetAttribute(steps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)h->smem_bytes);
+  if (e != cudaSuccess) {
+    rc = cuda_status(e, "jmm_plain_create set-up", __FILE__, __LINE__);
+    plain_free(h);
+    return rc;
+  }
+  rc = plain_reset_separations(h);
+  if (rc != JMM_OK) {
+    plain_free(h);
+    return rc;
+  }
+  *out = h;
+  return JMM_OK;
+}
+
+extern "C" int jmm_plain_destroy(jmm_plain *h) {
+  plain_free(h);
+  return JMM_OK;
+}
+
+static int get_scalars(jmm_plain *h, Scalars *s) {
+  JMM_CUDA(cudaMemcpy(s, h->a.s, sizeof(Scalars), cudaMemcpyDeviceToHost));
+  return JMM_OK;
+}
+
+static int put_scalars(jmm_plain *h, const Scalars *s) {
+  JMM_CUDA(cudaMemcpy(h->a.s, s, sizeof(Scalars), cudaMemcpyHostToDevice));
+  return JMM_OK;
+}
+
+extern "C" int jmm_plain_set_config(jmm_plain *h, const double *r, uint64_t n, double l,
+                                    uint64_t sn) {
+  clear_error();
+  JMM_CHECK_ARG(h && r, "null argument");
+  JMM_CHECK_ARG(n == h->a.n, "N does not match the chain");
+  JMM_CHECK_ARG(l > 0, "box length must be positive");
+  Scalars s;
+  int rc = get_scalars(h, &s);
+  if (rc) return rc;
+  s.l = l;
+  s.sn = sn;
+  s.tot[JMM_Q_E] = 10.0E10;
+  s.tot[JMM_Q_VIR] = 10.0E10;
+  s.tot[JMM_Q_HV] = 10.0E10;
+  JMM_CUDA(cudaMemcpy(h->a.r, r, n * sizeof(double), cudaMemcpyHostToDevice));
+  rc = put_scalars(h, &s);
+  if (rc) return rc;
+  h->initialised = false;
+  return plain_reset_separations(h);
+}
+
+extern "C" int jmm_plain_fad(jmm_plain *h, uint64_t nm, double d) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  JMM_CHECK_ARG(nm < h->a.n, "particle index out of range");
+  fad_kernel<<<1, kThreads>>>(h->a, nm, d);
+  int rc = plain_sync("fad_kernel");
+  if (rc == JMM_OK) h->initialised = true;
+  return rc;
+}
+
+extern "C" int jmm_plain_steps(jmm_plain *h, uint64_t n_steps, const jmm_draw *replay,
+                               jmm_step_record *log) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  if (!h->initialised)
+    return fail(JMM_ERR_STATE, "jmm_plain_steps: run jmm_plain_fad first (the driver's step 0)");
+  const uint64_t chunk_max = (replay || log) ? (1u << 16) : (1u << 20);
+  for (uint64_t done = 0; done < n_steps;) {
+    const uint64_t chunk = (n_steps - done) < chunk_max ? (n_steps - done) : chunk_max;
+    if (replay) {
+      if (h->replay_cap < chunk) {
+        cudaFree(h->d_replay);
+        h->d_replay = nullptr;
+        JMM_CUDA(cudaMalloc((void **)&h->d_replay, chunk * sizeof(jmm_draw)));
+        h->replay_cap = chunk;
+      }
+      for (uint64_t k = 0; k < chunk; ++k) {
+        if (replay[done + k].nm > h->a.n)
+          return fail(JMM_ERR_INVALID, "jmm_plain_steps: replay draw %llu has trial type %llu > N",
+                      (unsigned long long)(done + k), (unsigned long long)replay[done + k].nm);
+      }
+      JMM_CUDA(cudaMemcpy(h->d_replay, replay + done, chunk * sizeof(jmm_draw),
+                          cudaMemcpyHostToDevice));
+    }
+    if (log && h->log_cap < chunk) {
+      cudaFree(h->d_log);
+      h->d_log = nullptr;
+      JMM_CUDA(cudaMalloc((void **)&h->d_log, chunk * sizeof(jmm_step_record)));
+      h->log_cap = chunk;
+    }
+    steps_kernel<<<1, kThreads, h->smem_bytes>>>(h->a, chunk, replay ? h->d_replay : nullptr,
+                                                  log ? h->d_log : nullptr);
+    int rc = plain_sync("steps_kernel");
+    if (rc) return rc;
+    if (log)
+      JMM_CUDA(cudaMemcpy(log + done, h->d_log, chunk * sizeof(jmm_step_record),
+                          cudaMemcpyDeviceToHost));
+    done += chunk;
+  }
+  Scalars s;
+  int rc = get_scalars(h, &s);
+  if (rc) return rc;
+  if (s.error) return fail((int)s.error, "jmm_plain_steps: kernel reported error %u", s.error);
+  return JMM_OK;
+}
+
+extern "C" int jmm_plain_update_thermo(jmm_plain *h) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  update_thermo_kernel<<<1, 1>>>(h->a);
+  return plain_sync("update_thermo_kernel");
+}
+
+extern "C" int jmm_plain_reset_thermo(jmm_plain *h) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  Scalars s;
+  int rc = get_scalars(h, &s);
+  if (rc) return rc;
+  memset(s.thermo, 0, sizeof(s.thermo));
+  return put_scalars(h, &s);
+}
+
+extern "C" int jmm_plain_echeck(jmm_plain *h, double *e_test, int32_t *reset) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  Scalars before;
+  int rc = get_scalars(h, &before);
+  if (rc) return rc;
+  echeck_kernel<<<1, kThreads>>>(h->a);
+  rc = plain_sync("echeck_kernel");
+  if (rc) return rc;
+  Scalars s;
+  rc = get_scalars(h, &s);
+  if (rc) return rc;
+  if (e_test) *e_test = s.echeck_e;
+  if (reset) *reset = s.echeck_resets > before.echeck_resets ? 1 : 0;
+  return JMM_OK;
+}
+
+extern "C" int jmm_plain_set_step_sizes(jmm_plain *h, double max_step, double max_dl) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  Scalars s;
+  int rc = get_scalars(h, &s);
+  if (rc) return rc;
+  s.max_step = max_step;
+  s.max_dl = max_dl;
+  return put_scalars(h, &s);
+}
+
+extern "C" int jmm_plain_get_state(jmm_plain *h, jmm_state *out) {
+  clear_error();
+  JMM_CHECK_ARG(h && out, "null argument");
+  Scalars s;
+  int rc = get_scalars(h, &s);
+  if (rc) return rc;
+  memset(out, 0, sizeof(*out));
+  out->sn = s.sn;
+  out->rng_block = s.rng_block;
+  out->rng_slot = s.rng_slot;
+  out->error = s.error;
+  out->l = s.l;
+  memcpy(out->tot, s.tot, sizeof(s.tot));
+  out->d_acc[0] = s.d_acc[0];
+  out->d_acc[1] = s.d_acc[1];
+  out->v_acc[0] = s.v_acc[0];
+  out->v_acc[1] = s.v_acc[1];
+  out->max_step = s.max_step;
+  out->max_dl = s.max_dl;
+  memcpy(out->thermo, s.thermo, sizeof(s.thermo));
+  out->echeck_count = s.echeck_count;
+  out->echeck_resets = s.echeck_resets;
+  out->echeck_e = s.echeck_e;
+  out->echeck_e_before = s.echeck_e_before;
+  return JMM_OK;
+}
+
+extern "C" int jmm_plain_get_positions(jmm_plain *h, double *r, uint64_t n) {
+  clear_error();
+  JMM_CHECK_ARG(h && r, "null argument");
+  JMM_CHECK_ARG(n == h->a.n, "N does not match the chain");
+  JMM_CUDA(cudaMemcpy(r, h->a.r, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return JMM_OK;
+}
+
+extern "C" int jmm_plain_get_separations(jmm_plain *h, double *rij, uint64_t n_pairs) {
+  clear_error();
+  JMM_CHECK_ARG(h && rij, "null argument");
+  const uint64_t n = h->a.n;
+  JMM_CHECK_ARG(n_pairs == n * (n - 1) / 2, "n_pairs must be N(N-1)/2");
+  double *dense = (double *)malloc(h->a.nn * sizeof(double));
+  if (!dense) return fail(JMM_ERR_NOMEM, "jmm_plain_get_separations: host allocation failed");
+  cudaError_t e = cudaMemcpy(dense, h->a.rij, h->a.nn * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    free(dense);
+    return cuda_status(e, "cudaMemcpy separations", __FILE__, __LINE__);
+  }
+  uint64_t k = 0;
+  for (uint64_t i = 0; i < n; ++i)
+    for (uint64_t j = i + 1; j < n; ++j) rij[k++] = dense[i * n + j];
+  free(dense);
+  return JMM_OK;
+}

@@ -1,0 +1,133 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Runs the reference's move loop, compiled from its own sources with the
+project's Philox stand-in for GSL (oracle/Makefile target ``ref``), on a set
+of INPUT files, and stores per-step trajectories, final positions, thermo
+accumulators and the reference's own output files as small compressed
+fixtures.  It needs the reference tree (REF_SRC, default
+/root/reference/src) and is run by hand:
+
+    python tests/golden/make_golden.py
+
+The fixtures are what the CPU and GPU parity tests compare against; nothing
+at test time reads the reference tree.
+"""
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+ORACLE = os.path.join(REPO, "oracle")
+HARNESS = os.path.join(ORACLE, "_ref", "ref_harness")
+
+REF_STEP_DTYPE = np.dtype([
+    ("sn", "<u8"), ("nm", "<u8"), ("rn", "<f8"), ("e", "<f8"), ("vir", "<f8"),
+    ("hv", "<f8"), ("l", "<f8"), ("e12", "<f8"), ("e6", "<f8"), ("vir12", "<f8"),
+    ("vir6", "<f8"), ("hv12", "<f8"), ("hv6", "<f8"), ("d_acc0", "<u8"),
+    ("d_acc1", "<u8"), ("v_acc0", "<u8"), ("v_acc1", "<u8"),
+])
+
+# keyword -> value; every keyword is written because the reference leaves
+# omitted ones uninitialised (src/readInput.cpp:38-57)
+BASE = dict(ENSEMBLE="NLT", N=64, P=1.0, L=106.66666666666667, T=1.0,
+            NUMSTEPS=3000, POT="LJcut 3.0", NBN=-1, MAXSTEP=0.3, MAXDV=0.5,
+            CPI=1000, TPI=500, RBW=0.1, RHONB=10, RHOPI=1000000000, GSW=200.0,
+            GNS=1, GBW=0.1, GNB=10, GPI=1000000000, SEED=1, ENGCHECK=500,
+            DADJ=10**18, VADJ=10**18)
+
+CASES = {
+    # the CPU-runnable plain workload: NLT, N=64, rho=0.6, LJcut 3.0, T=1
+    "nlt64_ljcut": dict(),
+    # NPT with the full-energy volume move fav (src/jmmMCState.cpp:2161-2293)
+    "npt64_ljcut": dict(ENSEMBLE="NPT", P=1.0, SEED=7, ENGCHECK=1000, MAXDV=0.5),
+    # POT LJ with a neighbour-number limit: NPT volume move is fav
+    "npt48_lj_nbn2": dict(ENSEMBLE="NPT", N=48, POT="LJ", NBN=2, SEED=11,
+                          ENGCHECK=700, MAXDV=0.5),
+    # HARMONIC with NBN 1, as in the reference's test/INPUTstd
+    "npt10_harmonic_nbn1": dict(ENSEMBLE="NPT", N=10, P=0.7, T=0.4,
+                                POT="HARMONIC", NBN=1, MAXSTEP=0.1, MAXDV=1.0,
+                                SEED=125, ENGCHECK=1, NUMSTEPS=2000),
+    # the per-chain size of the batched workload, NLT at rho = 0.6
+    "nlt256_ljcut": dict(N=256, L=256 / 0.6, SEED=3, NUMSTEPS=2000,
+                         ENGCHECK=1000, TPI=400, CPI=1000),
+    # dense NPT start (L = N) with a wide volume step: many volume moves
+    "npt32_ljcut_wide": dict(ENSEMBLE="NPT", N=32, P=2.0, T=1.5, MAXDV=2.0,
+                             SEED=99, NUMSTEPS=4000, ENGCHECK=250),
+}
+
+
+def input_text(kw):
+    lines = []
+    for key in ("ENSEMBLE", "N", "P", "L", "T", "NUMSTEPS", "POT", "NBN",
+                "MAXSTEP", "MAXDV", "CPI", "TPI", "RBW", "RHONB", "RHOPI",
+                "GSW", "GNS", "GBW", "GNB", "GPI", "SEED", "ENGCHECK", "DADJ",
+                "VADJ"):
+        v = kw[key]
+        if isinstance(v, float):
+            v = repr(v)
+        lines.append(f"{key:<10} {v}")
+    return "\n".join(lines) + "\n"
+
+
+def build_reference():
+    subprocess.run(["make", "-s", "-C", ORACLE, "ref"], check=True)
+
+
+def run_case(name, overrides):
+    kw = dict(BASE)
+    kw.update(overrides)
+    text = input_text(kw)
+    with tempfile.TemporaryDirectory() as tmp:
+        with open(os.path.join(tmp, "INPUT"), "w") as f:
+            f.write(text)
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        out = subprocess.run([HARNESS, "steps.bin", "final.bin"], cwd=tmp, env=env,
+                             check=True, capture_output=True, text=True)
+        steps = np.fromfile(os.path.join(tmp, "steps.bin"), dtype=REF_STEP_DTYPE)
+        raw = np.fromfile(os.path.join(tmp, "final.bin"), dtype="<u8", count=1)
+        n = int(raw[0])
+        fin = np.fromfile(os.path.join(tmp, "final.bin"), dtype="<f8")[1:]
+        r_final, thermo = fin[:n], fin[n:n + 12]
+        files = {}
+        for fn in ("thermo.dat.mcs", "config.dat.mcs"):
+            with open(os.path.join(tmp, fn)) as f:
+                files[fn] = f.read()
+    outcome = np.zeros(len(steps), dtype=np.int8)
+    acc = (np.diff(steps["d_acc0"].astype(np.int64)) + np.diff(steps["v_acc0"].astype(np.int64)))
+    outcome[1:] = acc
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"),
+        input=np.array(text),
+        sn=steps["sn"].astype(np.uint32),
+        nm=steps["nm"].astype(np.uint32),
+        rn=steps["rn"],
+        e=steps["e"], vir=steps["vir"], hv=steps["hv"], l=steps["l"],
+        e12=steps["e12"], e6=steps["e6"],
+        d_acc0=steps["d_acc0"].astype(np.uint32), d_acc1=steps["d_acc1"].astype(np.uint32),
+        v_acc0=steps["v_acc0"].astype(np.uint32), v_acc1=steps["v_acc1"].astype(np.uint32),
+        accepted=outcome,
+        r_final=r_final, thermo_final=thermo,
+        thermo_file=np.array(files["thermo.dat.mcs"]),
+        config_file=np.array(files["config.dat.mcs"]),
+        stdout_tail=np.array("\n".join(out.stdout.splitlines()[-4:])),
+    )
+    return dict(name=name, input=kw, steps=len(steps) - 1)
+
+
+def main():
+    build_reference()
+    index = [run_case(name, over) for name, over in CASES.items()]
+    with open(os.path.join(HERE, "index.json"), "w") as f:
+        json.dump(dict(generator="tests/golden/make_golden.py",
+                       rng="Philox4x32-10, one block per step (oracle/philox.h)",
+                       cases=index), f, indent=1)
+    print("\n".join(f"{c['name']}: {c['steps']} steps" for c in index))
+
+
+if __name__ == "__main__":
+    sys.exit(main())

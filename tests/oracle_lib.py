@@ -1,0 +1,162 @@
+"""ctypes handle on the oracle's CPU library (oracle/_build/libjmmoracle.so).
+
+Test infrastructure: the CPU restatement that the CUDA paths are checked
+against.  It shares the public structs of include/jmm_gpu.h.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from jmmonedmc_gb300 import abi
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB = os.path.join(REPO, "oracle", "_build", "libjmmoracle.so")
+_lib = None
+
+P = C.POINTER
+u64, i32, u32, dbl, vp = C.c_uint64, C.c_int32, C.c_uint32, C.c_double, C.c_void_p
+
+SIGS = {
+    "jmmo_plain_create": ([P(abi.Params)], vp),
+    "jmmo_plain_set_config": ([vp, P(dbl), u64, dbl, u64], C.c_int),
+    "jmmo_plain_fad": ([vp, u64, dbl], C.c_int),
+    "jmmo_plain_steps": ([vp, u64, vp, vp], C.c_int),
+    "jmmo_plain_update_thermo": ([vp], C.c_int),
+    "jmmo_plain_reset_thermo": ([vp], C.c_int),
+    "jmmo_plain_echeck": ([vp, P(dbl), P(i32)], C.c_int),
+    "jmmo_plain_set_step_sizes": ([vp, dbl, dbl], C.c_int),
+    "jmmo_plain_get_state": ([vp, P(abi.State)], C.c_int),
+    "jmmo_plain_get_positions": ([vp, P(dbl), u64], C.c_int),
+    "jmmo_plain_get_separations": ([vp, P(dbl), u64], C.c_int),
+    "jmmo_plain_destroy": ([vp], None),
+    "jmmo_philox_raw": ([P(u32), P(u32), P(u32)], None),
+    "jmmo_step_words_export": ([u64, u64, u32, P(u32)], None),
+}
+
+
+def extra_sigs(sigs):
+    SIGS.update(sigs)
+    if _lib is not None:
+        _bind(_lib)
+
+
+def _bind(lib):
+    for name, (args, res) in SIGS.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.argtypes = args
+        fn.restype = res
+
+
+def load():
+    global _lib
+    if _lib is None:
+        subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle")], check=True)
+        _lib = C.CDLL(LIB)
+        _bind(_lib)
+    return _lib
+
+
+def _ok(rc, name):
+    if rc != 0:
+        raise RuntimeError(f"{name} returned {rc}")
+
+
+class OraclePlain:
+    """Same surface as jmmonedmc_gb300.plain.PlainChain, on the CPU."""
+
+    def __init__(self, params):
+        self.lib = load()
+        self.params = params
+        self._h = self.lib.jmmo_plain_create(C.byref(params))
+        if not self._h:
+            raise ValueError("jmmo_plain_create rejected the parameters")
+
+    @property
+    def n(self):
+        return int(self.params.n)
+
+    def close(self):
+        if self._h:
+            self.lib.jmmo_plain_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def fad(self, nm=0, d=0.5):
+        _ok(self.lib.jmmo_plain_fad(self._h, nm, d), "fad")
+
+    def steps(self, n_steps, replay=None, log=False):
+        rp = None
+        if replay is not None:
+            arr = (abi.Draw * n_steps)()
+            for k in range(n_steps):
+                arr[k].nm, arr[k].rn, arr[k].ran = (int(replay[k][0]), float(replay[k][1]),
+                                                    float(replay[k][2]))
+            rp = C.cast(arr, C.c_void_p)
+        rec = (abi.StepRecord * n_steps)() if log else None
+        _ok(self.lib.jmmo_plain_steps(self._h, n_steps, rp,
+                                      C.cast(rec, C.c_void_p) if rec is not None else None),
+            "steps")
+        if rec is not None:
+            return np.frombuffer(rec, dtype=np.dtype(abi.STEP_RECORD_DTYPE)).copy()
+        return None
+
+    def set_config(self, r, l, sn=0):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        _ok(self.lib.jmmo_plain_set_config(self._h, r.ctypes.data_as(P(dbl)), r.size, l, sn),
+            "set_config")
+
+    def update_thermo(self):
+        _ok(self.lib.jmmo_plain_update_thermo(self._h), "update_thermo")
+
+    def reset_thermo(self):
+        _ok(self.lib.jmmo_plain_reset_thermo(self._h), "reset_thermo")
+
+    def echeck(self):
+        e = C.c_double()
+        reset = C.c_int32()
+        _ok(self.lib.jmmo_plain_echeck(self._h, C.byref(e), C.byref(reset)), "echeck")
+        return e.value, bool(reset.value)
+
+    def set_step_sizes(self, max_step, max_dl):
+        _ok(self.lib.jmmo_plain_set_step_sizes(self._h, max_step, max_dl), "set_step_sizes")
+
+    def state(self):
+        st = abi.State()
+        _ok(self.lib.jmmo_plain_get_state(self._h, C.byref(st)), "get_state")
+        return st
+
+    def positions(self):
+        r = np.empty(self.n, dtype=np.float64)
+        _ok(self.lib.jmmo_plain_get_positions(self._h, r.ctypes.data_as(P(dbl)), self.n),
+            "get_positions")
+        return r
+
+    def separations(self):
+        m = self.n * (self.n - 1) // 2
+        rij = np.empty(m, dtype=np.float64)
+        _ok(self.lib.jmmo_plain_get_separations(self._h, rij.ctypes.data_as(P(dbl)), m),
+            "get_separations")
+        return rij
+
+
+
+def philox_raw(ctr, key):
+    lib = load()
+    c = (u32 * 4)(*ctr)
+    k = (u32 * 2)(*key)
+    o = (u32 * 4)()
+    lib.jmmo_philox_raw(c, k, o)
+    return list(o)
+
+
+def step_words(seed, block, chain=0):
+    lib = load()
+    o = (u32 * 4)()
+    lib.jmmo_step_words_export(seed, block, chain, o)
+    return list(o)
