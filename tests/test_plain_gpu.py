@@ -48,10 +48,14 @@ def _compare_logs(a, b, fields=("sn", "nm", "kind", "outcome")):
     for f in ("rn", "e", "vir", "hv", "l"):
         d = np.nonzero(gc.bits(a[f]) != gc.bits(b[f]))[0]
         assert d.size == 0, f"{f} differs first at step {d[0]}"
-    for f in ("ran", "bf"):
-        both_nan = np.isnan(a[f]) & np.isnan(b[f])
-        same = gc.bits(a[f]) == gc.bits(b[f])
-        assert np.all(both_nan | same), f
+    both_nan = np.isnan(a["ran"]) & np.isnan(b["ran"])
+    assert np.all(both_nan | (gc.bits(a["ran"]) == gc.bits(b["ran"]))), "ran"
+    # bf = exp(...): CUDA's exp and the host libm's may differ in the last
+    # place; the decisions (outcome, above) must not.
+    fa, fb = a["bf"], b["bf"]
+    nan = np.isnan(fa) & np.isnan(fb)
+    close = np.abs(fa - fb) <= 4 * np.spacing(np.maximum(np.abs(fa), np.abs(fb)))
+    assert np.all(nan | close), "bf beyond 4 ulp"
 
 
 CONFIGS = [
