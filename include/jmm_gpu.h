@@ -160,6 +160,109 @@ int jmm_plain_get_positions(jmm_plain *h, double *r, uint64_t n);
 int jmm_plain_get_separations(jmm_plain *h, double *rij, uint64_t n_pairs);
 int jmm_plain_destroy(jmm_plain *h);
 
+/* ---- batched form: many independent chains ------------------------------
+ *
+ * Each chain is the reference's sequential single-particle Metropolis chain
+ * (random particle, uniform displacement, hard walls at +-L/2 by default),
+ * run with FP32 pair energies and FP64 totals and accumulators.  Thousands of
+ * chains of uneven N, temperature, pressure and potential share one
+ * persistent kernel: a group of lanes per chain, positions staged in shared
+ * memory, the energy change reduced with warp shuffles.  Particles keep
+ * their order along the line (a move that would pass a neighbour is
+ * rejected), so a move needs only the index neighbours within the cut-off.
+ * Chain k draws from Philox block (step, k) of the batch seed.
+ */
+#define JMM_BOUNDARY_WALLS 0     /* hard walls at +-L/2 (src/jmmMCState.cpp:1188-1193) */
+#define JMM_BOUNDARY_PERIODIC 1  /* ring of length L                                   */
+#define JMM_VOLMOVE_LINEAR 0     /* dL uniform in +-vol_step, weight N ln(L'/L) (fav)  */
+#define JMM_VOLMOVE_LNL 1        /* ln L uniform in +-vol_step, weight (N+1) ln(L'/L)  */
+#define JMM_VOLSCHED_RANDOM 0    /* trial type uniform over N+1 each step (Step)       */
+#define JMM_VOLSCHED_SWEEP 1     /* N displacements then one volume move per sweep     */
+#define JMM_PREC_FAST 0          /* hardware reciprocal and exp: production            */
+#define JMM_PREC_EXACT 1         /* IEEE reciprocal, portable exp: replayable on a CPU */
+#define JMM_INIT_LATTICE 0       /* r_i = ((i+0.5)/N - 0.5) L  (jmmMCState.cpp:559-562) */
+#define JMM_INIT_JITTER 1        /* lattice plus U(-jitter, jitter) per particle        */
+
+typedef struct jmm_chain_desc {
+  uint32_t n;          /* particles                                          */
+  int32_t potential;   /* JMM_POT_LJCUT | JMM_POT_SOFTSPHERE | JMM_POT_GAUSS */
+  int32_t ensemble;    /* JMM_NLT (constant L) | JMM_NPT                     */
+  int32_t reserved0;
+  double eps;
+  double sigma;
+  double cutoff;
+  double t;            /* temperature                                        */
+  double p;            /* pressure (NPT)                                     */
+  double l0;           /* initial box length                                 */
+  double max_step;     /* displacement half-width                            */
+  double vol_step;     /* ln L half-width (LNL) or max dL (LINEAR)           */
+} jmm_chain_desc;
+
+typedef struct jmm_batch_config {
+  uint64_t seed;
+  int32_t boundary;          /* JMM_BOUNDARY_*                                  */
+  int32_t vol_move;          /* JMM_VOLMOVE_*                                   */
+  int32_t vol_schedule;      /* JMM_VOLSCHED_*                                  */
+  int32_t precision;         /* JMM_PREC_*                                      */
+  uint32_t resum_sweeps;     /* constant-L chains: FP64 re-sum of E every this
+                                many sweeps (0 = only at the end of a run)      */
+  uint32_t lanes_per_chain;  /* 4, 8, 16 or 32; 0 = 8                           */
+  uint32_t chains_per_block; /* 0 = 4                                           */
+  int32_t init;              /* JMM_INIT_*                                      */
+  double jitter;             /* half-width of the initial jitter               */
+} jmm_batch_config;
+
+/* Per-chain state and statistics, FP64 (also the device-side record). */
+typedef struct jmm_chain_result {
+  double e;              /* running total energy                               */
+  double l;              /* box length                                         */
+  uint64_t steps;        /* attempted moves since creation                     */
+  uint64_t samples;      /* steps accumulated since the last reset             */
+  double sum_e, sum_e2, sum_l, sum_l2, sum_le, sum_rho, sum_rho2;
+  uint64_t disp_acc, disp_att, vol_acc, vol_att;
+  uint64_t pair_evals;   /* pair energies evaluated                            */
+  double max_drift;      /* largest |running E - fresh FP64 sum| at a re-sum   */
+  uint32_t error;        /* JMM_ERR_* seen by the kernel, 0 = none             */
+  uint32_t window_overflows; /* moves whose neighbour window was extended      */
+} jmm_chain_result;
+
+typedef struct jmm_batch jmm_batch;
+
+int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                     uint32_t n_chains, jmm_batch **out);
+/* n_sweeps sweeps of every chain (N steps, N+1 with volume moves), then wait. */
+int jmm_batch_run(jmm_batch *b, uint64_t n_sweeps);
+/* Same, enqueued on a CUDA stream (cudaStream_t passed as void*), no wait. */
+int jmm_batch_run_async(jmm_batch *b, uint64_t n_sweeps, void *stream);
+int jmm_batch_results(jmm_batch *b, jmm_chain_result *out, uint32_t n_chains);
+/* Zero the statistics (sums, samples, counters) but keep the state. */
+int jmm_batch_reset_stats(jmm_batch *b);
+int jmm_batch_get_positions(jmm_batch *b, uint32_t chain, float *x, uint32_t n);
+int jmm_batch_set_positions(jmm_batch *b, uint32_t chain, const float *x, uint32_t n,
+                            double l);
+/* FP64 sums of the FP32 pair energies of every chain's current positions. */
+int jmm_batch_energies(jmm_batch *b, double *e, uint32_t n_chains);
+/* Device addresses of the positions (float, chain k at offsets[k]) and of the
+ * jmm_chain_result array, for zero-copy tooling (torch, benchmarks). */
+int jmm_batch_device_views(jmm_batch *b, void **positions, void **results,
+                           uint64_t *offsets, uint32_t n_chains);
+/* Time candidate launch shapes on a copy of the state and keep the fastest;
+ * writes the chosen lanes_per_chain and chains_per_block. */
+int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t *lanes_per_chain,
+                       uint32_t *chains_per_block);
+int jmm_batch_destroy(jmm_batch *b);
+
+/* Host-buffer convenience: create, upload positions (NULL = the configured
+ * initial lattice), run n_sweeps, copy results and positions back, destroy. */
+int jmm_batch_run_host(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                       uint32_t n_chains, const float *x_in, uint64_t n_sweeps,
+                       jmm_chain_result *results, float *x_out);
+
+/* The Philox words of steps [block0, block0 + count) of one chain, computed
+ * on the device (4 words per step), for RNG verification tooling. */
+int jmm_rng_words(uint64_t seed, uint64_t block0, uint32_t chain, uint64_t count,
+                  uint32_t *out);
+
 const char *jmm_last_error(void);
 /* 1 when a CUDA device can be used by this library, else 0. */
 int jmm_device_available(void);

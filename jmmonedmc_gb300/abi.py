@@ -126,3 +126,119 @@ def make_params(n, ensemble=JMM_NLT, potential=JMM_POT_LJCUT, p=1.0, l=None,
     prm.seed = seed
     prm.eci = eci
     return prm
+
+
+# ---- batched form ---------------------------------------------------------
+JMM_BOUNDARY_WALLS = 0
+JMM_BOUNDARY_PERIODIC = 1
+JMM_VOLMOVE_LINEAR = 0
+JMM_VOLMOVE_LNL = 1
+JMM_VOLSCHED_RANDOM = 0
+JMM_VOLSCHED_SWEEP = 1
+JMM_PREC_FAST = 0
+JMM_PREC_EXACT = 1
+JMM_INIT_LATTICE = 0
+JMM_INIT_JITTER = 1
+
+
+class ChainDesc(C.Structure):
+    _fields_ = [
+        ("n", C.c_uint32),
+        ("potential", C.c_int32),
+        ("ensemble", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("eps", C.c_double),
+        ("sigma", C.c_double),
+        ("cutoff", C.c_double),
+        ("t", C.c_double),
+        ("p", C.c_double),
+        ("l0", C.c_double),
+        ("max_step", C.c_double),
+        ("vol_step", C.c_double),
+    ]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [
+        ("seed", C.c_uint64),
+        ("boundary", C.c_int32),
+        ("vol_move", C.c_int32),
+        ("vol_schedule", C.c_int32),
+        ("precision", C.c_int32),
+        ("resum_sweeps", C.c_uint32),
+        ("lanes_per_chain", C.c_uint32),
+        ("chains_per_block", C.c_uint32),
+        ("init", C.c_int32),
+        ("jitter", C.c_double),
+    ]
+
+
+class ChainResult(C.Structure):
+    _fields_ = [
+        ("e", C.c_double),
+        ("l", C.c_double),
+        ("steps", C.c_uint64),
+        ("samples", C.c_uint64),
+        ("sum_e", C.c_double),
+        ("sum_e2", C.c_double),
+        ("sum_l", C.c_double),
+        ("sum_l2", C.c_double),
+        ("sum_le", C.c_double),
+        ("sum_rho", C.c_double),
+        ("sum_rho2", C.c_double),
+        ("disp_acc", C.c_uint64),
+        ("disp_att", C.c_uint64),
+        ("vol_acc", C.c_uint64),
+        ("vol_att", C.c_uint64),
+        ("pair_evals", C.c_uint64),
+        ("max_drift", C.c_double),
+        ("error", C.c_uint32),
+        ("window_overflows", C.c_uint32),
+    ]
+
+
+CHAIN_RESULT_DTYPE = [
+    ("e", "<f8"), ("l", "<f8"), ("steps", "<u8"), ("samples", "<u8"),
+    ("sum_e", "<f8"), ("sum_e2", "<f8"), ("sum_l", "<f8"), ("sum_l2", "<f8"),
+    ("sum_le", "<f8"), ("sum_rho", "<f8"), ("sum_rho2", "<f8"),
+    ("disp_acc", "<u8"), ("disp_att", "<u8"), ("vol_acc", "<u8"), ("vol_att", "<u8"),
+    ("pair_evals", "<u8"), ("max_drift", "<f8"), ("error", "<u4"),
+    ("window_overflows", "<u4"),
+]
+
+
+def make_chain(n, potential=JMM_POT_LJCUT, ensemble=JMM_NLT, eps=1.0, sigma=1.0,
+               cutoff=3.0, t=1.0, p=1.0, l0=None, rho=None, max_step=0.3, vol_step=0.01):
+    d = ChainDesc()
+    d.n = n
+    d.potential = potential
+    d.ensemble = ensemble
+    d.eps = eps
+    d.sigma = sigma
+    d.cutoff = cutoff
+    d.t = t
+    d.p = p
+    if l0 is None:
+        l0 = n / (rho if rho is not None else 0.6)
+    d.l0 = l0
+    d.max_step = max_step
+    d.vol_step = vol_step
+    return d
+
+
+def make_batch_config(seed=1, boundary=JMM_BOUNDARY_WALLS, vol_move=JMM_VOLMOVE_LNL,
+                      vol_schedule=JMM_VOLSCHED_SWEEP, precision=JMM_PREC_FAST,
+                      resum_sweeps=100, lanes_per_chain=0, chains_per_block=0,
+                      init=JMM_INIT_LATTICE, jitter=0.0):
+    c = BatchConfig()
+    c.seed = seed
+    c.boundary = boundary
+    c.vol_move = vol_move
+    c.vol_schedule = vol_schedule
+    c.precision = precision
+    c.resum_sweeps = resum_sweeps
+    c.lanes_per_chain = lanes_per_chain
+    c.chains_per_block = chains_per_block
+    c.init = init
+    c.jitter = jitter
+    return c

@@ -1,0 +1,152 @@
+"""Python handle on the batched chain form (jmm_batch_* in include/jmm_gpu.h).
+
+``ChainBatch`` owns thousands of independent Metropolis chains of uneven N,
+temperature, pressure and potential that run in one persistent CUDA kernel;
+``run(n_sweeps)`` launches a CUDA graph holding that kernel.  Statistics come
+back as a numpy structured array (``CHAIN_RESULT_DTYPE``), with helpers for
+the averages the reference's analysis scripts form (scripts/Analyze_Mean.py).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _native, abi
+
+P = C.POINTER
+_native.register({
+    "jmm_batch_create": [P(abi.BatchConfig), P(abi.ChainDesc), C.c_uint32, P(C.c_void_p)],
+    "jmm_batch_run": [C.c_void_p, C.c_uint64],
+    "jmm_batch_run_async": [C.c_void_p, C.c_uint64, C.c_void_p],
+    "jmm_batch_results": [C.c_void_p, P(abi.ChainResult), C.c_uint32],
+    "jmm_batch_reset_stats": [C.c_void_p],
+    "jmm_batch_get_positions": [C.c_void_p, C.c_uint32, P(C.c_float), C.c_uint32],
+    "jmm_batch_set_positions": [C.c_void_p, C.c_uint32, P(C.c_float), C.c_uint32, C.c_double],
+    "jmm_batch_energies": [C.c_void_p, P(C.c_double), C.c_uint32],
+    "jmm_batch_device_views": [C.c_void_p, P(C.c_void_p), P(C.c_void_p), P(C.c_uint64),
+                               C.c_uint32],
+    "jmm_batch_autotune": [C.c_void_p, C.c_uint32, P(C.c_uint32), P(C.c_uint32)],
+    "jmm_batch_destroy": [C.c_void_p],
+    "jmm_batch_run_host": [P(abi.BatchConfig), P(abi.ChainDesc), C.c_uint32, P(C.c_float),
+                           C.c_uint64, P(abi.ChainResult), P(C.c_float)],
+    "jmm_rng_words": [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint64, P(C.c_uint32)],
+})
+
+
+def chain_array(chains):
+    arr = (abi.ChainDesc * len(chains))()
+    for k, c in enumerate(chains):
+        arr[k] = c
+    return arr
+
+
+def results_to_numpy(buf):
+    return np.frombuffer(buf, dtype=np.dtype(abi.CHAIN_RESULT_DTYPE)).copy()
+
+
+class ChainBatch:
+    def __init__(self, config: abi.BatchConfig, chains):
+        self.config = config
+        self.chains = list(chains)
+        self._arr = chain_array(self.chains)
+        self._h = C.c_void_p()
+        _native.call("jmm_batch_create", C.byref(config), self._arr, len(self.chains),
+                     C.byref(self._h))
+
+    @property
+    def n_chains(self):
+        return len(self.chains)
+
+    def close(self):
+        if self._h:
+            _native.load().jmm_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def run(self, n_sweeps):
+        _native.call("jmm_batch_run", self._h, n_sweeps)
+
+    def run_async(self, n_sweeps, stream=None):
+        """Enqueue on a CUDA stream handle (int, e.g. torch's cuda_stream)."""
+        _native.call("jmm_batch_run_async", self._h, n_sweeps,
+                     C.c_void_p(stream) if stream else None)
+
+    def results(self):
+        buf = (abi.ChainResult * self.n_chains)()
+        _native.call("jmm_batch_results", self._h, buf, self.n_chains)
+        return results_to_numpy(buf)
+
+    def reset_stats(self):
+        _native.call("jmm_batch_reset_stats", self._h)
+
+    def positions(self, chain):
+        n = self.chains[chain].n
+        x = np.empty(n, dtype=np.float32)
+        _native.call("jmm_batch_get_positions", self._h, chain,
+                     x.ctypes.data_as(P(C.c_float)), n)
+        return x
+
+    def set_positions(self, chain, x, l):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        _native.call("jmm_batch_set_positions", self._h, chain,
+                     x.ctypes.data_as(P(C.c_float)), x.size, float(l))
+
+    def energies(self):
+        e = np.empty(self.n_chains, dtype=np.float64)
+        _native.call("jmm_batch_energies", self._h, e.ctypes.data_as(P(C.c_double)),
+                     self.n_chains)
+        return e
+
+    def device_views(self):
+        """(positions device address, results device address, offsets)."""
+        px, pr = C.c_void_p(), C.c_void_p()
+        off = np.empty(self.n_chains, dtype=np.uint64)
+        _native.call("jmm_batch_device_views", self._h, C.byref(px), C.byref(pr),
+                     off.ctypes.data_as(P(C.c_uint64)), self.n_chains)
+        return px.value, pr.value, off
+
+    def autotune(self, trial_sweeps=4):
+        g, c = C.c_uint32(), C.c_uint32()
+        _native.call("jmm_batch_autotune", self._h, trial_sweeps, C.byref(g), C.byref(c))
+        return g.value, c.value
+
+
+def run_host(config, chains, n_sweeps, x_in=None):
+    """Create, run and read back in one call through host buffers."""
+    arr = chain_array(chains)
+    n_tot = sum(int(c.n) for c in chains)
+    res = (abi.ChainResult * len(chains))()
+    x_out = np.empty(n_tot, dtype=np.float32)
+    xin_ptr = None
+    if x_in is not None:
+        x_in = np.ascontiguousarray(x_in, dtype=np.float32)
+        xin_ptr = x_in.ctypes.data_as(P(C.c_float))
+    _native.call("jmm_batch_run_host", C.byref(config), arr, len(chains), xin_ptr, n_sweeps,
+                 res, x_out.ctypes.data_as(P(C.c_float)))
+    return results_to_numpy(res), x_out
+
+
+def rng_words(seed, block0, chain, count):
+    out = np.empty(4 * count, dtype=np.uint32)
+    _native.call("jmm_rng_words", seed, block0, chain, count,
+                 out.ctypes.data_as(P(C.c_uint32)))
+    return out.reshape(count, 4)
+
+
+def averages(res):
+    """Per-chain <E>, <E^2>, <L>, <L^2>, <LE>, <rho>, <rho^2> from the sums."""
+    s = res["samples"].astype(np.float64)
+    out = {}
+    for k in ("e", "e2", "l", "l2", "le", "rho", "rho2"):
+        out[k] = res["sum_" + k] / s
+    return out

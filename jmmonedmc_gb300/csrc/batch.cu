@@ -1,0 +1,575 @@
+// batch.cu -- host side of the batched chain kernel (jmm_batch_* in
+// include/jmm_gpu.h): validation, HBM layout, launch shapes, the CUDA graph
+// that holds a run, the launch-shape autotuner and the host-buffer entry.
+//
+// Layout: positions are FP32, chain k at a 16-byte aligned offset (user
+// order); per-chain parameters live in launch order (chains sorted by N,
+// largest first, so that a block holds chains of similar length); each block
+// stages its chains' positions in shared memory for the whole run.
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "batch_core.cuh"
+#include "common.cuh"
+
+using namespace jmm;
+using namespace jmm::batch;
+
+namespace {
+
+constexpr size_t kMaxSmem = 227 * 1024;
+
+typedef void (*ChainsKernel)(const ChainParams *, jmm_chain_result *, float *, KernelCfg);
+
+ChainsKernel pick_kernel(uint32_t g, bool exact) {
+  switch (g) {
+    case 4: return exact ? chains_kernel<4, true> : chains_kernel<4, false>;
+    case 8: return exact ? chains_kernel<8, true> : chains_kernel<8, false>;
+    case 16: return exact ? chains_kernel<16, true> : chains_kernel<16, false>;
+    case 32: return exact ? chains_kernel<32, true> : chains_kernel<32, false>;
+    default: return nullptr;
+  }
+}
+
+uint64_t pad4(uint64_t n) { return (n + 3) & ~uint64_t(3); }
+
+}  // namespace
+
+struct jmm_batch {
+  jmm_batch_config cfg;
+  uint32_t n_chains = 0;
+  std::vector<jmm_chain_desc> chains;
+  std::vector<uint64_t> x_off;  // by user index
+  std::vector<uint32_t> order;  // launch order -> user index
+  uint64_t total_floats = 0;
+  std::vector<ChainParams> params;  // launch order
+  ChainParams *d_params = nullptr;
+  jmm_chain_result *d_res = nullptr;
+  float *d_x = nullptr;
+  double *d_e = nullptr;
+  uint32_t g = 8, cpb = 4, n_blocks = 0;
+  size_t smem = 0;
+  cudaStream_t stream = nullptr;
+  std::map<uint64_t, cudaGraphExec_t> graphs;  // n_sweeps -> instantiated run
+};
+
+static void drop_graphs(jmm_batch *b) {
+  for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+}
+
+static void batch_free(jmm_batch *b) {
+  if (!b) return;
+  drop_graphs(b);
+  cudaFree(b->d_params);
+  cudaFree(b->d_res);
+  cudaFree(b->d_x);
+  cudaFree(b->d_e);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+// Per-chain kernel parameters for launch shape (g, cpb); uploads them.
+static int apply_layout(jmm_batch *b, uint32_t g, uint32_t cpb) {
+  if (!pick_kernel(g, false)) return fail(JMM_ERR_INVALID, "lanes_per_chain must be 4, 8, 16 or 32");
+  if (cpb == 0 || cpb * g > 256 || (cpb * g) % 32 != 0)
+    return fail(JMM_ERR_INVALID, "chains_per_block * lanes_per_chain must be a multiple of 32, <= 256");
+  const uint32_t w = g / 2;
+  if (b->cfg.boundary == JMM_BOUNDARY_PERIODIC) {
+    for (const auto &c : b->chains)
+      if (c.n < 2 * w + 1)
+        return fail(JMM_ERR_INVALID, "periodic chains need N >= lanes_per_chain + 1");
+  }
+  std::vector<ChainParams> prm(b->n_chains);
+  size_t smem_max = 0;
+  const uint32_t n_blocks = (b->n_chains + cpb - 1) / cpb;
+  for (uint32_t blk = 0; blk < n_blocks; ++blk) {
+    uint64_t s_off = 0;
+    for (uint32_t k = 0; k < cpb; ++k) {
+      const uint32_t slot = blk * cpb + k;
+      if (slot >= b->n_chains) break;
+      const uint32_t id = b->order[slot];
+      const jmm_chain_desc &c = b->chains[id];
+      ChainParams &P = prm[slot];
+      memset(&P, 0, sizeof(P));
+      P.id = id;
+      P.n = c.n;
+      P.pot = (uint32_t)c.potential;
+      P.ensemble = (uint32_t)c.ensemble;
+      P.steps_per_sweep = c.ensemble == JMM_NPT ? c.n + 1 : c.n;
+      P.s_off = (uint32_t)s_off;
+      P.x_off = b->x_off[id];
+      P.eps4 = c.potential == JMM_POT_LJCUT ? (float)(4.0 * c.eps) : (float)c.eps;
+      P.sigma2 = (float)(c.sigma * c.sigma);
+      P.inv_sigma2 = (float)(1.0 / (c.sigma * c.sigma));
+      P.rc2 = (float)(c.cutoff * c.cutoff);
+      P.rc = (float)c.cutoff;
+      P.beta = (float)(1.0 / c.t);
+      P.beta_d = 1.0 / c.t;
+      P.p = c.p;
+      P.two_max_step = (float)(2.0 * c.max_step);
+      P.vol_step = (float)c.vol_step;
+      s_off += pad4(c.n);
+    }
+    smem_max = std::max(smem_max, (size_t)s_off * sizeof(float));
+  }
+  if (smem_max > kMaxSmem)
+    return fail(JMM_ERR_INVALID, "a block's chains need %zu bytes of shared memory (max %zu): "
+                "lower chains_per_block", smem_max, kMaxSmem);
+  ChainsKernel kf = pick_kernel(g, b->cfg.precision == JMM_PREC_EXACT);
+  JMM_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+  JMM_CUDA(cudaMemcpy(b->d_params, prm.data(), prm.size() * sizeof(ChainParams),
+                      cudaMemcpyHostToDevice));
+  b->params.swap(prm);
+  b->g = g;
+  b->cpb = cpb;
+  b->n_blocks = n_blocks;
+  b->smem = smem_max;
+  drop_graphs(b);
+  return JMM_OK;
+}
+
+static int launch(jmm_batch *b, uint64_t n_sweeps, cudaStream_t s) {
+  KernelCfg kc;
+  kc.seed = b->cfg.seed;
+  kc.n_sweeps = n_sweeps;
+  kc.boundary = b->cfg.boundary;
+  kc.vol_move = b->cfg.vol_move;
+  kc.vol_schedule = b->cfg.vol_schedule;
+  kc.resum_sweeps = (int32_t)b->cfg.resum_sweeps;
+  kc.n_chains = b->n_chains;
+  kc.chains_per_block = b->cpb;
+  ChainsKernel kf = pick_kernel(b->g, b->cfg.precision == JMM_PREC_EXACT);
+  kf<<<b->n_blocks, b->g * b->cpb, b->smem, s>>>(b->d_params, b->d_res, b->d_x, kc);
+  JMM_CUDA(cudaGetLastError());
+  return JMM_OK;
+}
+
+static int energies(jmm_batch *b, cudaStream_t s) {
+  const uint32_t per_block = 8;
+  const uint32_t blocks = (b->n_chains + per_block - 1) / per_block;
+  if (b->cfg.precision == JMM_PREC_EXACT)
+    energies_kernel<true><<<blocks, 32 * per_block, 0, s>>>(b->d_params, b->d_x, b->d_res, b->d_e,
+                                                           b->n_chains, b->cfg.boundary);
+  else
+    energies_kernel<false><<<blocks, 32 * per_block, 0, s>>>(b->d_params, b->d_x, b->d_res, b->d_e,
+                                                            b->n_chains, b->cfg.boundary);
+  JMM_CUDA(cudaGetLastError());
+  return JMM_OK;
+}
+
+__global__ void set_energies_kernel(jmm_chain_result *res, const double *e, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) res[i].e = e[i];
+}
+
+static int validate(const jmm_batch_config *cfg, const jmm_chain_desc *chains, uint32_t n_chains) {
+  JMM_CHECK_ARG(cfg && chains && n_chains > 0, "null argument or no chains");
+  JMM_CHECK_ARG(cfg->boundary == JMM_BOUNDARY_WALLS || cfg->boundary == JMM_BOUNDARY_PERIODIC,
+                "unknown boundary");
+  JMM_CHECK_ARG(cfg->vol_move == JMM_VOLMOVE_LINEAR || cfg->vol_move == JMM_VOLMOVE_LNL,
+                "unknown volume move");
+  JMM_CHECK_ARG(cfg->vol_schedule == JMM_VOLSCHED_RANDOM || cfg->vol_schedule == JMM_VOLSCHED_SWEEP,
+                "unknown volume schedule");
+  JMM_CHECK_ARG(cfg->precision == JMM_PREC_FAST || cfg->precision == JMM_PREC_EXACT,
+                "unknown precision");
+  for (uint32_t k = 0; k < n_chains; ++k) {
+    const jmm_chain_desc &c = chains[k];
+    if (c.n < 2 || c.n > 16384)
+      return fail(JMM_ERR_INVALID, "chain %u: N must be in [2, 16384]", k);
+    if (c.potential != JMM_POT_LJCUT && c.potential != JMM_POT_SOFTSPHERE &&
+        c.potential != JMM_POT_GAUSS)
+      return fail(JMM_ERR_INVALID, "chain %u: potential must be LJcut, soft sphere or Gaussian", k);
+    if (c.ensemble != JMM_NLT && c.ensemble != JMM_NPT)
+      return fail(JMM_ERR_INVALID, "chain %u: unknown ensemble", k);
+    if (!(c.t > 0) || !(c.l0 > 0) || !(c.sigma > 0) || !(c.cutoff > 0) || !(c.max_step > 0))
+      return fail(JMM_ERR_INVALID, "chain %u: T, L, sigma, cut-off and step must be positive", k);
+    if (cfg->boundary == JMM_BOUNDARY_PERIODIC && !(c.l0 > 2 * c.cutoff))
+      return fail(JMM_ERR_INVALID, "chain %u: a periodic ring needs L > 2 cut-off", k);
+    const double spacing = c.l0 / c.n;
+    if (cfg->init == JMM_INIT_JITTER && !(cfg->jitter >= 0 && cfg->jitter < 0.5 * spacing))
+      return fail(JMM_ERR_INVALID, "chain %u: jitter must be below half the lattice spacing", k);
+  }
+  return JMM_OK;
+}
+
+// Lattice r_i = ((i+0.5)/N - 0.5) L (src/jmmMCState.cpp:559-562), plus the
+// optional jitter from Philox blocks (2^63 + i) of the chain's stream.
+static void initial_positions(const jmm_batch_config *cfg, const jmm_chain_desc &c, uint32_t id,
+                              float *x) {
+  for (uint32_t i = 0; i < c.n; ++i) {
+    double r = ((i + 0.5) / c.n - 0.5) * c.l0;
+    if (cfg->init == JMM_INIT_JITTER) {
+      const Words4 w = step_words(cfg->seed, (1ull << 63) | i, id);
+      r += cfg->jitter * (2.0 * word_to_unit(w.w[0]) - 1.0);
+    }
+    x[i] = (float)r;
+  }
+}
+
+extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                                uint32_t n_chains, jmm_batch **out) {
+  clear_error();
+  JMM_CHECK_ARG(out, "null output");
+  *out = nullptr;
+  int rc = validate(cfg, chains, n_chains);
+  if (rc) return rc;
+  if (!jmm_device_available()) return fail(JMM_ERR_CUDA, "jmm_batch_create: no CUDA device");
+  jmm_batch *b = new (std::nothrow) jmm_batch();
+  if (!b) return fail(JMM_ERR_NOMEM, "jmm_batch_create: host allocation failed");
+  b->cfg = *cfg;
+  b->n_chains = n_chains;
+  b->chains.assign(chains, chains + n_chains);
+  b->x_off.resize(n_chains);
+  uint64_t off = 0;
+  for (uint32_t k = 0; k < n_chains; ++k) {
+    b->x_off[k] = off;
+    off += pad4(chains[k].n);
+  }
+  b->total_floats = off;
+  b->order.resize(n_chains);
+  std::iota(b->order.begin(), b->order.end(), 0u);
+  std::stable_sort(b->order.begin(), b->order.end(),
+                   [&](uint32_t a, uint32_t c) { return chains[a].n > chains[c].n; });
+
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_params, n_chains * sizeof(ChainParams));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_res, n_chains * sizeof(jmm_chain_result));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_x, b->total_floats * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_e, n_chains * sizeof(double));
+  if (e != cudaSuccess) {
+    rc = cuda_status(e, "jmm_batch_create allocation", __FILE__, __LINE__);
+    batch_free(b);
+    return rc;
+  }
+  std::vector<float> x(b->total_floats, 0.0f);
+  std::vector<jmm_chain_result> res(n_chains);
+  for (uint32_t k = 0; k < n_chains; ++k) {
+    initial_positions(cfg, chains[k], k, x.data() + b->x_off[k]);
+    memset(&res[k], 0, sizeof(jmm_chain_result));
+    res[k].l = chains[k].l0;
+  }
+  e = cudaMemcpy(b->d_x, x.data(), x.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_res, res.data(), res.size() * sizeof(jmm_chain_result),
+                   cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    rc = cuda_status(e, "jmm_batch_create upload", __FILE__, __LINE__);
+    batch_free(b);
+    return rc;
+  }
+  const uint32_t g = cfg->lanes_per_chain ? cfg->lanes_per_chain : 8;
+  const uint32_t cpb = cfg->chains_per_block ? cfg->chains_per_block : 128 / g;
+  rc = apply_layout(b, g, cpb);
+  if (rc == JMM_OK) rc = energies(b, b->stream);
+  if (rc == JMM_OK) {
+    set_energies_kernel<<<(n_chains + 255) / 256, 256, 0, b->stream>>>(b->d_res, b->d_e, n_chains);
+    e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) rc = cuda_status(e, "jmm_batch_create energies", __FILE__, __LINE__);
+  }
+  if (rc) {
+    batch_free(b);
+    return rc;
+  }
+  *out = b;
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_destroy(jmm_batch *b) {
+  batch_free(b);
+  return JMM_OK;
+}
+
+static int graph_for(jmm_batch *b, uint64_t n_sweeps, cudaGraphExec_t *exec) {
+  auto it = b->graphs.find(n_sweeps);
+  if (it != b->graphs.end()) {
+    *exec = it->second;
+    return JMM_OK;
+  }
+  cudaGraph_t graph;
+  JMM_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = launch(b, n_sweeps, b->stream);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+  e = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+  b->graphs[n_sweeps] = *exec;
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_run_async(jmm_batch *b, uint64_t n_sweeps, void *stream) {
+  clear_error();
+  JMM_CHECK_ARG(b, "null handle");
+  if (n_sweeps == 0) return JMM_OK;
+  cudaGraphExec_t exec;
+  int rc = graph_for(b, n_sweeps, &exec);
+  if (rc) return rc;
+  JMM_CUDA(cudaGraphLaunch(exec, stream ? (cudaStream_t)stream : b->stream));
+  return JMM_OK;
+}
+
+static int check_errors(jmm_batch *b) {
+  std::vector<jmm_chain_result> res(b->n_chains);
+  JMM_CUDA(cudaMemcpy(res.data(), b->d_res, res.size() * sizeof(jmm_chain_result),
+                      cudaMemcpyDeviceToHost));
+  for (uint32_t k = 0; k < b->n_chains; ++k)
+    if (res[k].error)
+      return fail((int)res[k].error, "chain %u reported error %u (energy %g)", k, res[k].error,
+                  res[k].e);
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_run(jmm_batch *b, uint64_t n_sweeps) {
+  int rc = jmm_batch_run_async(b, n_sweeps, nullptr);
+  if (rc) return rc;
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  return check_errors(b);
+}
+
+extern "C" int jmm_batch_results(jmm_batch *b, jmm_chain_result *out, uint32_t n_chains) {
+  clear_error();
+  JMM_CHECK_ARG(b && out, "null argument");
+  JMM_CHECK_ARG(n_chains == b->n_chains, "n_chains does not match the batch");
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  JMM_CUDA(cudaMemcpy(out, b->d_res, n_chains * sizeof(jmm_chain_result), cudaMemcpyDeviceToHost));
+  return JMM_OK;
+}
+
+__global__ void reset_stats_kernel(jmm_chain_result *res, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  jmm_chain_result r = res[i];
+  r.samples = 0;
+  r.sum_e = r.sum_e2 = r.sum_l = r.sum_l2 = r.sum_le = r.sum_rho = r.sum_rho2 = 0.0;
+  r.disp_acc = r.disp_att = r.vol_acc = r.vol_att = 0;
+  r.pair_evals = 0;
+  r.max_drift = 0.0;
+  r.window_overflows = 0;
+  res[i] = r;
+}
+
+extern "C" int jmm_batch_reset_stats(jmm_batch *b) {
+  clear_error();
+  JMM_CHECK_ARG(b, "null handle");
+  reset_stats_kernel<<<(b->n_chains + 255) / 256, 256, 0, b->stream>>>(b->d_res, b->n_chains);
+  JMM_CUDA(cudaGetLastError());
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_get_positions(jmm_batch *b, uint32_t chain, float *x, uint32_t n) {
+  clear_error();
+  JMM_CHECK_ARG(b && x, "null argument");
+  JMM_CHECK_ARG(chain < b->n_chains, "chain index out of range");
+  JMM_CHECK_ARG(n == b->chains[chain].n, "N does not match the chain");
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  JMM_CUDA(cudaMemcpy(x, b->d_x + b->x_off[chain], n * sizeof(float), cudaMemcpyDeviceToHost));
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_set_positions(jmm_batch *b, uint32_t chain, const float *x, uint32_t n,
+                                       double l) {
+  clear_error();
+  JMM_CHECK_ARG(b && x, "null argument");
+  JMM_CHECK_ARG(chain < b->n_chains, "chain index out of range");
+  JMM_CHECK_ARG(n == b->chains[chain].n, "N does not match the chain");
+  JMM_CHECK_ARG(l > 0, "box length must be positive");
+  const bool periodic = b->cfg.boundary == JMM_BOUNDARY_PERIODIC;
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!(x[i] == x[i]) || (i > 0 && !(x[i] > x[i - 1])))
+      return fail(JMM_ERR_INVALID, "positions must be finite and strictly increasing");
+    if (!periodic && !(fabs((double)x[i]) <= 0.5 * l))
+      return fail(JMM_ERR_INVALID, "position %u lies beyond the walls at +-L/2", i);
+  }
+  if (periodic && !(x[n - 1] < x[0] + l))
+    return fail(JMM_ERR_INVALID, "periodic positions must span less than L");
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  JMM_CUDA(cudaMemcpy(b->d_x + b->x_off[chain], x, n * sizeof(float), cudaMemcpyHostToDevice));
+  jmm_chain_result r;
+  JMM_CUDA(cudaMemcpy(&r, b->d_res + chain, sizeof(r), cudaMemcpyDeviceToHost));
+  r.l = l;
+  JMM_CUDA(cudaMemcpy(b->d_res + chain, &r, sizeof(r), cudaMemcpyHostToDevice));
+  int rc = energies(b, b->stream);
+  if (rc) return rc;
+  double e;
+  JMM_CUDA(cudaMemcpyAsync(&e, b->d_e + chain, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  r.e = e;
+  JMM_CUDA(cudaMemcpy(b->d_res + chain, &r, sizeof(r), cudaMemcpyHostToDevice));
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_energies(jmm_batch *b, double *e, uint32_t n_chains) {
+  clear_error();
+  JMM_CHECK_ARG(b && e, "null argument");
+  JMM_CHECK_ARG(n_chains == b->n_chains, "n_chains does not match the batch");
+  int rc = energies(b, b->stream);
+  if (rc) return rc;
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  JMM_CUDA(cudaMemcpy(e, b->d_e, n_chains * sizeof(double), cudaMemcpyDeviceToHost));
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_device_views(jmm_batch *b, void **positions, void **results,
+                                      uint64_t *offsets, uint32_t n_chains) {
+  clear_error();
+  JMM_CHECK_ARG(b, "null handle");
+  if (positions) *positions = b->d_x;
+  if (results) *results = b->d_res;
+  if (offsets) {
+    JMM_CHECK_ARG(n_chains == b->n_chains, "n_chains does not match the batch");
+    memcpy(offsets, b->x_off.data(), n_chains * sizeof(uint64_t));
+  }
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t *lanes_out,
+                                  uint32_t *cpb_out) {
+  clear_error();
+  JMM_CHECK_ARG(b, "null handle");
+  if (trial_sweeps == 0) trial_sweeps = 4;
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  float *x_save = nullptr;
+  jmm_chain_result *r_save = nullptr;
+  JMM_CUDA(cudaMalloc((void **)&x_save, b->total_floats * sizeof(float)));
+  cudaError_t e = cudaMalloc((void **)&r_save, b->n_chains * sizeof(jmm_chain_result));
+  if (e != cudaSuccess) {
+    cudaFree(x_save);
+    return cuda_status(e, "autotune cudaMalloc", __FILE__, __LINE__);
+  }
+  cudaMemcpy(x_save, b->d_x, b->total_floats * sizeof(float), cudaMemcpyDeviceToDevice);
+  cudaMemcpy(r_save, b->d_res, b->n_chains * sizeof(jmm_chain_result), cudaMemcpyDeviceToDevice);
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  const uint32_t g0 = b->g, c0 = b->cpb;
+  float best = 1e30f;
+  uint32_t best_g = g0, best_c = c0;
+  int rc = JMM_OK;
+  for (uint32_t g : {4u, 8u, 16u, 32u}) {
+    for (uint32_t threads : {32u, 64u, 128u, 256u}) {
+      const uint32_t cpb = threads / g;
+      if (cpb == 0) continue;
+      if (apply_layout(b, g, cpb) != JMM_OK) {
+        clear_error();
+        continue;
+      }
+      float ms = 0.0f;
+      for (int rep = 0; rep < 2; ++rep) {  // first run warms the code path
+        cudaMemcpyAsync(b->d_x, x_save, b->total_floats * sizeof(float), cudaMemcpyDeviceToDevice,
+                        b->stream);
+        cudaMemcpyAsync(b->d_res, r_save, b->n_chains * sizeof(jmm_chain_result),
+                        cudaMemcpyDeviceToDevice, b->stream);
+        cudaEventRecord(t0, b->stream);
+        rc = launch(b, trial_sweeps, b->stream);
+        cudaEventRecord(t1, b->stream);
+        if (rc) break;
+        cudaEventSynchronize(t1);
+        cudaEventElapsedTime(&ms, t0, t1);
+      }
+      if (rc) break;
+      if (ms < best) {
+        best = ms;
+        best_g = g;
+        best_c = cpb;
+      }
+    }
+    if (rc) break;
+  }
+  cudaMemcpy(b->d_x, x_save, b->total_floats * sizeof(float), cudaMemcpyDeviceToDevice);
+  cudaMemcpy(b->d_res, r_save, b->n_chains * sizeof(jmm_chain_result), cudaMemcpyDeviceToDevice);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaFree(x_save);
+  cudaFree(r_save);
+  if (rc) return rc;
+  rc = apply_layout(b, best_g, best_c);
+  if (rc) return rc;
+  b->cfg.lanes_per_chain = best_g;
+  b->cfg.chains_per_block = best_c;
+  if (lanes_out) *lanes_out = best_g;
+  if (cpb_out) *cpb_out = best_c;
+  JMM_CUDA(cudaDeviceSynchronize());
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_run_host(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                                  uint32_t n_chains, const float *x_in, uint64_t n_sweeps,
+                                  jmm_chain_result *results, float *x_out) {
+  jmm_batch *b = nullptr;
+  int rc = jmm_batch_create(cfg, chains, n_chains, &b);
+  if (rc) return rc;
+  if (x_in) {
+    std::vector<float> staged(b->total_floats, 0.0f);
+    uint64_t src = 0;
+    for (uint32_t k = 0; k < n_chains; ++k) {
+      memcpy(staged.data() + b->x_off[k], x_in + src, chains[k].n * sizeof(float));
+      src += chains[k].n;
+    }
+    cudaError_t e = cudaMemcpy(b->d_x, staged.data(), staged.size() * sizeof(float),
+                               cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      batch_free(b);
+      return cuda_status(e, "jmm_batch_run_host upload", __FILE__, __LINE__);
+    }
+    rc = energies(b, b->stream);
+    if (rc == JMM_OK)
+      set_energies_kernel<<<(n_chains + 255) / 256, 256, 0, b->stream>>>(b->d_res, b->d_e,
+                                                                          n_chains);
+  }
+  if (rc == JMM_OK) rc = jmm_batch_run(b, n_sweeps);
+  if (rc == JMM_OK && results) rc = jmm_batch_results(b, results, n_chains);
+  if (rc == JMM_OK && x_out) {
+    std::vector<float> staged(b->total_floats);
+    cudaError_t e = cudaMemcpy(staged.data(), b->d_x, staged.size() * sizeof(float),
+                               cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      rc = cuda_status(e, "jmm_batch_run_host download", __FILE__, __LINE__);
+    } else {
+      uint64_t dst = 0;
+      for (uint32_t k = 0; k < n_chains; ++k) {
+        memcpy(x_out + dst, staged.data() + b->x_off[k], chains[k].n * sizeof(float));
+        dst += chains[k].n;
+      }
+    }
+  }
+  batch_free(b);
+  return rc;
+}
+
+__global__ void rng_words_kernel(uint64_t seed, uint64_t block0, uint32_t chain, uint64_t count,
+                                 uint32_t *out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const Words4 w = step_words(seed, block0 + i, chain);
+    out[4 * i + 0] = w.w[0];
+    out[4 * i + 1] = w.w[1];
+    out[4 * i + 2] = w.w[2];
+    out[4 * i + 3] = w.w[3];
+  }
+}
+
+extern "C" int jmm_rng_words(uint64_t seed, uint64_t block0, uint32_t chain, uint64_t count,
+                             uint32_t *out) {
+  clear_error();
+  JMM_CHECK_ARG(out || count == 0, "null output");
+  if (count == 0) return JMM_OK;
+  if (!jmm_device_available()) return fail(JMM_ERR_CUDA, "jmm_rng_words: no CUDA device");
+  uint32_t *d = nullptr;
+  JMM_CUDA(cudaMalloc((void **)&d, count * 4 * sizeof(uint32_t)));
+  const uint64_t blocks64 = (count + 255) / 256;
+  const int blocks = (int)(blocks64 < 4096 ? blocks64 : 4096);
+  rng_words_kernel<<<blocks, 256>>>(seed, block0, chain, count, d);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(out, d, count * 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_status(e, "jmm_rng_words", __FILE__, __LINE__);
+  return JMM_OK;
+}

@@ -31,4 +31,20 @@ void jmmo_plain_destroy(jmmo_plain *h);
 void jmmo_philox_raw(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 void jmmo_step_words_export(uint64_t seed, uint64_t block, uint32_t chain, uint32_t out[4]);
 
+typedef struct jmmo_batch jmmo_batch;
+
+jmmo_batch *jmmo_batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                              uint32_t n_chains, int fp64);
+void jmmo_batch_destroy(jmmo_batch *b);
+int jmmo_batch_run(jmmo_batch *b, uint64_t n_sweeps);
+int jmmo_batch_run_chain(jmmo_batch *b, uint32_t chain, uint64_t n_sweeps);
+int jmmo_batch_results(jmmo_batch *b, jmm_chain_result *out, uint32_t n_chains);
+int jmmo_batch_get_positions(jmmo_batch *b, uint32_t chain, double *x, uint32_t n);
+int jmmo_batch_set_positions(jmmo_batch *b, uint32_t chain, const double *x, uint32_t n,
+                             double l);
+int jmmo_batch_energies(jmmo_batch *b, double *e, uint32_t n_chains);
+double jmmo_energy64(const jmm_chain_desc *c, const double *x, double l, int periodic);
+float jmmo_portable_logf(float x);
+float jmmo_portable_expf(float x);
+
 #endif

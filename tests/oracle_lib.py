@@ -160,3 +160,82 @@ def step_words(seed, block, chain=0):
     o = (u32 * 4)()
     lib.jmmo_step_words_export(seed, block, chain, o)
     return list(o)
+
+
+# ---- batched form ----------------------------------------------------------
+extra_sigs({
+    "jmmo_batch_create": ([P(abi.BatchConfig), P(abi.ChainDesc), u32, C.c_int], vp),
+    "jmmo_batch_destroy": ([vp], None),
+    "jmmo_batch_run": ([vp, u64], C.c_int),
+    "jmmo_batch_run_chain": ([vp, u32, u64], C.c_int),
+    "jmmo_batch_results": ([vp, P(abi.ChainResult), u32], C.c_int),
+    "jmmo_batch_get_positions": ([vp, u32, P(dbl), u32], C.c_int),
+    "jmmo_batch_set_positions": ([vp, u32, P(dbl), u32, dbl], C.c_int),
+    "jmmo_batch_energies": ([vp, P(dbl), u32], C.c_int),
+    "jmmo_energy64": ([P(abi.ChainDesc), P(dbl), dbl, C.c_int], dbl),
+    "jmmo_portable_logf": ([C.c_float], C.c_float),
+    "jmmo_portable_expf": ([C.c_float], C.c_float),
+})
+
+
+class OracleBatch:
+    """CPU restatement of jmm_batch_*: fp64=False replays the EXACT kernel."""
+
+    def __init__(self, config, chains, fp64=False):
+        from jmmonedmc_gb300.batch import chain_array
+        self.lib = load()
+        self.chains = list(chains)
+        self._arr = chain_array(self.chains)
+        self._h = self.lib.jmmo_batch_create(C.byref(config), self._arr, len(self.chains),
+                                             1 if fp64 else 0)
+        if not self._h:
+            raise ValueError("jmmo_batch_create failed")
+
+    @property
+    def n_chains(self):
+        return len(self.chains)
+
+    def close(self):
+        if self._h:
+            self.lib.jmmo_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def run(self, n_sweeps):
+        _ok(self.lib.jmmo_batch_run(self._h, n_sweeps), "batch_run")
+
+    def run_chain(self, chain, n_sweeps):
+        _ok(self.lib.jmmo_batch_run_chain(self._h, chain, n_sweeps), "batch_run_chain")
+
+    def results(self):
+        from jmmonedmc_gb300.batch import results_to_numpy
+        buf = (abi.ChainResult * self.n_chains)()
+        _ok(self.lib.jmmo_batch_results(self._h, buf, self.n_chains), "batch_results")
+        return results_to_numpy(buf)
+
+    def positions(self, chain):
+        n = self.chains[chain].n
+        x = np.empty(n, dtype=np.float64)
+        _ok(self.lib.jmmo_batch_get_positions(self._h, chain, x.ctypes.data_as(P(dbl)), n),
+            "batch_get_positions")
+        return x
+
+    def set_positions(self, chain, x, l):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        _ok(self.lib.jmmo_batch_set_positions(self._h, chain, x.ctypes.data_as(P(dbl)), x.size,
+                                              float(l)), "batch_set_positions")
+
+    def energies(self):
+        e = np.empty(self.n_chains, dtype=np.float64)
+        _ok(self.lib.jmmo_batch_energies(self._h, e.ctypes.data_as(P(dbl)), self.n_chains),
+            "batch_energies")
+        return e
+
+
+def energy64(chain_desc, x, l, periodic=False):
+    lib = load()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    return lib.jmmo_energy64(C.byref(chain_desc), x.ctypes.data_as(P(dbl)), float(l),
+                             1 if periodic else 0)

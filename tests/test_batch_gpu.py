@@ -1,0 +1,168 @@
+"""Parity of the batched chain kernel (jmm_batch_*) with the oracle.
+
+* EXACT precision: every field of every chain's result, and every position,
+  equals the oracle's FP32 replay bit for bit, across boundaries, ensembles,
+  volume moves, schedules, potentials, uneven N and lane counts, over several
+  launches.
+* FAST precision (hardware reciprocal/exp, the production mode): energies of
+  the GPU's configurations agree with the FP64 oracle to 1e-6 relative
+  (fresh sums) and 1e-5 relative (running totals, which carry the FP32 drift
+  since the last re-summation); short trajectories track the FP64 chain.
+"""
+import numpy as np
+import pytest
+
+from jmmonedmc_gb300 import abi
+from jmmonedmc_gb300.batch import ChainBatch, rng_words, run_host
+from tests import oracle_lib
+
+pytestmark = pytest.mark.gpu
+
+RESULT_FIELDS = [f for f, _ in abi.CHAIN_RESULT_DTYPE]
+
+
+def _mixed_chains(rng, n_chains, nmin, nmax, ensemble=None, pots=(abi.JMM_POT_LJCUT,)):
+    chains = []
+    for k in range(n_chains):
+        n = int(rng.integers(nmin, nmax + 1))
+        pot = pots[k % len(pots)]
+        cutoff = {abi.JMM_POT_LJCUT: 3.0, abi.JMM_POT_SOFTSPHERE: 2.5, abi.JMM_POT_GAUSS: 4.0}[pot]
+        ens = ensemble if ensemble is not None else (abi.JMM_NPT if k % 2 else abi.JMM_NLT)
+        rho = float(rng.uniform(0.3, 0.9))
+        chains.append(abi.make_chain(n, potential=pot, ensemble=ens, cutoff=cutoff,
+                                     t=float(rng.uniform(0.5, 2.0)),
+                                     p=float(rng.uniform(0.5, 2.0)), rho=rho,
+                                     max_step=0.3, vol_step=0.02))
+    return chains
+
+
+def _assert_same(gpu, ora, chains):
+    rg, ro = gpu.results(), ora.results()
+    for f in RESULT_FIELDS:
+        a, b = rg[f], ro[f]
+        if a.dtype.kind == "f":
+            bad = np.nonzero(a.view(np.uint64) != b.view(np.uint64))[0]
+        else:
+            bad = np.nonzero(a != b)[0]
+        assert bad.size == 0, f"{f} differs for chains {bad[:8]}: gpu {a[bad[:3]]} oracle {b[bad[:3]]}"
+    for k in range(len(chains)):
+        xg = gpu.positions(k).astype(np.float64)
+        xo = ora.positions(k)
+        assert np.array_equal(xg, xo), f"positions of chain {k} differ"
+
+
+EXACT_CASES = {
+    "npt256_lnl_sweep_walls": dict(cfg=dict(vol_move=abi.JMM_VOLMOVE_LNL,
+                                            vol_schedule=abi.JMM_VOLSCHED_SWEEP),
+                                   n=(256, 256), ens=abi.JMM_NPT),
+    "mixed_random_linear": dict(cfg=dict(vol_move=abi.JMM_VOLMOVE_LINEAR,
+                                         vol_schedule=abi.JMM_VOLSCHED_RANDOM),
+                                n=(32, 300), ens=None),
+    "periodic_mixed_pots": dict(cfg=dict(boundary=abi.JMM_BOUNDARY_PERIODIC, resum_sweeps=3),
+                                n=(40, 200), ens=None,
+                                pots=(abi.JMM_POT_LJCUT, abi.JMM_POT_SOFTSPHERE, abi.JMM_POT_GAUSS)),
+    "nvt_gauss_dense": dict(cfg=dict(resum_sweeps=2), n=(64, 128), ens=abi.JMM_NLT,
+                            pots=(abi.JMM_POT_GAUSS,)),
+}
+
+
+@pytest.mark.parametrize("lanes", [4, 8, 16, 32])
+@pytest.mark.parametrize("case", sorted(EXACT_CASES))
+def test_batch_exact_matches_oracle(gpu, case, lanes):
+    spec = EXACT_CASES[case]
+    rng = np.random.default_rng(abs(hash(case)) % (2 ** 32))
+    chains = _mixed_chains(rng, 24, *spec["n"], ensemble=spec["ens"],
+                           pots=spec.get("pots", (abi.JMM_POT_LJCUT,)))
+    cfg = abi.make_batch_config(seed=11, precision=abi.JMM_PREC_EXACT, lanes_per_chain=lanes,
+                                init=abi.JMM_INIT_JITTER, jitter=0.05, **spec["cfg"])
+    gpu = ChainBatch(cfg, chains)
+    ora = oracle_lib.OracleBatch(cfg, chains)
+    _assert_same(gpu, ora, chains)  # initial lattice and energies
+    for sweeps in (1, 7, 30):
+        gpu.run(sweeps)
+        ora.run(sweeps)
+        _assert_same(gpu, ora, chains)
+
+
+def test_batch_rng_words_match_oracle(gpu):
+    got = rng_words(0xDEADBEEF12345, 1, 77, 1000)
+    for i in (0, 1, 500, 999):
+        assert list(got[i]) == oracle_lib.step_words(0xDEADBEEF12345, 1 + i, 77)
+
+
+def test_batch_fast_energies_within_tolerance(gpu):
+    rng = np.random.default_rng(5)
+    chains = _mixed_chains(rng, 64, 64, 512,
+                           pots=(abi.JMM_POT_LJCUT, abi.JMM_POT_SOFTSPHERE, abi.JMM_POT_GAUSS))
+    cfg = abi.make_batch_config(seed=2, precision=abi.JMM_PREC_FAST, resum_sweeps=20)
+    gpu = ChainBatch(cfg, chains)
+    gpu.run(60)
+    res = gpu.results()
+    assert np.all(res["error"] == 0)
+    fresh = gpu.energies()
+    for k, c in enumerate(chains):
+        x = gpu.positions(k).astype(np.float64)
+        e64 = oracle_lib.energy64(c, x, res["l"][k])
+        scale = max(1.0, abs(e64))
+        assert abs(fresh[k] - e64) <= 1e-6 * scale, (k, fresh[k], e64)
+        assert abs(res["e"][k] - e64) <= 1e-5 * scale, (k, res["e"][k], e64)
+        assert np.all(np.diff(x) > 0), "particles must stay ordered"
+        assert np.all(np.abs(x) <= res["l"][k] / 2 + 1e-4)
+
+
+def test_batch_fast_tracks_fp64_chain(gpu):
+    """For a few sweeps, FAST decisions coincide with the FP64 chain's for
+    nearly every chain (they part only where an FP32 rounding flips a
+    near-tie decision)."""
+    rng = np.random.default_rng(9)
+    chains = _mixed_chains(rng, 128, 64, 64, ensemble=abi.JMM_NPT)
+    cfg = abi.make_batch_config(seed=4, precision=abi.JMM_PREC_FAST)
+    gpu = ChainBatch(cfg, chains)
+    ora = oracle_lib.OracleBatch(cfg, chains, fp64=True)
+    gpu.run(5)
+    ora.run(5)
+    rg, ro = gpu.results(), ora.results()
+    same = (rg["disp_acc"] == ro["disp_acc"]) & (rg["vol_acc"] == ro["vol_acc"])
+    assert same.mean() >= 0.95, same.mean()
+    np.testing.assert_allclose(rg["e"][same], ro["e"][same], rtol=1e-5, atol=1e-4)
+
+
+def test_batch_host_entry_matches_device_run(gpu):
+    chains = [abi.make_chain(100, ensemble=abi.JMM_NPT, t=1.2, p=0.8)]
+    cfg = abi.make_batch_config(seed=8, precision=abi.JMM_PREC_EXACT)
+    res_h, x_h = run_host(cfg, chains, 20)
+    gpu = ChainBatch(cfg, chains)
+    gpu.run(20)
+    res_d = gpu.results()
+    assert res_h["e"][0] == res_d["e"][0] and res_h["sum_e"][0] == res_d["sum_e"][0]
+    assert np.array_equal(x_h, gpu.positions(0))
+
+
+def test_batch_autotune_keeps_state(gpu):
+    rng = np.random.default_rng(1)
+    chains = _mixed_chains(rng, 40, 64, 128, ensemble=abi.JMM_NPT)
+    cfg = abi.make_batch_config(seed=6, precision=abi.JMM_PREC_EXACT)
+    gpu = ChainBatch(cfg, chains)
+    before = gpu.results()
+    g, c = gpu.autotune(trial_sweeps=2)
+    assert g in (4, 8, 16, 32) and c * g in (32, 64, 128, 256)
+    after = gpu.results()
+    assert np.array_equal(before["e"], after["e"]) and np.array_equal(before["steps"], after["steps"])
+    # the EXACT result does not depend on the block shape, only on the lanes
+    cfg2 = abi.make_batch_config(seed=6, precision=abi.JMM_PREC_EXACT, lanes_per_chain=g)
+    ora = oracle_lib.OracleBatch(cfg2, chains)
+    gpu.run(5)
+    ora.run(5)
+    _assert_same(gpu, ora, chains)
+
+
+def test_batch_rejects_bad_input(gpu):
+    from jmmonedmc_gb300._native import JmmError
+    with pytest.raises(JmmError):
+        ChainBatch(abi.make_batch_config(), [abi.make_chain(1)])
+    with pytest.raises(JmmError):
+        ChainBatch(abi.make_batch_config(boundary=abi.JMM_BOUNDARY_PERIODIC),
+                   [abi.make_chain(16, cutoff=3.0, l0=5.0)])
+    b = ChainBatch(abi.make_batch_config(), [abi.make_chain(16)])
+    with pytest.raises(JmmError):
+        b.set_positions(0, np.linspace(1, -1, 16), 30.0)  # not increasing
