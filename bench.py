@@ -1,0 +1,432 @@
+#!/usr/bin/env python
+"""Benchmark: attempted Monte Carlo moves per second on one GB300.
+
+Workload (the batched NPT configuration): 4096 independent chains of N = 256
+Lennard-Jones 12-6 particles (eps = sigma = 1, cut-off 3 sigma, hard walls),
+T log-spaced over 0.5-2.0, P uniform over 0.5-2.0 per chain, ln L volume
+moves (delta = 0.01) closing every sweep of N displacement moves (maximum
+displacement 0.3 sigma), starting from the lattice at rho = 0.6; FP32 pair
+energies, FP64 totals and accumulators.  Inputs are synthetic and seeded.
+
+One bench step = one CUDA-graph launch of the persistent chain kernel over
+all chains for --sweeps-per-step sweeps (default 1000, so the default 10
+timed steps are the configuration's full 10^4 sweeps).  Every attempted
+move (displacement or volume) counts.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's own algorithm for the same chains
+(the plain FP64 single-chain loop: O(N) displacement with per-pair state,
+O(N^2) volume move) on the host cores, one chain per core.
+Prints exactly one JSON line (rank 0).
+"""
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+METRIC = "attempted MC moves/s (batched chains, FP32 pairs / FP64 totals)"
+UNIT = "moves/s"
+FLOP_PER_PAIR = 9  # d, r^2, inv2 scale, inv6 (2), inv6-1, products (2), select
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--sweeps-per-step", type=int, default=1000)
+    ap.add_argument("--chains", type=int, default=4096)
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=1.5,
+                    help="wall seconds per host core for the CPU baseline sample")
+    ap.add_argument("--no-autotune", action="store_true")
+    return ap.parse_args()
+
+
+def workload(args, rank=0):
+    """Chain descriptions of the batched NPT workload (rank-shifted seed)."""
+    from jmmonedmc_gb300 import abi
+    from jmmonedmc_gb300.philox_host import uniforms
+    n_ch = args.chains
+    seed = args.seed + 1000003 * rank
+    temps = [0.5 * 4.0 ** (c / max(1, n_ch - 1)) for c in range(n_ch)]
+    press = [0.5 + 1.5 * u for u in uniforms(seed, n_ch, stream=0xB0)]
+    chains = [abi.make_chain(args.n, potential=abi.JMM_POT_LJCUT, ensemble=abi.JMM_NPT,
+                             eps=1.0, sigma=1.0, cutoff=3.0, t=temps[c], p=press[c],
+                             rho=0.6, max_step=0.3, vol_step=0.01) for c in range(n_ch)]
+    cfg = abi.make_batch_config(seed=seed, vol_move=abi.JMM_VOLMOVE_LNL,
+                                vol_schedule=abi.JMM_VOLSCHED_SWEEP,
+                                precision=abi.JMM_PREC_FAST)
+    return cfg, chains
+
+
+def config_dict(args, extra=None):
+    d = {
+        "workload": (f"batched NPT: {args.chains} chains x N={args.n}, LJ 12-6 eps=sigma=1 rc=3, "
+                     "hard walls, T log-spaced 0.5-2.0, P U(0.5,2.0), ln L moves delta=0.01 "
+                     "once per sweep, max displacement 0.3, start rho=0.6 lattice"),
+        "chains": args.chains,
+        "particles_per_chain": args.n,
+        "sweeps_per_step": args.sweeps_per_step,
+        "moves_per_sweep": args.n + 1,
+        "l2": "flushed between timed steps (256 MiB device write); inputs 4 MiB < L2",
+        "precision": "FP32 pair energies, FP64 running totals and accumulators",
+    }
+    if extra:
+        d.update(extra)
+    return d
+
+
+# ---- clocks ------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.idx = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                    power.append(float(parts[3]))
+                except ValueError:
+                    continue
+                for name, val in zip(names, parts[5:9]):
+                    if val.lower().startswith("active"):
+                        reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+# ---- CPU baseline: the reference's algorithm on the host cores -------------
+
+def _cpu_worker(job):
+    """One host core: the reference's chain (plain FP64, pair-state arrays)
+    for the workload's chain `k`, run for `seconds` wall seconds."""
+    k, n, t, p, seed, seconds, repo = job
+    sys.path.insert(0, repo)
+    from jmmonedmc_gb300 import abi
+    from tests import oracle_lib
+    params = abi.make_params(n=n, ensemble=abi.JMM_NPT, potential=abi.JMM_POT_LJCUT, p=p, t=t,
+                             cutoff=3.0, max_step=0.3, max_dl=0.01 * n / 0.6, seed=seed + k,
+                             eci=0)
+    chain = oracle_lib.OraclePlain(params)
+    chain.fad()
+    chunk = n + 1
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        chain.steps(chunk)
+        steps += chunk
+        if time.perf_counter() - t0 >= seconds:
+            break
+    return steps, time.perf_counter() - t0
+
+
+def cpu_reference_sample(chains, seconds, seed):
+    """Aggregate moves/s of the reference algorithm, one chain per host core."""
+    import multiprocessing as mp
+    from tests import oracle_lib
+    oracle_lib.load()  # build the oracle library before the workers start
+    cores = os.cpu_count() or 1
+    picks = [int(i * len(chains) / cores) for i in range(cores)]
+    jobs = [(k, int(chains[k].n), float(chains[k].t), float(chains[k].p), seed, seconds, REPO)
+            for k in picks]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        out = pool.map(_cpu_worker, jobs)
+    wall = time.perf_counter() - t0
+    steps = sum(s for s, _ in out)
+    per_core_wall = max(w for _, w in out)
+    return {
+        "value": steps / per_core_wall,
+        "unit": UNIT,
+        "cores": cores,
+        "kind": "port",
+        "sample": (f"{cores} chains of the workload (N={chains[0].n}, NPT, LJcut 3.0), one per "
+                   f"host core, each run for {seconds:.1f} s with the reference's algorithm "
+                   "(oracle/plain_oracle.c: FP64, per-pair state, O(N) displacement, "
+                   "O(N^2) volume move, linear dL); aggregate attempted moves / wall"),
+        "steps": steps,
+        "wall_s": wall,
+    }
+
+
+# ---- roofline inputs -----------------------------------------------------------
+
+def profile_traffic(args, pair_evals_per_launch, sweeps):
+    """DRAM bytes per launch of the chain kernel from the committed ncu summary
+    (measured on a smaller launch and scaled by the launch's sweeps)."""
+    path = os.path.join(REPO, "profiles", "chains_kernel_batched_npt.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        text = f.read()
+    m = re.search(r"dram_bytes_per_chain_sweep:\s*([0-9.eE+-]+)", text)
+    m0 = re.search(r"dram_bytes_per_chain_launch_fixed:\s*([0-9.eE+-]+)", text)
+    if not m:
+        return None
+    per = float(m.group(1))
+    fixed = float(m0.group(1)) if m0 else 0.0
+    return args.chains * (per * sweeps + fixed)
+
+
+# ---- our implementation ----------------------------------------------------------
+
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import ctypes as C
+
+    from jmmonedmc_gb300 import _native, abi, build
+    if not os.path.exists(_native.lib_path()):
+        build.build_native()
+    from jmmonedmc_gb300.batch import ChainBatch, run_host
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    cfg, chains = workload(args, rank)
+
+    cpu = None
+    if rank == 0 and world == 1:
+        cpu = cpu_reference_sample(chains, args.cpu_seconds, args.seed)
+
+    lib = _native.load()
+    fp32_peak, rcp_peak = C.c_double(), C.c_double()
+    _native.call("jmm_measure_peaks", C.byref(fp32_peak), C.byref(rcp_peak))
+
+    b = ChainBatch(cfg, chains)
+    if args.no_autotune:
+        lanes, cpb = b.config.lanes_per_chain or 8, 0
+    else:
+        lanes, cpb = b.autotune(trial_sweeps=5)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    S = args.sweeps_per_step
+    for _ in range(args.warmup):
+        b.run_async(S, stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    before = b.results()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record(stream)
+        b.run_async(S, stream.cuda_stream)
+        ends[k].record(stream)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    after = b.results()
+    if np.any(after["error"] != 0):
+        raise RuntimeError(f"chain errors: {np.unique(after['error'])}")
+    moves = int((after["steps"] - before["steps"]).sum())
+    pairs = int((after["pair_evals"] - before["pair_evals"]).sum())
+    total_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms, moves, pairs], dtype=torch.float64, device=dev)
+        tmax = t.clone()
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        tsum = t.clone()
+        torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
+        total_ms, moves_all, pairs_all = float(tmax[0]), float(tsum[1]), float(tsum[2])
+    else:
+        moves_all, pairs_all = moves, pairs
+
+    # e2e: host buffers through the C ABI (jmm_batch_run_host), H2D and D2H inside
+    n_tot = args.chains * args.n
+    x_host = torch.empty(n_tot, dtype=torch.float32, pin_memory=True).numpy()
+    x_off = 0
+    for k in range(args.chains):
+        x_host[x_off:x_off + args.n] = b.positions(k)
+        x_off += args.n
+    lbox = after["l"].copy()
+    for k, c in enumerate(chains):
+        c.l0 = float(lbox[k])
+    e2e_cfg = abi.make_batch_config(seed=cfg.seed + 7, vol_move=cfg.vol_move,
+                                    vol_schedule=cfg.vol_schedule, precision=cfg.precision,
+                                    lanes_per_chain=lanes, chains_per_block=cpb)
+    e2e_times, e2e_moves = [], 0
+    for _ in range(args.e2e_steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        res_h, x_out = run_host(e2e_cfg, chains, S, x_in=x_host)
+        e2e_times.append(time.perf_counter() - t0)
+        e2e_moves += int(res_h["steps"].sum())
+        x_host[:] = x_out
+        for k, c in enumerate(chains):
+            c.l0 = float(res_h["l"][k])
+    e2e_value = e2e_moves / sum(e2e_times) * world
+    h2d = n_tot * 4 + args.chains * C.sizeof(abi.ChainDesc) + C.sizeof(abi.BatchConfig)
+    d2h = n_tot * 4 + args.chains * C.sizeof(abi.ChainResult)
+
+    launch_ms = total_ms / args.steps
+    flop_per_launch = pairs / args.steps * FLOP_PER_PAIR
+    achieved = flop_per_launch / (launch_ms * 1e-3) / 1e12
+    traffic = profile_traffic(args, pairs / args.steps, S)
+    line = {
+        "metric": METRIC,
+        "value": moves_all / (total_ms * 1e-3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded Philox: T log-spaced, P uniform, lattice start)",
+        "config": config_dict(args, {"lanes_per_chain": lanes, "chains_per_block": cpb,
+                                     "parallelism": f"replicas{world}",
+                                     "wall_s_timed": wall}),
+        "roofline": {
+            "bound": "fp32",
+            "achieved": achieved,
+            "peak": fp32_peak.value,
+            "unit": "TFLOP/s",
+            "frac": achieved / fp32_peak.value,
+            "traffic": traffic,
+            "peak_source": "measured live by jmm_measure_peaks (FP32 FMA kernel; "
+                           "MEASURED_PEAKS.json holds no FP32 figure)",
+            "pair_evals_per_launch": pairs / args.steps,
+            "flop_per_pair": FLOP_PER_PAIR,
+            "mufu_rcp_frac": (pairs / args.steps) / (launch_ms * 1e-3) / (rcp_peak.value * 1e12),
+            "kernel": "jmm::batch::chains_kernel",
+        },
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "how": "jmm_batch_run_host per step: pinned host positions in, results and "
+                       "positions out, batch set-up inside the timed region"},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    return line
+
+
+# ---- the reference arm -----------------------------------------------------------
+
+def run_reference(args):
+    cfg, chains = workload(args, 0)
+    cores = os.cpu_count() or 1
+    per_step = max(0.2, args.cpu_seconds / 2)
+    vals = []
+    samples = []
+    for _ in range(args.warmup):
+        cpu_reference_sample(chains, 0.2, args.seed)
+    t_total, steps_total = 0.0, 0
+    for _ in range(args.steps):
+        s = cpu_reference_sample(chains, per_step, args.seed)
+        vals.append(s["value"])
+        samples.append(s)
+        t_total += s["steps"] / s["value"]
+        steps_total += s["steps"]
+    value = steps_total / t_total
+    return {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_total / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (same chains as the GPU arm)",
+        "config": config_dict(args, {"parallelism": f"host cores x{cores}"}),
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": samples[-1]["sample"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args)), flush=True)
+        return 0
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    line = run_ours(args, rank, world, local_rank)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -263,6 +263,11 @@ int jmm_batch_run_host(const jmm_batch_config *cfg, const jmm_chain_desc *chains
 int jmm_rng_words(uint64_t seed, uint64_t block0, uint32_t chain, uint64_t count,
                   uint32_t *out);
 
+/* Roofline denominators measured live on the current device: FP32 FMA
+ * throughput (TFLOP/s, 2 FLOP per FMA) and MUFU reciprocal throughput
+ * (T ops/s), each the best of several event-timed launches. */
+int jmm_measure_peaks(double *fp32_tflops, double *rcp_tops);
+
 const char *jmm_last_error(void);
 /* 1 when a CUDA device can be used by this library, else 0. */
 int jmm_device_available(void);

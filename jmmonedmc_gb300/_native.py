@@ -46,6 +46,7 @@ SIGNATURES = {
     "jmm_plain_destroy": [vp],
     "jmm_last_error": [],
     "jmm_device_available": [],
+    "jmm_measure_peaks": [P(dbl), P(dbl)],
 }
 _RESTYPES = {"jmm_last_error": C.c_char_p}
 

@@ -29,6 +29,7 @@ UNITS = {
     "batch.cu": [],
     "grad.cu": [],
     "noalloc.cu": [],
+    "peak.cu": [],
 }
 
 

@@ -146,7 +146,7 @@ __device__ void group_energies(const float *xs, const ChainParams &P, int gl, un
   }
   u_old = group_sum_d<G>(uo, gmask);
   u_new = kScaled ? group_sum_d<G>(un, gmask) : u_old;
-  pairs += cnt;
+  pairs += __reduce_add_sync(gmask, cnt);
 }
 
 // Running statistics of one chain between folds.

@@ -124,7 +124,10 @@ def test_batch_fast_tracks_fp64_chain(gpu):
     rg, ro = gpu.results(), ora.results()
     same = (rg["disp_acc"] == ro["disp_acc"]) & (rg["vol_acc"] == ro["vol_acc"])
     assert same.mean() >= 0.95, same.mean()
-    np.testing.assert_allclose(rg["e"][same], ro["e"][same], rtol=1e-5, atol=1e-4)
+    # FP32 positions (|x| up to L/2 ~ 50, ulp ~ 4e-6) move the energies of the
+    # tracked chains apart by ~1e-5 relative within a few sweeps
+    np.testing.assert_allclose(rg["e"][same], ro["e"][same], rtol=2e-4, atol=1e-3)
+    np.testing.assert_allclose(rg["l"][same], ro["l"][same], rtol=1e-5)
 
 
 def test_batch_host_entry_matches_device_run(gpu):

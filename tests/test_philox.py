@@ -22,3 +22,10 @@ def test_step_words_layout():
     want = oracle_lib.philox_raw((block & 0xFFFFFFFF, block >> 32, 7, 0),
                                  (seed & 0xFFFFFFFF, seed >> 32))
     assert got == want
+
+
+def test_host_philox_matches_oracle():
+    from jmmonedmc_gb300.philox_host import philox4x32_10
+    for ctr, key, want in KAT:
+        assert philox4x32_10(*ctr, *key) == want
+    assert list(philox4x32_10(5, 0, 9, 0, 1, 0)) == oracle_lib.philox_raw((5, 0, 9, 0), (1, 0))
