@@ -247,10 +247,13 @@ def run_ours(args, rank, world, local_rank):
 
     b = ChainBatch(cfg, chains)
     if args.no_autotune:
-        lanes, cpb = b.config.lanes_per_chain or 8, 0
+        lanes, spr, cpb = 0, 0, 0
     else:
-        lanes, cpb = b.autotune(trial_sweeps=5)
-    stream = torch.cuda.current_stream(dev)
+        lanes, spr, cpb = b.autotune(trial_sweeps=5)
+    # a stream of our own: torch's default stream is the legacy stream, whose
+    # handle (0) would not name it to the library
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     S = args.sweeps_per_step
     for _ in range(args.warmup):
@@ -305,7 +308,8 @@ def run_ours(args, rank, world, local_rank):
         c.l0 = float(lbox[k])
     e2e_cfg = abi.make_batch_config(seed=cfg.seed + 7, vol_move=cfg.vol_move,
                                     vol_schedule=cfg.vol_schedule, precision=cfg.precision,
-                                    lanes_per_chain=lanes, chains_per_block=cpb)
+                                    lanes_per_chain=lanes, steps_per_round=spr,
+                                    chains_per_block=cpb)
     e2e_times, e2e_moves = [], 0
     for _ in range(args.e2e_steps):
         torch.cuda.synchronize(dev)
@@ -337,7 +341,8 @@ def run_ours(args, rank, world, local_rank):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded Philox: T log-spaced, P uniform, lattice start)",
-        "config": config_dict(args, {"lanes_per_chain": lanes, "chains_per_block": cpb,
+        "config": config_dict(args, {"lanes_per_chain": lanes, "steps_per_round": spr,
+                                     "chains_per_block": cpb,
                                      "parallelism": f"replicas{world}",
                                      "wall_s_timed": wall}),
         "roofline": {

@@ -206,8 +206,11 @@ typedef struct jmm_batch_config {
   int32_t precision;         /* JMM_PREC_*                                      */
   uint32_t resum_sweeps;     /* constant-L chains: FP64 re-sum of E every this
                                 many sweeps (0 = only at the end of a run)      */
-  uint32_t lanes_per_chain;  /* 4, 8, 16 or 32; 0 = 8                           */
-  uint32_t chains_per_block; /* 0 = 4                                           */
+  uint32_t lanes_per_chain;  /* window lanes G of one trial move: 8, 16 or 32;
+                                0 = 8                                           */
+  uint32_t steps_per_round;  /* S steps evaluated at once per chain, G*S = 16 or
+                                32; 0 = 32/G                                    */
+  uint32_t chains_per_block; /* 0 = 128 / (G*S)                                 */
   int32_t init;              /* JMM_INIT_*                                      */
   double jitter;             /* half-width of the initial jitter               */
 } jmm_batch_config;
@@ -247,9 +250,9 @@ int jmm_batch_energies(jmm_batch *b, double *e, uint32_t n_chains);
 int jmm_batch_device_views(jmm_batch *b, void **positions, void **results,
                            uint64_t *offsets, uint32_t n_chains);
 /* Time candidate launch shapes on a copy of the state and keep the fastest;
- * writes the chosen lanes_per_chain and chains_per_block. */
+ * writes the chosen lanes_per_chain, steps_per_round and chains_per_block. */
 int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t *lanes_per_chain,
-                       uint32_t *chains_per_block);
+                       uint32_t *steps_per_round, uint32_t *chains_per_block);
 int jmm_batch_destroy(jmm_batch *b);
 
 /* Host-buffer convenience: create, upload positions (NULL = the configured

@@ -167,6 +167,7 @@ class BatchConfig(C.Structure):
         ("precision", C.c_int32),
         ("resum_sweeps", C.c_uint32),
         ("lanes_per_chain", C.c_uint32),
+        ("steps_per_round", C.c_uint32),
         ("chains_per_block", C.c_uint32),
         ("init", C.c_int32),
         ("jitter", C.c_double),
@@ -228,8 +229,8 @@ def make_chain(n, potential=JMM_POT_LJCUT, ensemble=JMM_NLT, eps=1.0, sigma=1.0,
 
 def make_batch_config(seed=1, boundary=JMM_BOUNDARY_WALLS, vol_move=JMM_VOLMOVE_LNL,
                       vol_schedule=JMM_VOLSCHED_SWEEP, precision=JMM_PREC_FAST,
-                      resum_sweeps=100, lanes_per_chain=0, chains_per_block=0,
-                      init=JMM_INIT_LATTICE, jitter=0.0):
+                      resum_sweeps=100, lanes_per_chain=0, steps_per_round=0,
+                      chains_per_block=0, init=JMM_INIT_LATTICE, jitter=0.0):
     c = BatchConfig()
     c.seed = seed
     c.boundary = boundary
@@ -238,6 +239,7 @@ def make_batch_config(seed=1, boundary=JMM_BOUNDARY_WALLS, vol_move=JMM_VOLMOVE_
     c.precision = precision
     c.resum_sweeps = resum_sweeps
     c.lanes_per_chain = lanes_per_chain
+    c.steps_per_round = steps_per_round
     c.chains_per_block = chains_per_block
     c.init = init
     c.jitter = jitter

@@ -24,7 +24,8 @@ _native.register({
     "jmm_batch_energies": [C.c_void_p, P(C.c_double), C.c_uint32],
     "jmm_batch_device_views": [C.c_void_p, P(C.c_void_p), P(C.c_void_p), P(C.c_uint64),
                                C.c_uint32],
-    "jmm_batch_autotune": [C.c_void_p, C.c_uint32, P(C.c_uint32), P(C.c_uint32)],
+    "jmm_batch_autotune": [C.c_void_p, C.c_uint32, P(C.c_uint32), P(C.c_uint32),
+                           P(C.c_uint32)],
     "jmm_batch_destroy": [C.c_void_p],
     "jmm_batch_run_host": [P(abi.BatchConfig), P(abi.ChainDesc), C.c_uint32, P(C.c_float),
                            C.c_uint64, P(abi.ChainResult), P(C.c_float)],
@@ -116,9 +117,11 @@ class ChainBatch:
         return px.value, pr.value, off
 
     def autotune(self, trial_sweeps=4):
-        g, c = C.c_uint32(), C.c_uint32()
-        _native.call("jmm_batch_autotune", self._h, trial_sweeps, C.byref(g), C.byref(c))
-        return g.value, c.value
+        """(lanes_per_chain, steps_per_round, chains_per_block) chosen."""
+        g, s, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        _native.call("jmm_batch_autotune", self._h, trial_sweeps, C.byref(g), C.byref(s),
+                     C.byref(c))
+        return g.value, s.value, c.value
 
 
 def run_host(config, chains, n_sweeps, x_in=None):

@@ -26,14 +26,14 @@ constexpr size_t kMaxSmem = 227 * 1024;
 
 typedef void (*ChainsKernel)(const ChainParams *, jmm_chain_result *, float *, KernelCfg);
 
-ChainsKernel pick_kernel(uint32_t g, bool exact) {
-  switch (g) {
-    case 4: return exact ? chains_kernel<4, true> : chains_kernel<4, false>;
-    case 8: return exact ? chains_kernel<8, true> : chains_kernel<8, false>;
-    case 16: return exact ? chains_kernel<16, true> : chains_kernel<16, false>;
-    case 32: return exact ? chains_kernel<32, true> : chains_kernel<32, false>;
-    default: return nullptr;
-  }
+// Launch shapes: G window lanes x S steps per round, G*S = 16 or 32 lanes.
+ChainsKernel pick_kernel(uint32_t g, uint32_t s, bool exact) {
+  if (g == 8 && s == 4) return exact ? chains_kernel<8, 4, true> : chains_kernel<8, 4, false>;
+  if (g == 8 && s == 2) return exact ? chains_kernel<8, 2, true> : chains_kernel<8, 2, false>;
+  if (g == 16 && s == 2) return exact ? chains_kernel<16, 2, true> : chains_kernel<16, 2, false>;
+  if (g == 16 && s == 1) return exact ? chains_kernel<16, 1, true> : chains_kernel<16, 1, false>;
+  if (g == 32 && s == 1) return exact ? chains_kernel<32, 1, true> : chains_kernel<32, 1, false>;
+  return nullptr;
 }
 
 uint64_t pad4(uint64_t n) { return (n + 3) & ~uint64_t(3); }
@@ -52,7 +52,7 @@ struct jmm_batch {
   jmm_chain_result *d_res = nullptr;
   float *d_x = nullptr;
   double *d_e = nullptr;
-  uint32_t g = 8, cpb = 4, n_blocks = 0;
+  uint32_t g = 8, spr = 4, cpb = 4, n_blocks = 0;
   size_t smem = 0;
   cudaStream_t stream = nullptr;
   std::map<uint64_t, cudaGraphExec_t> graphs;  // n_sweeps -> instantiated run
@@ -74,11 +74,14 @@ static void batch_free(jmm_batch *b) {
   delete b;
 }
 
-// Per-chain kernel parameters for launch shape (g, cpb); uploads them.
-static int apply_layout(jmm_batch *b, uint32_t g, uint32_t cpb) {
-  if (!pick_kernel(g, false)) return fail(JMM_ERR_INVALID, "lanes_per_chain must be 4, 8, 16 or 32");
-  if (cpb == 0 || cpb * g > 256 || (cpb * g) % 32 != 0)
-    return fail(JMM_ERR_INVALID, "chains_per_block * lanes_per_chain must be a multiple of 32, <= 256");
+// Per-chain kernel parameters for launch shape (g, spr, cpb); uploads them.
+static int apply_layout(jmm_batch *b, uint32_t g, uint32_t spr, uint32_t cpb) {
+  if (!pick_kernel(g, spr, false))
+    return fail(JMM_ERR_INVALID, "unsupported launch shape: lanes_per_chain x steps_per_round "
+                "must be 8x4, 8x2, 16x2, 16x1 or 32x1");
+  const uint32_t lanes = g * spr;
+  if (cpb == 0 || cpb * lanes > 256)
+    return fail(JMM_ERR_INVALID, "chains_per_block * lanes per chain must be <= 256");
   const uint32_t w = g / 2;
   if (b->cfg.boundary == JMM_BOUNDARY_PERIODIC) {
     for (const auto &c : b->chains)
@@ -88,8 +91,9 @@ static int apply_layout(jmm_batch *b, uint32_t g, uint32_t cpb) {
   std::vector<ChainParams> prm(b->n_chains);
   size_t smem_max = 0;
   const uint32_t n_blocks = (b->n_chains + cpb - 1) / cpb;
+  const uint64_t ring_floats = (uint64_t)cpb * kRingWords;
   for (uint32_t blk = 0; blk < n_blocks; ++blk) {
-    uint64_t s_off = 0;
+    uint64_t s_off = ring_floats;
     for (uint32_t k = 0; k < cpb; ++k) {
       const uint32_t slot = blk * cpb + k;
       if (slot >= b->n_chains) break;
@@ -121,12 +125,13 @@ static int apply_layout(jmm_batch *b, uint32_t g, uint32_t cpb) {
   if (smem_max > kMaxSmem)
     return fail(JMM_ERR_INVALID, "a block's chains need %zu bytes of shared memory (max %zu): "
                 "lower chains_per_block", smem_max, kMaxSmem);
-  ChainsKernel kf = pick_kernel(g, b->cfg.precision == JMM_PREC_EXACT);
+  ChainsKernel kf = pick_kernel(g, spr, b->cfg.precision == JMM_PREC_EXACT);
   JMM_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
   JMM_CUDA(cudaMemcpy(b->d_params, prm.data(), prm.size() * sizeof(ChainParams),
                       cudaMemcpyHostToDevice));
   b->params.swap(prm);
   b->g = g;
+  b->spr = spr;
   b->cpb = cpb;
   b->n_blocks = n_blocks;
   b->smem = smem_max;
@@ -144,8 +149,8 @@ static int launch(jmm_batch *b, uint64_t n_sweeps, cudaStream_t s) {
   kc.resum_sweeps = (int32_t)b->cfg.resum_sweeps;
   kc.n_chains = b->n_chains;
   kc.chains_per_block = b->cpb;
-  ChainsKernel kf = pick_kernel(b->g, b->cfg.precision == JMM_PREC_EXACT);
-  kf<<<b->n_blocks, b->g * b->cpb, b->smem, s>>>(b->d_params, b->d_res, b->d_x, kc);
+  ChainsKernel kf = pick_kernel(b->g, b->spr, b->cfg.precision == JMM_PREC_EXACT);
+  kf<<<b->n_blocks, b->g * b->spr * b->cpb, b->smem, s>>>(b->d_params, b->d_res, b->d_x, kc);
   JMM_CUDA(cudaGetLastError());
   return JMM_OK;
 }
@@ -264,8 +269,9 @@ extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_des
     return rc;
   }
   const uint32_t g = cfg->lanes_per_chain ? cfg->lanes_per_chain : 8;
-  const uint32_t cpb = cfg->chains_per_block ? cfg->chains_per_block : 128 / g;
-  rc = apply_layout(b, g, cpb);
+  const uint32_t spr = cfg->steps_per_round ? cfg->steps_per_round : (g <= 32 ? 32 / g : 1);
+  const uint32_t cpb = cfg->chains_per_block ? cfg->chains_per_block : 128 / (g * spr ? g * spr : 1);
+  rc = apply_layout(b, g, spr, cpb);
   if (rc == JMM_OK) rc = energies(b, b->stream);
   if (rc == JMM_OK) {
     set_energies_kernel<<<(n_chains + 255) / 256, 256, 0, b->stream>>>(b->d_res, b->d_e, n_chains);
@@ -308,6 +314,9 @@ extern "C" int jmm_batch_run_async(jmm_batch *b, uint64_t n_sweeps, void *stream
   clear_error();
   JMM_CHECK_ARG(b, "null handle");
   if (n_sweeps == 0) return JMM_OK;
+  for (const auto &c : b->chains)
+    if (n_sweeps * (uint64_t)(c.n + 1) >= (1ull << 31))
+      return fail(JMM_ERR_INVALID, "one run may hold at most 2^31 steps per chain: split it");
   cudaGraphExec_t exec;
   int rc = graph_for(b, n_sweeps, &exec);
   if (rc) return rc;
@@ -431,7 +440,7 @@ extern "C" int jmm_batch_device_views(jmm_batch *b, void **positions, void **res
 }
 
 extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t *lanes_out,
-                                  uint32_t *cpb_out) {
+                                  uint32_t *spr_out, uint32_t *cpb_out) {
   clear_error();
   JMM_CHECK_ARG(b, "null handle");
   if (trial_sweeps == 0) trial_sweeps = 4;
@@ -449,15 +458,17 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
   cudaEvent_t t0, t1;
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
-  const uint32_t g0 = b->g, c0 = b->cpb;
+  const uint32_t g0 = b->g, s0 = b->spr, c0 = b->cpb;
   float best = 1e30f;
-  uint32_t best_g = g0, best_c = c0;
+  uint32_t best_g = g0, best_s = s0, best_c = c0;
   int rc = JMM_OK;
-  for (uint32_t g : {4u, 8u, 16u, 32u}) {
+  const uint32_t shapes[][2] = {{8, 4}, {8, 2}, {16, 2}, {16, 1}, {32, 1}};
+  for (const auto &shape : shapes) {
+    const uint32_t g = shape[0], spr = shape[1];
     for (uint32_t threads : {32u, 64u, 128u, 256u}) {
-      const uint32_t cpb = threads / g;
+      const uint32_t cpb = threads / (g * spr);
       if (cpb == 0) continue;
-      if (apply_layout(b, g, cpb) != JMM_OK) {
+      if (apply_layout(b, g, spr, cpb) != JMM_OK) {
         clear_error();
         continue;
       }
@@ -478,6 +489,7 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
       if (ms < best) {
         best = ms;
         best_g = g;
+        best_s = spr;
         best_c = cpb;
       }
     }
@@ -490,11 +502,13 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
   cudaFree(x_save);
   cudaFree(r_save);
   if (rc) return rc;
-  rc = apply_layout(b, best_g, best_c);
+  rc = apply_layout(b, best_g, best_s, best_c);
   if (rc) return rc;
   b->cfg.lanes_per_chain = best_g;
+  b->cfg.steps_per_round = best_s;
   b->cfg.chains_per_block = best_c;
   if (lanes_out) *lanes_out = best_g;
+  if (spr_out) *spr_out = best_s;
   if (cpb_out) *cpb_out = best_c;
   JMM_CUDA(cudaDeviceSynchronize());
   return JMM_OK;

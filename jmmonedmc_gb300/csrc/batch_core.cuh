@@ -2,20 +2,28 @@
 //
 // One chain is the reference's sequential single-particle Metropolis chain
 // (Step/qad2/fav, src/jmmMCState.cpp:1758-1811, :1160-1464, :2161-2293),
-// re-cast for many chains per GPU:
-//  * a group of G lanes owns one chain; lane g looks at neighbour
-//    side(g)*k(g) of the moved particle, side = -1 for g < W = G/2, k =
-//    g % W + 1, and evaluates that pair at the old and the trial position;
-//  * positions are FP32 in shared memory and stay ordered along the line,
-//    so the partners within the cut-off are index neighbours; when the
-//    W-th neighbour on a side is still within the cut-off the window is
-//    extended in further chunks of W;
-//  * the energy change is the group's butterfly sum (xor 1, 2, 4, ...);
-//  * Philox words of 32 steps are drawn ahead, one step per lane, and
-//    handed out with shuffles;
-//  * the running energy is an FP64 base plus an FP32 offset that is folded
-//    into FP64 at every volume move, re-summation and launch end, together
-//    with the per-step accumulators (sum E, E^2, L, L^2, LE, rho, rho^2).
+// re-cast for many chains per GPU.  A chain owns L = G*S lanes (16 or 32):
+//
+//  * Window.  Particles stay ordered along the line, so the partners within
+//    the cut-off of the moved particle are index neighbours.  G lanes
+//    evaluate one trial move: lane w looks at neighbour side(w)*k(w),
+//    side = -1 for w < W = G/2, k = w % W + 1, at the old and the trial
+//    position; the energy change is the butterfly sum (xor 1, 2, 4, ...) of
+//    the G lanes.  When the W-th neighbour on a side is still within the
+//    cut-off the window is extended in chunks of W (a rare slow path).
+//  * Speculative rounds.  The S lane segments of a chain evaluate the next S
+//    steps of the chain at once, all from the current positions.  Step s of
+//    the round is kept if no earlier kept step of the round was accepted
+//    within W index positions of it (its window would have seen the moved
+//    particle); the first step that fails is re-evaluated at the start of
+//    the next round.  Kept steps are committed in order, so every step's
+//    outcome, the running energy and the statistics are those of the
+//    sequential chain, operation for operation.
+//  * Philox words of 32 steps ahead are drawn by the chain's lanes into a
+//    small shared buffer.
+//  * The running energy is an FP64 base plus an FP32 offset, folded into
+//    FP64 at every volume move, re-summation and launch end together with
+//    the per-step accumulators (sum E, E^2, L, L^2, LE, rho, rho^2).
 // Every FP32/FP64 operation is an explicit round-to-nearest intrinsic so
 // that the EXACT precision mode can be replayed bit for bit by the oracle;
 // the FAST mode differs only in using the hardware reciprocal and exp.
@@ -30,13 +38,16 @@
 namespace jmm {
 namespace batch {
 
+constexpr int kRingSteps = 32;  // Philox words drawn ahead per chain
+constexpr int kRingWords = 3 * kRingSteps;
+
 struct ChainParams {
   uint32_t id;               // user index: Philox stream and result slot
   uint32_t n;
   uint32_t pot;
   uint32_t ensemble;
   uint32_t steps_per_sweep;  // n, or n+1 with volume moves
-  uint32_t s_off;            // float offset of the chain in its block's shared memory
+  uint32_t s_off;            // float offset of the chain's positions in block shared memory
   uint64_t x_off;            // float offset of the chain's positions in HBM
   float eps4;                // LJ: 4 eps; soft sphere and Gaussian: eps
   float sigma2;
@@ -71,16 +82,35 @@ __device__ __forceinline__ float exp32(float x) {
   return __expf(x);
 }
 
-// Pair energy from the squared separation; 0 beyond the cut-off.
+// Pair energy from the squared separation; 0 beyond the cut-off (a select,
+// not a branch).  Runtime potential, for the rarely executed paths.
 template <bool kExact>
 __device__ __forceinline__ float pair_energy(float d2, const ChainParams &P) {
-  if (!(d2 <= P.rc2)) return 0.0f;
-  if (P.pot == JMM_POT_GAUSS)
-    return __fmul_rn(P.eps4, exp32<kExact>(-__fmul_rn(d2, P.inv_sigma2)));
-  const float inv2 = __fmul_rn(P.sigma2, rcp32<kExact>(d2));
-  const float inv6 = __fmul_rn(__fmul_rn(inv2, inv2), inv2);
-  if (P.pot == JMM_POT_SOFTSPHERE) return __fmul_rn(P.eps4, __fmul_rn(inv6, inv6));
-  return __fmul_rn(P.eps4, __fmul_rn(inv6, __fsub_rn(inv6, 1.0f)));  // LJ 12-6
+  float e;
+  if (P.pot == JMM_POT_GAUSS) {
+    e = __fmul_rn(P.eps4, exp32<kExact>(-__fmul_rn(d2, P.inv_sigma2)));
+  } else {
+    const float inv2 = __fmul_rn(P.sigma2, rcp32<kExact>(d2));
+    const float inv6 = __fmul_rn(__fmul_rn(inv2, inv2), inv2);
+    e = (P.pot == JMM_POT_SOFTSPHERE) ? __fmul_rn(P.eps4, __fmul_rn(inv6, inv6))
+                                      : __fmul_rn(P.eps4, __fmul_rn(inv6, __fsub_rn(inv6, 1.0f)));
+  }
+  return d2 <= P.rc2 ? e : 0.0f;
+}
+
+// The same with the potential fixed at compile time (the step loop).
+template <int POT, bool kExact>
+__device__ __forceinline__ float pair_energy_t(float d2, const ChainParams &P) {
+  float e;
+  if (POT == JMM_POT_GAUSS) {
+    e = __fmul_rn(P.eps4, exp32<kExact>(-__fmul_rn(d2, P.inv_sigma2)));
+  } else {
+    const float inv2 = __fmul_rn(P.sigma2, rcp32<kExact>(d2));
+    const float inv6 = __fmul_rn(__fmul_rn(inv2, inv2), inv2);
+    e = (POT == JMM_POT_SOFTSPHERE) ? __fmul_rn(P.eps4, __fmul_rn(inv6, inv6))
+                                    : __fmul_rn(P.eps4, __fmul_rn(inv6, __fsub_rn(inv6, 1.0f)));
+  }
+  return d2 <= P.rc2 ? e : 0.0f;
 }
 
 template <int G>
@@ -98,17 +128,18 @@ __device__ __forceinline__ double group_sum_d(double v, unsigned mask) {
 }
 
 // Total pair energy of the chain at positions xs (U_old) and at positions
-// scaled by s with box length lnew (U_new): lane g takes particles g, g+G, ...
-// and their right-hand neighbours in order until both separations exceed the
-// cut-off; per-particle sums are FP32, the lane and group sums FP64.
-template <int G, bool kExact, bool kScaled>
+// scaled by s with box length lnew (U_new): lane g of the chain's L lanes
+// takes particles g, g+L, ... and their right-hand neighbours in order until
+// both separations exceed the cut-off; per-particle sums are FP32, the lane
+// and chain sums FP64.
+template <int L, bool kExact, bool kScaled>
 __device__ void group_energies(const float *xs, const ChainParams &P, int gl, unsigned gmask,
                                bool periodic, float lf, float s, float lnf, double &u_old,
                                double &u_new, uint64_t &pairs, uint32_t &err) {
   const int n = (int)P.n;
   double uo = 0.0, un = 0.0;
   uint32_t cnt = 0;
-  for (int i = gl; i < n; i += G) {
+  for (int i = gl; i < n; i += L) {
     const float xi = xs[i];
     const float xin = kScaled ? __fmul_rn(xi, s) : xi;
     float eo = 0.0f, en = 0.0f;
@@ -144,8 +175,8 @@ __device__ void group_energies(const float *xs, const ChainParams &P, int gl, un
     uo = __dadd_rn(uo, (double)eo);
     if (kScaled) un = __dadd_rn(un, (double)en);
   }
-  u_old = group_sum_d<G>(uo, gmask);
-  u_new = kScaled ? group_sum_d<G>(un, gmask) : u_old;
+  u_old = group_sum_d<L>(uo, gmask);
+  u_new = kScaled ? group_sum_d<L>(un, gmask) : u_old;
   pairs += __reduce_add_sync(gmask, cnt);
 }
 
@@ -186,30 +217,52 @@ __device__ __forceinline__ float threshold_of(uint32_t w) {
   return -portable_logf(u);
 }
 
-template <int G, bool kExact>
-__global__ void __launch_bounds__(256) chains_kernel(const ChainParams *__restrict__ prm,
-                                                     jmm_chain_result *__restrict__ res,
-                                                     float *__restrict__ xg, KernelCfg cfg) {
+// Neighbour index of window lane (side, k), clamped for loads, and its
+// periodic shift.
+template <bool PER>
+__device__ __forceinline__ int window_index(int nm, int side, int k, int n, float lf, bool &inr,
+                                            float &shift) {
+  int j = nm + side * k;
+  shift = 0.0f;
+  if (!PER) {
+    inr = j >= 0 && j < n;
+    j = j < 0 ? 0 : (j >= n ? n - 1 : j);
+  } else {
+    inr = true;
+    if (j < 0) {
+      j += n;
+      shift = -lf;
+    } else if (j >= n) {
+      j -= n;
+      shift = lf;
+    }
+  }
+  return j;
+}
+
+// One chain for one launch: n_sweeps sweeps in speculative rounds of S steps.
+template <int G, int S, int POT, bool PER, bool kExact>
+__device__ __noinline__ void run_chain(const ChainParams &P, jmm_chain_result *__restrict__ res,
+                                       float *__restrict__ xg, float *xs, uint32_t *ring,
+                                       const KernelCfg &cfg, int cl, unsigned gmask) {
   constexpr int W = G / 2;
-  constexpr int KS = 32 / G;  // steps each lane draws ahead per batch of 32
-  extern __shared__ float smem[];
-  const int gl = threadIdx.x % G;
-  const int gw = (threadIdx.x & 31) / G;
-  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (gw * G));
-  const uint32_t slot = blockIdx.x * cfg.chains_per_block + threadIdx.x / G;
-  if (slot >= cfg.n_chains) return;
-  const ChainParams P = prm[slot];
+  constexpr int L = G * S;
+  constexpr unsigned kSlotBits = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
   const int n = (int)P.n;
-  float *xs = smem + P.s_off;
-  for (int i = gl; i < n; i += G) xs[i] = xg[P.x_off + i];
-  __syncwarp(gmask);
+  const int slot = cl / G;
+  const int wl = cl % G;
+  const int side = wl < W ? -1 : 1;
+  const int kk = wl % W + 1;
+  const int lane_shift = (int)(threadIdx.x & 31) - cl;  // first lane of the chain in the warp
+  uint32_t *ring_w0 = ring;
+  float *ring_u1 = reinterpret_cast<float *>(ring + kRingSteps);
+  float *ring_thr = reinterpret_cast<float *>(ring + 2 * kRingSteps);
 
   jmm_chain_result R = res[P.id];
-  const bool periodic = cfg.boundary == JMM_BOUNDARY_PERIODIC;
   const bool npt = P.ensemble == JMM_NPT;
   const bool per_sweep = cfg.vol_schedule == JMM_VOLSCHED_SWEEP;
-  double L = R.l;
-  float lf = (float)L, half_l = (float)__dmul_rn(L, 0.5);
+  double L_box = R.l;
+  float lf = (float)L_box, half_l = (float)__dmul_rn(L_box, 0.5);
   Seg g;
   g.e0 = R.e;
   g.delta = 0.0f;
@@ -221,174 +274,263 @@ __global__ void __launch_bounds__(256) chains_kernel(const ChainParams *__restri
   uint32_t sweeps_since_resum = 0;
   uint32_t err = R.error;
   uint64_t pairs = R.pair_evals;
-  const int side = gl < W ? -1 : 1;
-  const int kk = gl % W + 1;
-  const uint64_t total = cfg.n_sweeps * (uint64_t)spsw;
+  uint32_t d_acc = 0, d_att = 0, v_acc = 0, v_att = 0, overflows = 0;
+  const uint32_t total = (uint32_t)(cfg.n_sweeps * (uint64_t)spsw);
   const uint64_t step0 = R.steps;
 
-  for (uint64_t t = 0; t < total; t += 32) {
-    uint32_t r_w0[KS];
-    float r_u1[KS], r_thr[KS];
-#pragma unroll
-    for (int k = 0; k < KS; ++k) {
-      const uint64_t s = step0 + t + (uint64_t)(gl + G * k) + 1;
-      const Words4 w = step_words(cfg.seed, s, P.id);
-      r_w0[k] = w.w[0];
-      r_u1[k] = word_to_unit_f(w.w[1]);
-      r_thr[k] = threshold_of(w.w[2]);
+  uint32_t base = 0, pbase = 0;
+  bool ring_valid = false;
+  while (base < total) {
+    if (!ring_valid || base + S > pbase + kRingSteps) {
+      pbase = base;
+      __syncwarp(gmask);
+      for (int e = cl; e < kRingSteps; e += L) {
+        const Words4 w = step_words(cfg.seed, step0 + pbase + e + 1, P.id);
+        ring_w0[e] = w.w[0];
+        ring_u1[e] = word_to_unit_f(w.w[1]);
+        ring_thr[e] = threshold_of(w.w[2]);
+      }
+      __syncwarp(gmask);
+      ring_valid = true;
     }
-#pragma unroll
-    for (int k = 0; k < KS; ++k) {
-      for (int src = 0; src < G; ++src) {
-        if (t + (uint64_t)(k * G + src) >= total) break;
-        const uint32_t w0 = __shfl_sync(gmask, r_w0[k], src, G);
-        const float u1 = __shfl_sync(gmask, r_u1[k], src, G);
-        const float thr = __shfl_sync(gmask, r_thr[k], src, G);
-        bool vol = false;
-        int nm;
-        ++sweep_pos;
-        if (npt && !per_sweep) {
-          nm = (int)word_to_index(w0, (uint64_t)n + 1);
-          vol = nm == n;
-        } else {
-          nm = (int)word_to_index(w0, (uint64_t)n);
-          vol = npt && sweep_pos == spsw;
-        }
-        const bool sweep_end = sweep_pos == spsw;
-        if (sweep_end) sweep_pos = 0;
+    uint32_t rem = total - base;
+    if (rem > (uint32_t)S) rem = S;
+    if (rem > spsw - sweep_pos) rem = spsw - sweep_pos;
+    const uint32_t ri = base + slot - pbase;  // < 32
+    const uint32_t w0 = ring_w0[ri];
+    const float u1 = ring_u1[ri];
+    const float thr = ring_thr[ri];
+    int nm;
+    bool isvol;
+    if (npt && !per_sweep) {
+      nm = (int)word_to_index(w0, (uint64_t)n + 1);
+      isvol = nm == n;
+    } else {
+      nm = (int)word_to_index(w0, (uint64_t)n);
+      isvol = npt && (sweep_pos + (uint32_t)slot + 1 == spsw);
+    }
+    const unsigned volbits =
+        __ballot_sync(gmask, isvol && wl == 0 && (uint32_t)slot < rem) >> lane_shift;
 
-        if (!vol) {
-          // ---- displacement (qad2) ----
-          const float md = __fmul_rn(__fsub_rn(u1, 0.5f), P.two_max_step);
-          const float xo = xs[nm];
-          const float xn = __fadd_rn(xo, md);
-          float left, right;
-          if (periodic) {
-            left = nm > 0 ? xs[nm - 1] : __fsub_rn(xs[n - 1], lf);
-            right = nm + 1 < n ? xs[nm + 1] : __fadd_rn(xs[0], lf);
-          } else {
-            left = nm > 0 ? xs[nm - 1] : -INFINITY;
-            right = nm + 1 < n ? xs[nm + 1] : INFINITY;
+    if (volbits & 1u) {
+      // ---- volume move (fav), ln L or linear: all L lanes ----
+      double lnew;
+      float s;
+      double logw;  // weight term: (N+1) ln s or N ln(L'/L)
+      const float v = __fsub_rn(__fmul_rn(2.0f, u1), 1.0f);
+      if (cfg.vol_move == JMM_VOLMOVE_LNL) {
+        const float lns = __fmul_rn(P.vol_step, v);
+        s = portable_expf(lns);
+        lnew = __dmul_rn(L_box, (double)s);
+        logw = __dmul_rn((double)(n + 1), (double)lns);
+      } else {
+        const double dl = (double)__fmul_rn(P.vol_step, v);
+        lnew = __dadd_rn(L_box, dl);
+        const double ratio = __ddiv_rn(lnew, L_box);
+        s = (float)ratio;
+        logw = lnew > 0.0 ? __dmul_rn((double)n, log(ratio)) : -INFINITY;
+      }
+      double uo, un;
+      const float lnf = (float)lnew;
+      group_energies<L, kExact, true>(xs, P, cl, gmask, PER, lf, s, lnf, uo, un, pairs, err);
+      const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
+      if (drift > R.max_drift) R.max_drift = drift;
+      const double du = __dsub_rn(un, uo);
+      const double arg = __dsub_rn(
+          __dmul_rn(P.beta_d, __dadd_rn(du, __dmul_rn(P.p, __dsub_rn(lnew, L_box)))), logw);
+      bool acc = arg < (double)thr;
+      if (!(lnew > 0.0)) acc = false;
+      if (PER && !(lnew > 2.0 * (double)P.rc)) acc = false;
+      fold(g, R, L_box, (uint32_t)n);
+      v_att += 1;
+      if (acc) {
+        for (int i = cl; i < n; i += L) xs[i] = __fmul_rn(xs[i], s);
+        L_box = lnew;
+        lf = (float)L_box;
+        half_l = (float)__dmul_rn(L_box, 0.5);
+        g.e0 = un;
+        v_acc += 1;
+      } else {
+        g.e0 = uo;
+      }
+      __syncwarp(gmask);
+      g.sd = __fadd_rn(g.sd, g.delta);
+      g.sd2 = __fmaf_rn(g.delta, g.delta, g.sd2);
+      g.nseg += 1;
+      base += 1;
+      sweep_pos += 1;
+    } else {
+      if (volbits) rem = min(rem, (uint32_t)(__ffs(volbits) - 1) / G);
+      // ---- S displacement steps (qad2) from the current positions ----
+      const int nmc = nm < n ? nm : n - 1;
+      const float md = __fmul_rn(__fsub_rn(u1, 0.5f), P.two_max_step);
+      const float xo = xs[nmc];
+      const float xn = __fadd_rn(xo, md);
+      float left, right;
+      if (PER) {
+        left = nmc > 0 ? xs[nmc - 1] : __fsub_rn(xs[n - 1], lf);
+        right = nmc + 1 < n ? xs[nmc + 1] : __fadd_rn(xs[0], lf);
+      } else {
+        left = nmc > 0 ? xs[nmc - 1] : -INFINITY;
+        right = nmc + 1 < n ? xs[nmc + 1] : INFINITY;
+      }
+      bool ok = (xn > left) && (xn < right);
+      if (!PER) ok = ok && !(fabsf(xn) > half_l);
+      bool inr;
+      float shift;
+      const int j = window_index<PER>(nmc, side, kk, n, lf, inr, shift);
+      const float xj = __fadd_rn(xs[j], shift);
+      const float dnw = side > 0 ? __fsub_rn(xj, xn) : __fsub_rn(xn, xj);
+      const float dol = side > 0 ? __fsub_rn(xj, xo) : __fsub_rn(xo, xj);
+      const float dn2 = __fmul_rn(dnw, dnw), do2 = __fmul_rn(dol, dol);
+      const float t_pair =
+          inr ? __fsub_rn(pair_energy_t<POT, kExact>(dn2, P), pair_energy_t<POT, kExact>(do2, P))
+              : 0.0f;
+      const bool sat = ok && inr && kk == W && (dn2 <= P.rc2 || do2 <= P.rc2);
+      float de = group_sum<G>(t_pair, gmask);
+      const unsigned satbits = __ballot_sync(gmask, sat) >> lane_shift;
+      uint32_t f = rem;
+      uint32_t extra_chunks = 0;
+      if (satbits & kSlotBits) {
+        // slow path: slot 0's window reaches beyond W; extend it chunk by chunk
+        for (int chunk = 1;; ++chunk) {
+          const int k = chunk * W + kk;
+          bool inr2;
+          float shift2;
+          const int j2 = window_index<PER>(nmc, side, k, n, lf, inr2, shift2);
+          const float xj2 = __fadd_rn(xs[j2], shift2);
+          const float dn_2 = side > 0 ? __fsub_rn(xj2, xn) : __fsub_rn(xn, xj2);
+          const float do_2 = side > 0 ? __fsub_rn(xj2, xo) : __fsub_rn(xo, xj2);
+          const float dn22 = __fmul_rn(dn_2, dn_2), do22 = __fmul_rn(do_2, do_2);
+          const float t2 = inr2 ? __fsub_rn(pair_energy_t<POT, kExact>(dn22, P),
+                                            pair_energy_t<POT, kExact>(do22, P))
+                                : 0.0f;
+          de = __fadd_rn(de, group_sum<G>(t2, gmask));
+          extra_chunks += 1;
+          const bool sat2 = inr2 && (k == (chunk + 1) * W) && (dn22 <= P.rc2 || do22 <= P.rc2);
+          if (!((__ballot_sync(gmask, sat2) >> lane_shift) & kSlotBits)) break;
+          if (PER && 2 * (chunk + 2) * W > n - 1) {
+            err = JMM_ERR_INVALID;
+            break;
           }
-          bool ok = (xn > left) && (xn < right);
-          if (!periodic) ok = ok && !(fabsf(xn) > half_l);
-          R.disp_att += 1;
-          if (ok) {
-            float de = 0.0f;
-            for (int chunk = 0;; ++chunk) {
-              const int k = chunk * W + kk;
-              int j = nm + side * k;
-              bool valid = true;
-              float shift = 0.0f;
-              if (!periodic) {
-                valid = j >= 0 && j < n;
-              } else if (j < 0) {
-                j += n;
-                shift = -lf;
-              } else if (j >= n) {
-                j -= n;
-                shift = lf;
-              }
-              float t_pair = 0.0f;
-              bool sat = false;
-              if (valid) {
-                const float xj = __fadd_rn(xs[j], shift);
-                const float dnw = side > 0 ? __fsub_rn(xj, xn) : __fsub_rn(xn, xj);
-                const float dol = side > 0 ? __fsub_rn(xj, xo) : __fsub_rn(xo, xj);
-                const float dn2 = __fmul_rn(dnw, dnw), do2 = __fmul_rn(dol, dol);
-                t_pair = __fsub_rn(pair_energy<kExact>(dn2, P), pair_energy<kExact>(do2, P));
-                sat = (k == (chunk + 1) * W) && (dn2 <= P.rc2 || do2 <= P.rc2);
-              }
-              de = __fadd_rn(de, group_sum<G>(t_pair, gmask));
-              pairs += 2 * G;
-              if (!__any_sync(gmask, sat)) break;
-              if (chunk == 0) R.window_overflows += 1;
-              if (periodic && 2 * (chunk + 2) * W > n - 1) {
-                err = JMM_ERR_INVALID;
-                break;
-              }
-            }
-            const bool acc = (de <= 0.0f) || (__fmul_rn(de, P.beta) < thr);
-            if (acc) {
-              if (gl == 0) xs[nm] = xn;
-              g.delta = __fadd_rn(g.delta, de);
-              R.disp_acc += 1;
-            }
-            __syncwarp(gmask);
-          }
-        } else {
-          // ---- volume move (fav), ln L or linear ----
-          double lnew;
-          float s;
-          double logw;  // weight term: (N+1) ln s or N ln(L'/L)
-          const float v = __fsub_rn(__fmul_rn(2.0f, u1), 1.0f);
-          if (cfg.vol_move == JMM_VOLMOVE_LNL) {
-            const float lns = __fmul_rn(P.vol_step, v);
-            s = portable_expf(lns);
-            lnew = __dmul_rn(L, (double)s);
-            logw = __dmul_rn((double)(n + 1), (double)lns);
-          } else {
-            const double dl = (double)__fmul_rn(P.vol_step, v);
-            lnew = __dadd_rn(L, dl);
-            const double ratio = __ddiv_rn(lnew, L);
-            s = (float)ratio;
-            logw = lnew > 0.0 ? __dmul_rn((double)n, log(ratio)) : -INFINITY;
-          }
-          double uo, un;
-          const float lnf = (float)lnew;
-          group_energies<G, kExact, true>(xs, P, gl, gmask, periodic, lf, s, lnf, uo, un, pairs,
-                                          err);
-          const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
-          if (drift > R.max_drift) R.max_drift = drift;
-          const double du = __dsub_rn(un, uo);
-          const double arg = __dsub_rn(
-              __dmul_rn(P.beta_d, __dadd_rn(du, __dmul_rn(P.p, __dsub_rn(lnew, L)))), logw);
-          bool acc = arg < (double)thr;
-          if (!(lnew > 0.0)) acc = false;
-          if (periodic && !(lnew > 2.0 * (double)P.rc)) acc = false;
-          fold(g, R, L, (uint32_t)n);
-          R.vol_att += 1;
-          if (acc) {
-            for (int i = gl; i < n; i += G) xs[i] = __fmul_rn(xs[i], s);
-            L = lnew;
-            lf = (float)L;
-            half_l = (float)__dmul_rn(L, 0.5);
-            g.e0 = un;
-            R.vol_acc += 1;
-          } else {
-            g.e0 = uo;
-          }
-          __syncwarp(gmask);
         }
-        // ---- per-step sample (updateThermo) ----
-        g.sd = __fadd_rn(g.sd, g.delta);
-        g.sd2 = __fmaf_rn(g.delta, g.delta, g.sd2);
-        g.nseg += 1;
-        // ---- FP64 re-summation of constant-L chains ----
-        if (sweep_end && !npt && cfg.resum_sweeps > 0 &&
-            ++sweeps_since_resum >= (uint32_t)cfg.resum_sweeps) {
-          sweeps_since_resum = 0;
-          double uo, un;
-          group_energies<G, kExact, false>(xs, P, gl, gmask, periodic, lf, 1.0f, lf, uo, un,
-                                           pairs, err);
-          const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
-          if (drift > R.max_drift) R.max_drift = drift;
-          fold(g, R, L, (uint32_t)n);
-          g.e0 = uo;
+        f = 1;
+        overflows += 1;
+      }
+      const bool acc = ok && ((de <= 0.0f) || (__fmul_rn(de, P.beta) < thr));
+      const unsigned accbits = __ballot_sync(gmask, acc && wl == 0) >> lane_shift;
+      const unsigned okbits = __ballot_sync(gmask, ok && wl == 0) >> lane_shift;
+      // the first step of the round whose window saw an accepted earlier step
+      if (S > 1 && f > 1) {
+        int nms[S];
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2) nms[s2] = __shfl_sync(gmask, nmc, s2 * G, L);
+#pragma unroll
+        for (int s2 = 1; s2 < S; ++s2) {
+          bool conflict = ((satbits >> (s2 * G)) & kSlotBits) != 0;
+#pragma unroll
+          for (int s1 = 0; s1 < s2; ++s1) {
+            int dist = nms[s2] - nms[s1];
+            dist = dist < 0 ? -dist : dist;
+            if (PER) dist = min(dist, n - dist);
+            conflict = conflict || (((accbits >> (s1 * G)) & 1u) && dist <= W);
+          }
+          if (conflict && (uint32_t)s2 < f) f = s2;
         }
+      }
+      // commit steps 0 .. f-1 in order
+#pragma unroll
+      for (int s2 = 0; s2 < S; ++s2) {
+        if ((uint32_t)s2 < f) {
+          const float de_s = __shfl_sync(gmask, de, s2 * G, L);
+          if ((accbits >> (s2 * G)) & 1u) {
+            if (cl == s2 * G) xs[nmc] = xn;
+            g.delta = __fadd_rn(g.delta, de_s);
+            d_acc += 1;
+          }
+          g.sd = __fadd_rn(g.sd, g.delta);
+          g.sd2 = __fmaf_rn(g.delta, g.delta, g.sd2);
+        }
+      }
+      __syncwarp(gmask);
+      uint32_t nok = 0;
+#pragma unroll
+      for (int s2 = 0; s2 < S; ++s2) nok += ((uint32_t)s2 < f) ? ((okbits >> (s2 * G)) & 1u) : 0u;
+      pairs += (uint64_t)(2 * G) * (nok + ((okbits & 1u) ? extra_chunks : 0u));
+      d_att += f;
+      g.nseg += f;
+      base += f;
+      sweep_pos += f;
+    }
+    if (sweep_pos == spsw) {
+      sweep_pos = 0;
+      if (!npt && cfg.resum_sweeps > 0 && ++sweeps_since_resum >= (uint32_t)cfg.resum_sweeps) {
+        sweeps_since_resum = 0;
+        double uo, un;
+        group_energies<L, kExact, false>(xs, P, cl, gmask, PER, lf, 1.0f, lf, uo, un, pairs,
+                                         err);
+        const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
+        if (drift > R.max_drift) R.max_drift = drift;
+        fold(g, R, L_box, (uint32_t)n);
+        g.e0 = uo;
       }
     }
   }
-  fold(g, R, L, (uint32_t)n);
+  fold(g, R, L_box, (uint32_t)n);
   R.e = g.e0;
-  R.l = L;
+  R.l = L_box;
   R.steps = step0 + total;
   R.pair_evals = pairs;
+  R.disp_acc += d_acc;
+  R.disp_att += d_att;
+  R.vol_acc += v_acc;
+  R.vol_att += v_att;
+  R.window_overflows += overflows;
   if (!isfinite(R.e)) err = JMM_ERR_NUMERIC;
   R.error = err;
   __syncwarp(gmask);
-  for (int i = gl; i < n; i += G) xg[P.x_off + i] = xs[i];
-  if (gl == 0) res[P.id] = R;
+  for (int i = cl; i < n; i += L) xg[P.x_off + i] = xs[i];
+  if (cl == 0) res[P.id] = R;
+}
+
+template <int G, int S, bool kExact>
+__global__ void __launch_bounds__(256) chains_kernel(const ChainParams *__restrict__ prm,
+                                                     jmm_chain_result *__restrict__ res,
+                                                     float *__restrict__ xg, KernelCfg cfg) {
+  constexpr int L = G * S;
+  extern __shared__ float smem[];
+  const int cl = threadIdx.x % L;
+  const int cw = (threadIdx.x & 31) / L;
+  const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << (cw * L));
+  const uint32_t local = threadIdx.x / L;
+  const uint32_t slot = blockIdx.x * cfg.chains_per_block + local;
+  if (slot >= cfg.n_chains) return;
+  const ChainParams P = prm[slot];
+  uint32_t *ring = reinterpret_cast<uint32_t *>(smem) + local * kRingWords;
+  float *xs = smem + P.s_off;
+  for (int i = cl; i < (int)P.n; i += L) xs[i] = xg[P.x_off + i];
+  __syncwarp(gmask);
+  const bool periodic = cfg.boundary == JMM_BOUNDARY_PERIODIC;
+  switch (P.pot * 2 + (periodic ? 1 : 0)) {
+    case JMM_POT_LJCUT * 2:
+      run_chain<G, S, JMM_POT_LJCUT, false, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
+      break;
+    case JMM_POT_LJCUT * 2 + 1:
+      run_chain<G, S, JMM_POT_LJCUT, true, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
+      break;
+    case JMM_POT_SOFTSPHERE * 2:
+      run_chain<G, S, JMM_POT_SOFTSPHERE, false, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
+      break;
+    case JMM_POT_SOFTSPHERE * 2 + 1:
+      run_chain<G, S, JMM_POT_SOFTSPHERE, true, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
+      break;
+    case JMM_POT_GAUSS * 2:
+      run_chain<G, S, JMM_POT_GAUSS, false, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
+      break;
+    default:
+      run_chain<G, S, JMM_POT_GAUSS, true, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
+      break;
+  }
 }
 
 // Fresh FP64 energies of every chain (32 lanes per chain).

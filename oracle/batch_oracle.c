@@ -27,7 +27,8 @@ struct jmmo_batch {
   jmm_batch_config cfg;
   uint32_t n_chains;
   int fp64;
-  uint32_t g;
+  uint32_t g;      /* window lanes G of one trial move          */
+  uint32_t lanes;  /* lanes per chain G*S: energy-sum partition */
   jmm_chain_desc *chains;
   jmm_chain_result *res;
   float **xf;
@@ -406,7 +407,7 @@ static void run_chain(jmmo_batch *b, uint32_t c, uint64_t n_sweeps) {
           logw = lnew > 0.0 ? (double)n * log(ratio) : -INFINITY;
         }
         const float lnf = (float)lnew;
-        energies32(xs, P, G, periodic, lf, 1, s, lnf, &uo, &un, &pairs, &err);
+        energies32(xs, P, b->lanes, periodic, lf, 1, s, lnf, &uo, &un, &pairs, &err);
         const double drift = fabs((g.e0 + (double)g.delta) - uo);
         if (drift > R->max_drift) R->max_drift = drift;
         const double du = un - uo;
@@ -473,7 +474,7 @@ static void run_chain(jmmo_batch *b, uint32_t c, uint64_t n_sweeps) {
       sweeps_since_resum = 0;
       double uo, un;
       if (!fp64) {
-        energies32(xs, P, G, periodic, lf, 0, 1.0f, lf, &uo, &un, &pairs, &err);
+        energies32(xs, P, b->lanes, periodic, lf, 0, 1.0f, lf, &uo, &un, &pairs, &err);
         const double drift = fabs((g.e0 + (double)g.delta) - uo);
         if (drift > R->max_drift) R->max_drift = drift;
       } else {
@@ -521,6 +522,7 @@ jmmo_batch *jmmo_batch_create(const jmm_batch_config *cfg, const jmm_chain_desc 
   b->n_chains = n_chains;
   b->fp64 = fp64;
   b->g = cfg->lanes_per_chain ? cfg->lanes_per_chain : 8;
+  b->lanes = b->g * (cfg->steps_per_round ? cfg->steps_per_round : 32 / b->g);
   b->chains = (jmm_chain_desc *)malloc(n_chains * sizeof(jmm_chain_desc));
   memcpy(b->chains, chains, n_chains * sizeof(jmm_chain_desc));
   b->res = (jmm_chain_result *)calloc(n_chains, sizeof(jmm_chain_result));

@@ -66,15 +66,20 @@ EXACT_CASES = {
 }
 
 
-@pytest.mark.parametrize("lanes", [4, 8, 16, 32])
+SHAPES = [(8, 4), (8, 2), (16, 2), (16, 1), (32, 1)]
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=[f"{g}x{s}" for g, s in SHAPES])
 @pytest.mark.parametrize("case", sorted(EXACT_CASES))
-def test_batch_exact_matches_oracle(gpu, case, lanes):
+def test_batch_exact_matches_oracle(gpu, case, shape):
+    lanes, spr = shape
     spec = EXACT_CASES[case]
     rng = np.random.default_rng(abs(hash(case)) % (2 ** 32))
     chains = _mixed_chains(rng, 24, *spec["n"], ensemble=spec["ens"],
                            pots=spec.get("pots", (abi.JMM_POT_LJCUT,)))
     cfg = abi.make_batch_config(seed=11, precision=abi.JMM_PREC_EXACT, lanes_per_chain=lanes,
-                                init=abi.JMM_INIT_JITTER, jitter=0.05, **spec["cfg"])
+                                steps_per_round=spr, init=abi.JMM_INIT_JITTER, jitter=0.05,
+                                **spec["cfg"])
     gpu = ChainBatch(cfg, chains)
     ora = oracle_lib.OracleBatch(cfg, chains)
     _assert_same(gpu, ora, chains)  # initial lattice and energies
@@ -147,12 +152,13 @@ def test_batch_autotune_keeps_state(gpu):
     cfg = abi.make_batch_config(seed=6, precision=abi.JMM_PREC_EXACT)
     gpu = ChainBatch(cfg, chains)
     before = gpu.results()
-    g, c = gpu.autotune(trial_sweeps=2)
-    assert g in (4, 8, 16, 32) and c * g in (32, 64, 128, 256)
+    g, spr, c = gpu.autotune(trial_sweeps=2)
+    assert (g, spr) in SHAPES and c * g * spr in (32, 64, 128, 256)
     after = gpu.results()
     assert np.array_equal(before["e"], after["e"]) and np.array_equal(before["steps"], after["steps"])
     # the EXACT result does not depend on the block shape, only on the lanes
-    cfg2 = abi.make_batch_config(seed=6, precision=abi.JMM_PREC_EXACT, lanes_per_chain=g)
+    cfg2 = abi.make_batch_config(seed=6, precision=abi.JMM_PREC_EXACT, lanes_per_chain=g,
+                                 steps_per_round=spr)
     ora = oracle_lib.OracleBatch(cfg2, chains)
     gpu.run(5)
     ora.run(5)
