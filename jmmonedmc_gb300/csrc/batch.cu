@@ -26,15 +26,39 @@ constexpr size_t kMaxSmem = 227 * 1024;
 
 typedef void (*ChainsKernel)(const ChainParams *, jmm_chain_result *, float *, KernelCfg);
 
+template <int G, int S, bool E>
+ChainsKernel pick_pot(int pot, bool per) {
+  switch (pot * 2 + (per ? 1 : 0)) {
+    case JMM_POT_LJCUT * 2: return chains_kernel<G, S, JMM_POT_LJCUT, false, E>;
+    case JMM_POT_LJCUT * 2 + 1: return chains_kernel<G, S, JMM_POT_LJCUT, true, E>;
+    case JMM_POT_SOFTSPHERE * 2: return chains_kernel<G, S, JMM_POT_SOFTSPHERE, false, E>;
+    case JMM_POT_SOFTSPHERE * 2 + 1: return chains_kernel<G, S, JMM_POT_SOFTSPHERE, true, E>;
+    case JMM_POT_GAUSS * 2: return chains_kernel<G, S, JMM_POT_GAUSS, false, E>;
+    case JMM_POT_GAUSS * 2 + 1: return chains_kernel<G, S, JMM_POT_GAUSS, true, E>;
+    default: return nullptr;
+  }
+}
+
 // Launch shapes: G window lanes x S steps per round, G*S = 16 or 32 lanes.
-ChainsKernel pick_kernel(uint32_t g, uint32_t s, bool exact) {
-  if (g == 8 && s == 4) return exact ? chains_kernel<8, 4, true> : chains_kernel<8, 4, false>;
-  if (g == 8 && s == 2) return exact ? chains_kernel<8, 2, true> : chains_kernel<8, 2, false>;
-  if (g == 16 && s == 2) return exact ? chains_kernel<16, 2, true> : chains_kernel<16, 2, false>;
-  if (g == 16 && s == 1) return exact ? chains_kernel<16, 1, true> : chains_kernel<16, 1, false>;
-  if (g == 32 && s == 1) return exact ? chains_kernel<32, 1, true> : chains_kernel<32, 1, false>;
+ChainsKernel pick_kernel(uint32_t g, uint32_t s, bool exact, int pot, bool per) {
+  if (g == 8 && s == 4) return exact ? pick_pot<8, 4, true>(pot, per) : pick_pot<8, 4, false>(pot, per);
+  if (g == 8 && s == 2) return exact ? pick_pot<8, 2, true>(pot, per) : pick_pot<8, 2, false>(pot, per);
+  if (g == 16 && s == 2) return exact ? pick_pot<16, 2, true>(pot, per) : pick_pot<16, 2, false>(pot, per);
+  if (g == 16 && s == 1) return exact ? pick_pot<16, 1, true>(pot, per) : pick_pot<16, 1, false>(pot, per);
+  if (g == 32 && s == 1) return exact ? pick_pot<32, 1, true>(pot, per) : pick_pot<32, 1, false>(pot, per);
   return nullptr;
 }
+
+constexpr int kPots[3] = {JMM_POT_LJCUT, JMM_POT_SOFTSPHERE, JMM_POT_GAUSS};
+
+// The chains of one potential: a contiguous range of launch slots with its
+// own blocks and shared-memory size.
+struct PotClass {
+  int pot;
+  uint32_t first, count;
+  uint32_t n_blocks;
+  size_t smem;
+};
 
 uint64_t pad4(uint64_t n) { return (n + 3) & ~uint64_t(3); }
 
@@ -56,6 +80,9 @@ struct jmm_batch {
   size_t smem = 0;
   cudaStream_t stream = nullptr;
   std::map<uint64_t, cudaGraphExec_t> graphs;  // n_sweeps -> instantiated run
+  std::vector<PotClass> classes;
+  cudaStream_t side[3] = {nullptr, nullptr, nullptr};  // concurrent classes in a graph
+  cudaEvent_t fork = nullptr, join[3] = {nullptr, nullptr, nullptr};
 };
 
 static void drop_graphs(jmm_batch *b) {
@@ -70,75 +97,97 @@ static void batch_free(jmm_batch *b) {
   cudaFree(b->d_res);
   cudaFree(b->d_x);
   cudaFree(b->d_e);
+  for (int k = 0; k < 3; ++k) {
+    if (b->side[k]) cudaStreamDestroy(b->side[k]);
+    if (b->join[k]) cudaEventDestroy(b->join[k]);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
 
 // Per-chain kernel parameters for launch shape (g, spr, cpb); uploads them.
 static int apply_layout(jmm_batch *b, uint32_t g, uint32_t spr, uint32_t cpb) {
-  if (!pick_kernel(g, spr, false))
+  const bool per = b->cfg.boundary == JMM_BOUNDARY_PERIODIC;
+  const bool exact = b->cfg.precision == JMM_PREC_EXACT;
+  if (!pick_kernel(g, spr, false, JMM_POT_LJCUT, false))
     return fail(JMM_ERR_INVALID, "unsupported launch shape: lanes_per_chain x steps_per_round "
                 "must be 8x4, 8x2, 16x2, 16x1 or 32x1");
   const uint32_t lanes = g * spr;
   if (cpb == 0 || cpb * lanes > 256)
     return fail(JMM_ERR_INVALID, "chains_per_block * lanes per chain must be <= 256");
   const uint32_t w = g / 2;
-  if (b->cfg.boundary == JMM_BOUNDARY_PERIODIC) {
+  if (per) {
     for (const auto &c : b->chains)
       if (c.n < 2 * w + 1)
         return fail(JMM_ERR_INVALID, "periodic chains need N >= lanes_per_chain + 1");
   }
   std::vector<ChainParams> prm(b->n_chains);
-  size_t smem_max = 0;
-  const uint32_t n_blocks = (b->n_chains + cpb - 1) / cpb;
+  std::vector<PotClass> classes;
   const uint64_t ring_floats = (uint64_t)cpb * kRingWords;
-  for (uint32_t blk = 0; blk < n_blocks; ++blk) {
-    uint64_t s_off = ring_floats;
-    for (uint32_t k = 0; k < cpb; ++k) {
-      const uint32_t slot = blk * cpb + k;
-      if (slot >= b->n_chains) break;
-      const uint32_t id = b->order[slot];
-      const jmm_chain_desc &c = b->chains[id];
-      ChainParams &P = prm[slot];
-      memset(&P, 0, sizeof(P));
-      P.id = id;
-      P.n = c.n;
-      P.pot = (uint32_t)c.potential;
-      P.ensemble = (uint32_t)c.ensemble;
-      P.steps_per_sweep = c.ensemble == JMM_NPT ? c.n + 1 : c.n;
-      P.s_off = (uint32_t)s_off;
-      P.x_off = b->x_off[id];
-      P.eps4 = c.potential == JMM_POT_LJCUT ? (float)(4.0 * c.eps) : (float)c.eps;
-      P.sigma2 = (float)(c.sigma * c.sigma);
-      P.inv_sigma2 = (float)(1.0 / (c.sigma * c.sigma));
-      P.rc2 = (float)(c.cutoff * c.cutoff);
-      P.rc = (float)c.cutoff;
-      P.beta = (float)(1.0 / c.t);
-      P.beta_d = 1.0 / c.t;
-      P.p = c.p;
-      P.two_max_step = (float)(2.0 * c.max_step);
-      P.vol_step = (float)c.vol_step;
-      s_off += pad4(c.n);
+  uint32_t slot0 = 0;
+  for (int pot : kPots) {
+    PotClass pc;
+    pc.pot = pot;
+    pc.first = slot0;
+    pc.count = 0;
+    while (slot0 + pc.count < b->n_chains && b->chains[b->order[slot0 + pc.count]].potential == pot)
+      pc.count++;
+    pc.n_blocks = (pc.count + cpb - 1) / cpb;
+    pc.smem = 0;
+    for (uint32_t blk = 0; blk < pc.n_blocks; ++blk) {
+      uint64_t s_off = ring_floats;
+      for (uint32_t k = 0; k < cpb; ++k) {
+        const uint32_t local = blk * cpb + k;
+        if (local >= pc.count) break;
+        const uint32_t id = b->order[pc.first + local];
+        const jmm_chain_desc &c = b->chains[id];
+        ChainParams &P = prm[pc.first + local];
+        memset(&P, 0, sizeof(P));
+        P.id = id;
+        P.n = c.n;
+        P.pot = (uint32_t)c.potential;
+        P.ensemble = (uint32_t)c.ensemble;
+        P.steps_per_sweep = c.ensemble == JMM_NPT ? c.n + 1 : c.n;
+        P.s_off = (uint32_t)s_off;
+        P.x_off = b->x_off[id];
+        P.eps4 = c.potential == JMM_POT_LJCUT ? (float)(4.0 * c.eps) : (float)c.eps;
+        P.sigma2 = (float)(c.sigma * c.sigma);
+        P.inv_sigma2 = (float)(1.0 / (c.sigma * c.sigma));
+        P.rc2 = (float)(c.cutoff * c.cutoff);
+        P.rc = (float)c.cutoff;
+        P.beta = (float)(1.0 / c.t);
+        P.beta_d = 1.0 / c.t;
+        P.p = c.p;
+        P.two_max_step = (float)(2.0 * c.max_step);
+        P.vol_step = (float)c.vol_step;
+        s_off += pad4(c.n);
+      }
+      pc.smem = std::max(pc.smem, (size_t)s_off * sizeof(float));
     }
-    smem_max = std::max(smem_max, (size_t)s_off * sizeof(float));
+    if (pc.smem > kMaxSmem)
+      return fail(JMM_ERR_INVALID, "a block's chains need %zu bytes of shared memory (max %zu): "
+                  "lower chains_per_block", pc.smem, kMaxSmem);
+    if (pc.count) {
+      ChainsKernel kf = pick_kernel(g, spr, exact, pot, per);
+      JMM_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
+      classes.push_back(pc);
+    }
+    slot0 += pc.count;
   }
-  if (smem_max > kMaxSmem)
-    return fail(JMM_ERR_INVALID, "a block's chains need %zu bytes of shared memory (max %zu): "
-                "lower chains_per_block", smem_max, kMaxSmem);
-  ChainsKernel kf = pick_kernel(g, spr, b->cfg.precision == JMM_PREC_EXACT);
-  JMM_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
   JMM_CUDA(cudaMemcpy(b->d_params, prm.data(), prm.size() * sizeof(ChainParams),
                       cudaMemcpyHostToDevice));
   b->params.swap(prm);
+  b->classes.swap(classes);
   b->g = g;
   b->spr = spr;
   b->cpb = cpb;
-  b->n_blocks = n_blocks;
-  b->smem = smem_max;
   drop_graphs(b);
   return JMM_OK;
 }
 
+// One launch per potential class; with several classes they run on forked
+// streams that rejoin `s`, so that a graph holds them as parallel nodes.
 static int launch(jmm_batch *b, uint64_t n_sweeps, cudaStream_t s) {
   KernelCfg kc;
   kc.seed = b->cfg.seed;
@@ -147,11 +196,25 @@ static int launch(jmm_batch *b, uint64_t n_sweeps, cudaStream_t s) {
   kc.vol_move = b->cfg.vol_move;
   kc.vol_schedule = b->cfg.vol_schedule;
   kc.resum_sweeps = (int32_t)b->cfg.resum_sweeps;
-  kc.n_chains = b->n_chains;
   kc.chains_per_block = b->cpb;
-  ChainsKernel kf = pick_kernel(b->g, b->spr, b->cfg.precision == JMM_PREC_EXACT);
-  kf<<<b->n_blocks, b->g * b->spr * b->cpb, b->smem, s>>>(b->d_params, b->d_res, b->d_x, kc);
-  JMM_CUDA(cudaGetLastError());
+  const bool per = b->cfg.boundary == JMM_BOUNDARY_PERIODIC;
+  const bool exact = b->cfg.precision == JMM_PREC_EXACT;
+  const uint32_t threads = b->g * b->spr * b->cpb;
+  const bool fork = b->classes.size() > 1;
+  if (fork) JMM_CUDA(cudaEventRecord(b->fork, s));
+  for (size_t k = 0; k < b->classes.size(); ++k) {
+    const PotClass &pc = b->classes[k];
+    cudaStream_t st = fork ? b->side[k] : s;
+    if (fork) JMM_CUDA(cudaStreamWaitEvent(st, b->fork, 0));
+    kc.n_chains = pc.count;
+    ChainsKernel kf = pick_kernel(b->g, b->spr, exact, pc.pot, per);
+    kf<<<pc.n_blocks, threads, pc.smem, st>>>(b->d_params + pc.first, b->d_res, b->d_x, kc);
+    JMM_CUDA(cudaGetLastError());
+    if (fork) {
+      JMM_CUDA(cudaEventRecord(b->join[k], st));
+      JMM_CUDA(cudaStreamWaitEvent(s, b->join[k], 0));
+    }
+  }
   return JMM_OK;
 }
 
@@ -239,10 +302,17 @@ extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_des
   b->total_floats = off;
   b->order.resize(n_chains);
   std::iota(b->order.begin(), b->order.end(), 0u);
-  std::stable_sort(b->order.begin(), b->order.end(),
-                   [&](uint32_t a, uint32_t c) { return chains[a].n > chains[c].n; });
+  std::stable_sort(b->order.begin(), b->order.end(), [&](uint32_t a, uint32_t c) {
+    if (chains[a].potential != chains[c].potential) return chains[a].potential < chains[c].potential;
+    return chains[a].n > chains[c].n;
+  });
 
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+    e = cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_params, n_chains * sizeof(ChainParams));
   if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_res, n_chains * sizeof(jmm_chain_result));
   if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_x, b->total_floats * sizeof(float));

@@ -98,21 +98,6 @@ __device__ __forceinline__ float pair_energy(float d2, const ChainParams &P) {
   return d2 <= P.rc2 ? e : 0.0f;
 }
 
-// The same with the potential fixed at compile time (the step loop).
-template <int POT, bool kExact>
-__device__ __forceinline__ float pair_energy_t(float d2, const ChainParams &P) {
-  float e;
-  if (POT == JMM_POT_GAUSS) {
-    e = __fmul_rn(P.eps4, exp32<kExact>(-__fmul_rn(d2, P.inv_sigma2)));
-  } else {
-    const float inv2 = __fmul_rn(P.sigma2, rcp32<kExact>(d2));
-    const float inv6 = __fmul_rn(__fmul_rn(inv2, inv2), inv2);
-    e = (POT == JMM_POT_SOFTSPHERE) ? __fmul_rn(P.eps4, __fmul_rn(inv6, inv6))
-                                    : __fmul_rn(P.eps4, __fmul_rn(inv6, __fsub_rn(inv6, 1.0f)));
-  }
-  return d2 <= P.rc2 ? e : 0.0f;
-}
-
 template <int G>
 __device__ __forceinline__ float group_sum(float v, unsigned mask) {
 #pragma unroll
@@ -188,26 +173,56 @@ struct Seg {
   uint32_t nseg;   // steps sampled in the segment
 };
 
-__device__ __forceinline__ void fold(Seg &g, jmm_chain_result &R, double l, uint32_t n) {
-  const double nd = (double)g.nseg;
-  const double sdd = (double)g.sd, sd2d = (double)g.sd2;
-  const double lin = __dadd_rn(__dmul_rn(nd, g.e0), sdd);
-  R.sum_e = __dadd_rn(R.sum_e, lin);
-  R.sum_e2 = __dadd_rn(R.sum_e2, __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(nd, g.e0), g.e0),
-                                                     __dmul_rn(__dmul_rn(2.0, g.e0), sdd)),
-                                           sd2d));
-  R.sum_l = __dadd_rn(R.sum_l, __dmul_rn(nd, l));
-  R.sum_l2 = __dadd_rn(R.sum_l2, __dmul_rn(__dmul_rn(nd, l), l));
-  R.sum_le = __dadd_rn(R.sum_le, __dmul_rn(l, lin));
-  const double rho = __ddiv_rn((double)n, l);
-  R.sum_rho = __dadd_rn(R.sum_rho, __dmul_rn(nd, rho));
-  R.sum_rho2 = __dadd_rn(R.sum_rho2, __dmul_rn(__dmul_rn(nd, rho), rho));
-  R.samples += g.nseg;
+// Folds the segment into the chain's FP64 sums; the record lives in HBM and
+// only the chain's first lane (`writer`) updates it.
+__device__ __forceinline__ void fold(Seg &g, jmm_chain_result *__restrict__ rp, bool writer,
+                                     double l, uint32_t n) {
+  if (writer) {
+    const double nd = (double)g.nseg;
+    const double sdd = (double)g.sd, sd2d = (double)g.sd2;
+    const double lin = __dadd_rn(__dmul_rn(nd, g.e0), sdd);
+    rp->sum_e = __dadd_rn(rp->sum_e, lin);
+    rp->sum_e2 = __dadd_rn(rp->sum_e2,
+                           __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(nd, g.e0), g.e0),
+                                               __dmul_rn(__dmul_rn(2.0, g.e0), sdd)),
+                                     sd2d));
+    rp->sum_l = __dadd_rn(rp->sum_l, __dmul_rn(nd, l));
+    rp->sum_l2 = __dadd_rn(rp->sum_l2, __dmul_rn(__dmul_rn(nd, l), l));
+    rp->sum_le = __dadd_rn(rp->sum_le, __dmul_rn(l, lin));
+    const double rho = __ddiv_rn((double)n, l);
+    rp->sum_rho = __dadd_rn(rp->sum_rho, __dmul_rn(nd, rho));
+    rp->sum_rho2 = __dadd_rn(rp->sum_rho2, __dmul_rn(__dmul_rn(nd, rho), rho));
+    rp->samples += g.nseg;
+  }
   g.e0 = __dadd_rn(g.e0, (double)g.delta);
   g.delta = 0.0f;
   g.sd = 0.0f;
   g.sd2 = 0.0f;
   g.nseg = 0;
+}
+
+__device__ __forceinline__ void note_drift(jmm_chain_result *__restrict__ rp, bool writer,
+                                           double drift) {
+  if (writer && drift > rp->max_drift) rp->max_drift = drift;
+}
+
+// The per-chain constants of the step loop, kept in registers.
+struct Hot {
+  float eps4, sigma2, inv_sigma2, rc2, beta, two_max_step;
+};
+
+template <int POT, bool kExact>
+__device__ __forceinline__ float pair_energy_h(float d2, const Hot &H) {
+  float e;
+  if (POT == JMM_POT_GAUSS) {
+    e = __fmul_rn(H.eps4, exp32<kExact>(-__fmul_rn(d2, H.inv_sigma2)));
+  } else {
+    const float inv2 = __fmul_rn(H.sigma2, rcp32<kExact>(d2));
+    const float inv6 = __fmul_rn(__fmul_rn(inv2, inv2), inv2);
+    e = (POT == JMM_POT_SOFTSPHERE) ? __fmul_rn(H.eps4, __fmul_rn(inv6, inv6))
+                                    : __fmul_rn(H.eps4, __fmul_rn(inv6, __fsub_rn(inv6, 1.0f)));
+  }
+  return d2 <= H.rc2 ? e : 0.0f;
 }
 
 // The Metropolis threshold -ln u, u the midpoint of the 23-bit cell of w
@@ -242,9 +257,9 @@ __device__ __forceinline__ int window_index(int nm, int side, int k, int n, floa
 
 // One chain for one launch: n_sweeps sweeps in speculative rounds of S steps.
 template <int G, int S, int POT, bool PER, bool kExact>
-__device__ __noinline__ void run_chain(const ChainParams &P, jmm_chain_result *__restrict__ res,
-                                       float *__restrict__ xg, float *xs, uint32_t *ring,
-                                       const KernelCfg &cfg, int cl, unsigned gmask) {
+__device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result *__restrict__ res,
+                                          float *__restrict__ xg, float *xs, uint32_t *ring,
+                                          const KernelCfg &cfg, int cl, unsigned gmask) {
   constexpr int W = G / 2;
   constexpr int L = G * S;
   constexpr unsigned kSlotBits = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
@@ -254,29 +269,38 @@ __device__ __noinline__ void run_chain(const ChainParams &P, jmm_chain_result *_
   const int side = wl < W ? -1 : 1;
   const int kk = wl % W + 1;
   const int lane_shift = (int)(threadIdx.x & 31) - cl;  // first lane of the chain in the warp
+  const bool writer = cl == 0;
   uint32_t *ring_w0 = ring;
   float *ring_u1 = reinterpret_cast<float *>(ring + kRingSteps);
   float *ring_thr = reinterpret_cast<float *>(ring + 2 * kRingSteps);
+  Hot H;
+  H.eps4 = P.eps4;
+  H.sigma2 = P.sigma2;
+  H.inv_sigma2 = P.inv_sigma2;
+  H.rc2 = P.rc2;
+  H.beta = P.beta;
+  H.two_max_step = P.two_max_step;
 
-  jmm_chain_result R = res[P.id];
+  jmm_chain_result *rp = res + P.id;
   const bool npt = P.ensemble == JMM_NPT;
   const bool per_sweep = cfg.vol_schedule == JMM_VOLSCHED_SWEEP;
-  double L_box = R.l;
+  double L_box = rp->l;
   float lf = (float)L_box, half_l = (float)__dmul_rn(L_box, 0.5);
   Seg g;
-  g.e0 = R.e;
+  g.e0 = rp->e;
   g.delta = 0.0f;
   g.sd = 0.0f;
   g.sd2 = 0.0f;
   g.nseg = 0;
   const uint32_t spsw = P.steps_per_sweep;
-  uint32_t sweep_pos = (uint32_t)(R.steps % spsw);
+  const uint64_t step0 = rp->steps;
+  uint32_t sweep_pos = (uint32_t)(step0 % spsw);
   uint32_t sweeps_since_resum = 0;
-  uint32_t err = R.error;
-  uint64_t pairs = R.pair_evals;
+  uint32_t err = rp->error;
+  uint64_t pairs = rp->pair_evals;
   uint32_t d_acc = 0, d_att = 0, v_acc = 0, v_att = 0, overflows = 0;
   const uint32_t total = (uint32_t)(cfg.n_sweeps * (uint64_t)spsw);
-  const uint64_t step0 = R.steps;
+  __syncwarp(gmask);  // every lane has read the record before lane 0 updates it
 
   uint32_t base = 0, pbase = 0;
   bool ring_valid = false;
@@ -317,7 +341,10 @@ __device__ __noinline__ void run_chain(const ChainParams &P, jmm_chain_result *_
       double lnew;
       float s;
       double logw;  // weight term: (N+1) ln s or N ln(L'/L)
-      const float v = __fsub_rn(__fmul_rn(2.0f, u1), 1.0f);
+      // the volume step is slot 0's: every lane takes its uniforms
+      const float u1_0 = __shfl_sync(gmask, u1, 0, L);
+      const float thr_0 = __shfl_sync(gmask, thr, 0, L);
+      const float v = __fsub_rn(__fmul_rn(2.0f, u1_0), 1.0f);
       if (cfg.vol_move == JMM_VOLMOVE_LNL) {
         const float lns = __fmul_rn(P.vol_step, v);
         s = portable_expf(lns);
@@ -334,14 +361,14 @@ __device__ __noinline__ void run_chain(const ChainParams &P, jmm_chain_result *_
       const float lnf = (float)lnew;
       group_energies<L, kExact, true>(xs, P, cl, gmask, PER, lf, s, lnf, uo, un, pairs, err);
       const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
-      if (drift > R.max_drift) R.max_drift = drift;
+      note_drift(rp, writer, drift);
       const double du = __dsub_rn(un, uo);
       const double arg = __dsub_rn(
           __dmul_rn(P.beta_d, __dadd_rn(du, __dmul_rn(P.p, __dsub_rn(lnew, L_box)))), logw);
-      bool acc = arg < (double)thr;
+      bool acc = arg < (double)thr_0;
       if (!(lnew > 0.0)) acc = false;
       if (PER && !(lnew > 2.0 * (double)P.rc)) acc = false;
-      fold(g, R, L_box, (uint32_t)n);
+      fold(g, rp, writer, L_box, (uint32_t)n);
       v_att += 1;
       if (acc) {
         for (int i = cl; i < n; i += L) xs[i] = __fmul_rn(xs[i], s);
@@ -363,7 +390,7 @@ __device__ __noinline__ void run_chain(const ChainParams &P, jmm_chain_result *_
       if (volbits) rem = min(rem, (uint32_t)(__ffs(volbits) - 1) / G);
       // ---- S displacement steps (qad2) from the current positions ----
       const int nmc = nm < n ? nm : n - 1;
-      const float md = __fmul_rn(__fsub_rn(u1, 0.5f), P.two_max_step);
+      const float md = __fmul_rn(__fsub_rn(u1, 0.5f), H.two_max_step);
       const float xo = xs[nmc];
       const float xn = __fadd_rn(xo, md);
       float left, right;
@@ -384,9 +411,9 @@ __device__ __noinline__ void run_chain(const ChainParams &P, jmm_chain_result *_
       const float dol = side > 0 ? __fsub_rn(xj, xo) : __fsub_rn(xo, xj);
       const float dn2 = __fmul_rn(dnw, dnw), do2 = __fmul_rn(dol, dol);
       const float t_pair =
-          inr ? __fsub_rn(pair_energy_t<POT, kExact>(dn2, P), pair_energy_t<POT, kExact>(do2, P))
+          inr ? __fsub_rn(pair_energy_h<POT, kExact>(dn2, H), pair_energy_h<POT, kExact>(do2, H))
               : 0.0f;
-      const bool sat = ok && inr && kk == W && (dn2 <= P.rc2 || do2 <= P.rc2);
+      const bool sat = ok && inr && kk == W && (dn2 <= H.rc2 || do2 <= H.rc2);
       float de = group_sum<G>(t_pair, gmask);
       const unsigned satbits = __ballot_sync(gmask, sat) >> lane_shift;
       uint32_t f = rem;
@@ -402,12 +429,12 @@ __device__ __noinline__ void run_chain(const ChainParams &P, jmm_chain_result *_
           const float dn_2 = side > 0 ? __fsub_rn(xj2, xn) : __fsub_rn(xn, xj2);
           const float do_2 = side > 0 ? __fsub_rn(xj2, xo) : __fsub_rn(xo, xj2);
           const float dn22 = __fmul_rn(dn_2, dn_2), do22 = __fmul_rn(do_2, do_2);
-          const float t2 = inr2 ? __fsub_rn(pair_energy_t<POT, kExact>(dn22, P),
-                                            pair_energy_t<POT, kExact>(do22, P))
+          const float t2 = inr2 ? __fsub_rn(pair_energy_h<POT, kExact>(dn22, H),
+                                            pair_energy_h<POT, kExact>(do22, H))
                                 : 0.0f;
           de = __fadd_rn(de, group_sum<G>(t2, gmask));
           extra_chunks += 1;
-          const bool sat2 = inr2 && (k == (chunk + 1) * W) && (dn22 <= P.rc2 || do22 <= P.rc2);
+          const bool sat2 = inr2 && (k == (chunk + 1) * W) && (dn22 <= H.rc2 || do22 <= H.rc2);
           if (!((__ballot_sync(gmask, sat2) >> lane_shift) & kSlotBits)) break;
           if (PER && 2 * (chunk + 2) * W > n - 1) {
             err = JMM_ERR_INVALID;
@@ -417,7 +444,7 @@ __device__ __noinline__ void run_chain(const ChainParams &P, jmm_chain_result *_
         f = 1;
         overflows += 1;
       }
-      const bool acc = ok && ((de <= 0.0f) || (__fmul_rn(de, P.beta) < thr));
+      const bool acc = ok && ((de <= 0.0f) || (__fmul_rn(de, H.beta) < thr));
       const unsigned accbits = __ballot_sync(gmask, acc && wl == 0) >> lane_shift;
       const unsigned okbits = __ballot_sync(gmask, ok && wl == 0) >> lane_shift;
       // the first step of the round whose window saw an accepted earlier step
@@ -470,31 +497,36 @@ __device__ __noinline__ void run_chain(const ChainParams &P, jmm_chain_result *_
         group_energies<L, kExact, false>(xs, P, cl, gmask, PER, lf, 1.0f, lf, uo, un, pairs,
                                          err);
         const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
-        if (drift > R.max_drift) R.max_drift = drift;
-        fold(g, R, L_box, (uint32_t)n);
+        note_drift(rp, writer, drift);
+        fold(g, rp, writer, L_box, (uint32_t)n);
         g.e0 = uo;
       }
     }
   }
-  fold(g, R, L_box, (uint32_t)n);
-  R.e = g.e0;
-  R.l = L_box;
-  R.steps = step0 + total;
-  R.pair_evals = pairs;
-  R.disp_acc += d_acc;
-  R.disp_att += d_att;
-  R.vol_acc += v_acc;
-  R.vol_att += v_att;
-  R.window_overflows += overflows;
-  if (!isfinite(R.e)) err = JMM_ERR_NUMERIC;
-  R.error = err;
+  fold(g, rp, writer, L_box, (uint32_t)n);
+  if (!isfinite(g.e0)) err = JMM_ERR_NUMERIC;
+  if (writer) {
+    rp->e = g.e0;
+    rp->l = L_box;
+    rp->steps = step0 + total;
+    rp->pair_evals = pairs;
+    rp->disp_acc += d_acc;
+    rp->disp_att += d_att;
+    rp->vol_acc += v_acc;
+    rp->vol_att += v_att;
+    rp->window_overflows += overflows;
+    rp->error = err;
+  }
   __syncwarp(gmask);
   for (int i = cl; i < n; i += L) xg[P.x_off + i] = xs[i];
-  if (cl == 0) res[P.id] = R;
 }
 
-template <int G, int S, bool kExact>
-__global__ void __launch_bounds__(256) chains_kernel(const ChainParams *__restrict__ prm,
+// One kernel per (shape, potential, boundary, precision): the chains of one
+// potential class, L lanes each, chains_per_block chains per block.
+// 72 registers keep 27 single-warp chains resident per SM (4096 chains on
+// 152 SMs in one wave).
+template <int G, int S, int POT, bool PER, bool kExact>
+__global__ void __maxnreg__(72) chains_kernel(const ChainParams *__restrict__ prm,
                                                      jmm_chain_result *__restrict__ res,
                                                      float *__restrict__ xg, KernelCfg cfg) {
   constexpr int L = G * S;
@@ -510,27 +542,7 @@ __global__ void __launch_bounds__(256) chains_kernel(const ChainParams *__restri
   float *xs = smem + P.s_off;
   for (int i = cl; i < (int)P.n; i += L) xs[i] = xg[P.x_off + i];
   __syncwarp(gmask);
-  const bool periodic = cfg.boundary == JMM_BOUNDARY_PERIODIC;
-  switch (P.pot * 2 + (periodic ? 1 : 0)) {
-    case JMM_POT_LJCUT * 2:
-      run_chain<G, S, JMM_POT_LJCUT, false, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
-      break;
-    case JMM_POT_LJCUT * 2 + 1:
-      run_chain<G, S, JMM_POT_LJCUT, true, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
-      break;
-    case JMM_POT_SOFTSPHERE * 2:
-      run_chain<G, S, JMM_POT_SOFTSPHERE, false, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
-      break;
-    case JMM_POT_SOFTSPHERE * 2 + 1:
-      run_chain<G, S, JMM_POT_SOFTSPHERE, true, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
-      break;
-    case JMM_POT_GAUSS * 2:
-      run_chain<G, S, JMM_POT_GAUSS, false, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
-      break;
-    default:
-      run_chain<G, S, JMM_POT_GAUSS, true, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
-      break;
-  }
+  run_chain<G, S, POT, PER, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
 }
 
 // Fresh FP64 energies of every chain (32 lanes per chain).
