@@ -41,6 +41,7 @@ ChainsKernel pick_pot(int pot, bool per) {
 
 // Launch shapes: G window lanes x S steps per round, G*S = 16 or 32 lanes.
 ChainsKernel pick_kernel(uint32_t g, uint32_t s, bool exact, int pot, bool per) {
+  if (g == 4 && s == 8) return exact ? pick_pot<4, 8, true>(pot, per) : pick_pot<4, 8, false>(pot, per);
   if (g == 8 && s == 4) return exact ? pick_pot<8, 4, true>(pot, per) : pick_pot<8, 4, false>(pot, per);
   if (g == 8 && s == 2) return exact ? pick_pot<8, 2, true>(pot, per) : pick_pot<8, 2, false>(pot, per);
   if (g == 16 && s == 2) return exact ? pick_pot<16, 2, true>(pot, per) : pick_pot<16, 2, false>(pot, per);
@@ -112,15 +113,15 @@ static int apply_layout(jmm_batch *b, uint32_t g, uint32_t spr, uint32_t cpb) {
   const bool exact = b->cfg.precision == JMM_PREC_EXACT;
   if (!pick_kernel(g, spr, false, JMM_POT_LJCUT, false))
     return fail(JMM_ERR_INVALID, "unsupported launch shape: lanes_per_chain x steps_per_round "
-                "must be 8x4, 8x2, 16x2, 16x1 or 32x1");
+                "must be 4x8, 8x4, 8x2, 16x2, 16x1 or 32x1");
   const uint32_t lanes = g * spr;
   if (cpb == 0 || cpb * lanes > 256)
     return fail(JMM_ERR_INVALID, "chains_per_block * lanes per chain must be <= 256");
-  const uint32_t w = g / 2;
+  const uint32_t w = (uint32_t)window_of((int)g);
   if (per) {
     for (const auto &c : b->chains)
       if (c.n < 2 * w + 1)
-        return fail(JMM_ERR_INVALID, "periodic chains need N >= lanes_per_chain + 1");
+        return fail(JMM_ERR_INVALID, "periodic chains need N > twice the neighbour window");
   }
   std::vector<ChainParams> prm(b->n_chains);
   std::vector<PotClass> classes;
@@ -532,7 +533,7 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
   float best = 1e30f;
   uint32_t best_g = g0, best_s = s0, best_c = c0;
   int rc = JMM_OK;
-  const uint32_t shapes[][2] = {{8, 4}, {8, 2}, {16, 2}, {16, 1}, {32, 1}};
+  const uint32_t shapes[][2] = {{4, 8}, {8, 4}, {8, 2}, {16, 2}, {16, 1}, {32, 1}};
   for (const auto &shape : shapes) {
     const uint32_t g = shape[0], spr = shape[1];
     for (uint32_t threads : {32u, 64u, 128u, 256u}) {

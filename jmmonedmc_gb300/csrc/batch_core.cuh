@@ -255,19 +255,33 @@ __device__ __forceinline__ int window_index(int nm, int side, int k, int n, floa
   return j;
 }
 
+// Neighbours looked at on each side of a moved particle for G lanes per step:
+// 4 for G <= 8 (two lanes per side each take two offsets when G = 4), G/2
+// beyond.
+__host__ __device__ constexpr int window_of(int g) { return g <= 8 ? 4 : g / 2; }
+
+__host__ __device__ constexpr unsigned leader_bits(int g, int s) {
+  unsigned m = 0;
+  for (int k = 0; k < s; ++k) m |= 1u << (k * g);
+  return m;
+}
+
 // One chain for one launch: n_sweeps sweeps in speculative rounds of S steps.
 template <int G, int S, int POT, bool PER, bool kExact>
 __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result *__restrict__ res,
                                           float *__restrict__ xg, float *xs, uint32_t *ring,
                                           const KernelCfg &cfg, int cl, unsigned gmask) {
-  constexpr int W = G / 2;
+  constexpr int W = window_of(G);   // neighbours looked at on each side
+  constexpr int H2 = G / 2;         // lanes per side
+  constexpr int KPL = W / H2;       // neighbours per lane
   constexpr int L = G * S;
   constexpr unsigned kSlotBits = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
+  constexpr unsigned kLeaders = leader_bits(G, S);  // lane s*G of every slot
   const int n = (int)P.n;
   const int slot = cl / G;
   const int wl = cl % G;
-  const int side = wl < W ? -1 : 1;
-  const int kk = wl % W + 1;
+  const int side = wl < H2 ? -1 : 1;
+  const int kb = wl % H2 + 1;  // this lane's offsets: kb, kb + H2, ...
   const int lane_shift = (int)(threadIdx.x & 31) - cl;  // first lane of the chain in the warp
   const bool writer = cl == 0;
   uint32_t *ring_w0 = ring;
@@ -298,6 +312,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
   uint32_t sweeps_since_resum = 0;
   uint32_t err = rp->error;
   uint64_t pairs = rp->pair_evals;
+  uint32_t pairs32 = 0;  // displacement pair energies of this launch
   uint32_t d_acc = 0, d_att = 0, v_acc = 0, v_att = 0, overflows = 0;
   const uint32_t total = (uint32_t)(cfg.n_sweeps * (uint64_t)spsw);
   __syncwarp(gmask);  // every lane has read the record before lane 0 updates it
@@ -403,38 +418,53 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       }
       bool ok = (xn > left) && (xn < right);
       if (!PER) ok = ok && !(fabsf(xn) > half_l);
-      bool inr;
-      float shift;
-      const int j = window_index<PER>(nmc, side, kk, n, lf, inr, shift);
-      const float xj = __fadd_rn(xs[j], shift);
-      const float dnw = side > 0 ? __fsub_rn(xj, xn) : __fsub_rn(xn, xj);
-      const float dol = side > 0 ? __fsub_rn(xj, xo) : __fsub_rn(xo, xj);
-      const float dn2 = __fmul_rn(dnw, dnw), do2 = __fmul_rn(dol, dol);
-      const float t_pair =
-          inr ? __fsub_rn(pair_energy_h<POT, kExact>(dn2, H), pair_energy_h<POT, kExact>(do2, H))
-              : 0.0f;
-      const bool sat = ok && inr && kk == W && (dn2 <= H.rc2 || do2 <= H.rc2);
-      float de = group_sum<G>(t_pair, gmask);
+      // this lane's KPL neighbours, summed in offset order
+      float t_lane = 0.0f;
+      bool sat = false;
+#pragma unroll
+      for (int q = 0; q < KPL; ++q) {
+        const int k = kb + q * H2;
+        bool inr;
+        float shift;
+        const int j = window_index<PER>(nmc, side, k, n, lf, inr, shift);
+        const float xj = __fadd_rn(xs[j], shift);
+        const float dnw = side > 0 ? __fsub_rn(xj, xn) : __fsub_rn(xn, xj);
+        const float dol = side > 0 ? __fsub_rn(xj, xo) : __fsub_rn(xo, xj);
+        const float dn2 = __fmul_rn(dnw, dnw), do2 = __fmul_rn(dol, dol);
+        const float tq = inr ? __fsub_rn(pair_energy_h<POT, kExact>(dn2, H),
+                                         pair_energy_h<POT, kExact>(do2, H))
+                             : 0.0f;
+        t_lane = q == 0 ? tq : __fadd_rn(t_lane, tq);
+        if (q == KPL - 1) sat = ok && inr && k == W && (dn2 <= H.rc2 || do2 <= H.rc2);
+      }
+      float de = group_sum<G>(t_lane, gmask);
       const unsigned satbits = __ballot_sync(gmask, sat) >> lane_shift;
       uint32_t f = rem;
       uint32_t extra_chunks = 0;
       if (satbits & kSlotBits) {
         // slow path: slot 0's window reaches beyond W; extend it chunk by chunk
         for (int chunk = 1;; ++chunk) {
-          const int k = chunk * W + kk;
-          bool inr2;
-          float shift2;
-          const int j2 = window_index<PER>(nmc, side, k, n, lf, inr2, shift2);
-          const float xj2 = __fadd_rn(xs[j2], shift2);
-          const float dn_2 = side > 0 ? __fsub_rn(xj2, xn) : __fsub_rn(xn, xj2);
-          const float do_2 = side > 0 ? __fsub_rn(xj2, xo) : __fsub_rn(xo, xj2);
-          const float dn22 = __fmul_rn(dn_2, dn_2), do22 = __fmul_rn(do_2, do_2);
-          const float t2 = inr2 ? __fsub_rn(pair_energy_h<POT, kExact>(dn22, H),
-                                            pair_energy_h<POT, kExact>(do22, H))
-                                : 0.0f;
+          float t2 = 0.0f;
+          bool sat2 = false;
+#pragma unroll
+          for (int q = 0; q < KPL; ++q) {
+            const int k = chunk * W + kb + q * H2;
+            bool inr2;
+            float shift2;
+            const int j2 = window_index<PER>(nmc, side, k, n, lf, inr2, shift2);
+            const float xj2 = __fadd_rn(xs[j2], shift2);
+            const float dn_2 = side > 0 ? __fsub_rn(xj2, xn) : __fsub_rn(xn, xj2);
+            const float do_2 = side > 0 ? __fsub_rn(xj2, xo) : __fsub_rn(xo, xj2);
+            const float dn22 = __fmul_rn(dn_2, dn_2), do22 = __fmul_rn(do_2, do_2);
+            const float tq = inr2 ? __fsub_rn(pair_energy_h<POT, kExact>(dn22, H),
+                                              pair_energy_h<POT, kExact>(do22, H))
+                                  : 0.0f;
+            t2 = q == 0 ? tq : __fadd_rn(t2, tq);
+            if (q == KPL - 1)
+              sat2 = inr2 && k == (chunk + 1) * W && (dn22 <= H.rc2 || do22 <= H.rc2);
+          }
           de = __fadd_rn(de, group_sum<G>(t2, gmask));
           extra_chunks += 1;
-          const bool sat2 = inr2 && (k == (chunk + 1) * W) && (dn22 <= H.rc2 || do22 <= H.rc2);
           if (!((__ballot_sync(gmask, sat2) >> lane_shift) & kSlotBits)) break;
           if (PER && 2 * (chunk + 2) * W > n - 1) {
             err = JMM_ERR_INVALID;
@@ -445,45 +475,42 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
         overflows += 1;
       }
       const bool acc = ok && ((de <= 0.0f) || (__fmul_rn(de, H.beta) < thr));
-      const unsigned accbits = __ballot_sync(gmask, acc && wl == 0) >> lane_shift;
-      const unsigned okbits = __ballot_sync(gmask, ok && wl == 0) >> lane_shift;
-      // the first step of the round whose window saw an accepted earlier step
+      const unsigned accbits = __ballot_sync(gmask, acc) >> lane_shift;
       if (S > 1 && f > 1) {
-        int nms[S];
+        // lane w of slot s2 checks earlier slots s1 = w, w + G, ... for an
+        // accepted move within W index positions of its own particle
+        bool conflict = false;
 #pragma unroll
-        for (int s2 = 0; s2 < S; ++s2) nms[s2] = __shfl_sync(gmask, nmc, s2 * G, L);
-#pragma unroll
-        for (int s2 = 1; s2 < S; ++s2) {
-          bool conflict = ((satbits >> (s2 * G)) & kSlotBits) != 0;
-#pragma unroll
-          for (int s1 = 0; s1 < s2; ++s1) {
-            int dist = nms[s2] - nms[s1];
-            dist = dist < 0 ? -dist : dist;
-            if (PER) dist = min(dist, n - dist);
-            conflict = conflict || (((accbits >> (s1 * G)) & 1u) && dist <= W);
-          }
-          if (conflict && (uint32_t)s2 < f) f = s2;
+        for (int r = 0; r < (S + G - 1) / G; ++r) {
+          const int s1 = wl + r * G;
+          const int nm1 = __shfl_sync(gmask, nmc, (s1 < S ? s1 : 0) * G, L);
+          int dist = nm1 - nmc;
+          dist = dist < 0 ? -dist : dist;
+          if (PER) dist = min(dist, n - dist);
+          conflict = conflict || (s1 < slot && ((accbits >> (s1 * G)) & 1u) && dist <= W);
         }
+        const unsigned cbits = (__ballot_sync(gmask, conflict) >> lane_shift) | satbits;
+        const unsigned late = cbits & ~kSlotBits;  // slots 1 .. S-1
+        if (late) f = min(f, (uint32_t)(__ffs(late) - 1) / G);
       }
-      // commit steps 0 .. f-1 in order
+      // commit steps 0 .. f-1 in order: positions by every slot leader at
+      // once (their particles are distinct or unmoved), statistics in order
+      const unsigned committed = f >= (uint32_t)S ? kLeaders : (kLeaders & ((1u << (f * G)) - 1u));
+      if (wl == 0 && (uint32_t)slot < f && acc) xs[nmc] = xn;
+      const float de_acc = acc ? de : 0.0f;
 #pragma unroll
       for (int s2 = 0; s2 < S; ++s2) {
+        const float d_s = __shfl_sync(gmask, de_acc, s2 * G, L);
         if ((uint32_t)s2 < f) {
-          const float de_s = __shfl_sync(gmask, de, s2 * G, L);
-          if ((accbits >> (s2 * G)) & 1u) {
-            if (cl == s2 * G) xs[nmc] = xn;
-            g.delta = __fadd_rn(g.delta, de_s);
-            d_acc += 1;
-          }
+          g.delta = __fadd_rn(g.delta, d_s);
           g.sd = __fadd_rn(g.sd, g.delta);
           g.sd2 = __fmaf_rn(g.delta, g.delta, g.sd2);
         }
       }
       __syncwarp(gmask);
-      uint32_t nok = 0;
-#pragma unroll
-      for (int s2 = 0; s2 < S; ++s2) nok += ((uint32_t)s2 < f) ? ((okbits >> (s2 * G)) & 1u) : 0u;
-      pairs += (uint64_t)(2 * G) * (nok + ((okbits & 1u) ? extra_chunks : 0u));
+      const unsigned okbits = __ballot_sync(gmask, ok) >> lane_shift;
+      d_acc += __popc(accbits & committed);
+      pairs32 += (uint32_t)(4 * W) * (__popc(okbits & committed) + ((okbits & 1u) ? extra_chunks : 0u));
       d_att += f;
       g.nseg += f;
       base += f;
@@ -509,7 +536,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
     rp->e = g.e0;
     rp->l = L_box;
     rp->steps = step0 + total;
-    rp->pair_evals = pairs;
+    rp->pair_evals = pairs + pairs32;
     rp->disp_acc += d_acc;
     rp->disp_att += d_att;
     rp->vol_acc += v_acc;

@@ -236,7 +236,7 @@ static void run_chain(jmmo_batch *b, uint32_t c, uint64_t n_sweeps) {
   const chain_prm Pv = make_prm(&b->chains[c], c);
   const chain_prm *P = &Pv;
   const int fp64 = b->fp64;
-  const uint32_t G = b->g, W = G / 2;
+  const uint32_t G = b->g, W = G <= 8 ? 4 : G / 2;
   const int n = (int)P->n;
   float *xs = fp64 ? NULL : b->xf[c];
   double *xd = fp64 ? b->xd[c] : NULL;
@@ -291,39 +291,50 @@ static void run_chain(jmmo_batch *b, uint32_t c, uint64_t n_sweeps) {
         }
         int ok = (xn > left) && (xn < right);
         if (!periodic) ok = ok && !(fabsf(xn) > half_l);
+        float de_acc = 0.0f;
         if (ok) {
+          /* lane w of the G lanes of a step: side -1 for w < G/2; offsets
+           * kb, kb + G/2, ... (kb = w % (G/2) + 1) up to the window W,
+           * summed in offset order, then the butterfly over the G lanes */
+          const int H2 = (int)G / 2;
+          const int KPL = (int)W / H2;
           float de = 0.0f;
           for (int chunk = 0;; ++chunk) {
             float v[32] = {0};
             int any_sat = 0;
             for (uint32_t gl = 0; gl < G; ++gl) {
-              const int side = gl < W ? -1 : 1;
-              const int k = chunk * (int)W + (int)(gl % W) + 1;
-              int j = nm + side * k;
-              int valid = 1;
-              float shift = 0.0f;
-              if (!periodic) {
-                valid = j >= 0 && j < n;
-              } else if (j < 0) {
-                j += n;
-                shift = -lf;
-              } else if (j >= n) {
-                j -= n;
-                shift = lf;
+              const int side = (int)gl < H2 ? -1 : 1;
+              const int kb = (int)gl % H2 + 1;
+              float tl = 0.0f;
+              for (int q = 0; q < KPL; ++q) {
+                const int k = chunk * (int)W + kb + q * H2;
+                int j = nm + side * k;
+                int valid = 1;
+                float shift = 0.0f;
+                if (!periodic) {
+                  valid = j >= 0 && j < n;
+                } else if (j < 0) {
+                  j += n;
+                  shift = -lf;
+                } else if (j >= n) {
+                  j -= n;
+                  shift = lf;
+                }
+                float tq = 0.0f;
+                if (valid) {
+                  const float xj = xs[j] + shift;
+                  const float dnw = side > 0 ? xj - xn : xn - xj;
+                  const float dol = side > 0 ? xj - xo : xo - xj;
+                  const float dn2 = dnw * dnw, do2 = dol * dol;
+                  tq = pair_e32(dn2, P) - pair_e32(do2, P);
+                  if (k == (chunk + 1) * (int)W && (dn2 <= P->rc2 || do2 <= P->rc2)) any_sat = 1;
+                }
+                tl = q == 0 ? tq : tl + tq;
               }
-              float tp = 0.0f;
-              if (valid) {
-                const float xj = xs[j] + shift;
-                const float dnw = side > 0 ? xj - xn : xn - xj;
-                const float dol = side > 0 ? xj - xo : xo - xj;
-                const float dn2 = dnw * dnw, do2 = dol * dol;
-                tp = pair_e32(dn2, P) - pair_e32(do2, P);
-                if (k == (chunk + 1) * (int)W && (dn2 <= P->rc2 || do2 <= P->rc2)) any_sat = 1;
-              }
-              v[gl] = tp;
+              v[gl] = tl;
             }
             de = de + butterfly32(v, G);
-            pairs += 2 * G;
+            pairs += 4 * W;
             if (!any_sat) break;
             if (chunk == 0) R->window_overflows += 1;
             if (periodic && 2 * (chunk + 2) * (int)W > n - 1) {
@@ -334,10 +345,11 @@ static void run_chain(jmmo_batch *b, uint32_t c, uint64_t n_sweeps) {
           const int acc = (de <= 0.0f) || (de * P->beta < thr);
           if (acc) {
             xs[nm] = xn;
-            g.delta = g.delta + de;
+            de_acc = de;
             R->disp_acc += 1;
           }
         }
+        g.delta = g.delta + de_acc;
       } else {
         const double u1 = (double)(w[1] >> 8) * (1.0 / 16777216.0);
         const double thr = threshold64(w[2]);
