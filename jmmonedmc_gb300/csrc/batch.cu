@@ -41,6 +41,8 @@ ChainsKernel pick_pot(int pot, bool per) {
 
 // Launch shapes: G window lanes x S steps per round, G*S = 16 or 32 lanes.
 ChainsKernel pick_kernel(uint32_t g, uint32_t s, bool exact, int pot, bool per) {
+  if (g == 4 && s == 4) return exact ? pick_pot<4, 4, true>(pot, per) : pick_pot<4, 4, false>(pot, per);
+  if (g == 4 && s == 2) return exact ? pick_pot<4, 2, true>(pot, per) : pick_pot<4, 2, false>(pot, per);
   if (g == 4 && s == 8) return exact ? pick_pot<4, 8, true>(pot, per) : pick_pot<4, 8, false>(pot, per);
   if (g == 8 && s == 4) return exact ? pick_pot<8, 4, true>(pot, per) : pick_pot<8, 4, false>(pot, per);
   if (g == 8 && s == 2) return exact ? pick_pot<8, 2, true>(pot, per) : pick_pot<8, 2, false>(pot, per);
@@ -113,7 +115,7 @@ static int apply_layout(jmm_batch *b, uint32_t g, uint32_t spr, uint32_t cpb) {
   const bool exact = b->cfg.precision == JMM_PREC_EXACT;
   if (!pick_kernel(g, spr, false, JMM_POT_LJCUT, false))
     return fail(JMM_ERR_INVALID, "unsupported launch shape: lanes_per_chain x steps_per_round "
-                "must be 4x8, 8x4, 8x2, 16x2, 16x1 or 32x1");
+                "must be 4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or 32x1");
   const uint32_t lanes = g * spr;
   if (cpb == 0 || cpb * lanes > 256)
     return fail(JMM_ERR_INVALID, "chains_per_block * lanes per chain must be <= 256");
@@ -162,7 +164,7 @@ static int apply_layout(jmm_batch *b, uint32_t g, uint32_t spr, uint32_t cpb) {
         P.p = c.p;
         P.two_max_step = (float)(2.0 * c.max_step);
         P.vol_step = (float)c.vol_step;
-        s_off += pad4(c.n);
+        s_off += pad4(c.n + 2 * kGhost);
       }
       pc.smem = std::max(pc.smem, (size_t)s_off * sizeof(float));
     }
@@ -339,7 +341,7 @@ extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_des
     batch_free(b);
     return rc;
   }
-  const uint32_t g = cfg->lanes_per_chain ? cfg->lanes_per_chain : 8;
+  const uint32_t g = cfg->lanes_per_chain ? cfg->lanes_per_chain : 4;
   const uint32_t spr = cfg->steps_per_round ? cfg->steps_per_round : (g <= 32 ? 32 / g : 1);
   const uint32_t cpb = cfg->chains_per_block ? cfg->chains_per_block : 128 / (g * spr ? g * spr : 1);
   rc = apply_layout(b, g, spr, cpb);
@@ -533,7 +535,7 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
   float best = 1e30f;
   uint32_t best_g = g0, best_s = s0, best_c = c0;
   int rc = JMM_OK;
-  const uint32_t shapes[][2] = {{4, 8}, {8, 4}, {8, 2}, {16, 2}, {16, 1}, {32, 1}};
+  const uint32_t shapes[][2] = {{4, 8}, {4, 4}, {4, 2}, {8, 4}, {8, 2}, {16, 2}, {16, 1}, {32, 1}};
   for (const auto &shape : shapes) {
     const uint32_t g = shape[0], spr = shape[1];
     for (uint32_t threads : {32u, 64u, 128u, 256u}) {

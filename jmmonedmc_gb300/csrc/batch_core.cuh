@@ -40,6 +40,11 @@ namespace batch {
 
 constexpr int kRingSteps = 32;  // Philox words drawn ahead per chain
 constexpr int kRingWords = 3 * kRingSteps;
+// Ghost slots on each side of a chain's positions in shared memory: far
+// sentinels between hard walls, periodic images on a ring, so that the
+// neighbour window is read without bounds tests.
+constexpr int kGhost = 16;
+constexpr float kFar = 1e30f;
 
 struct ChainParams {
   uint32_t id;               // user index: Philox stream and result slot
@@ -255,6 +260,22 @@ __device__ __forceinline__ int window_index(int nm, int side, int k, int n, floa
   return j;
 }
 
+// Ghost slots: far sentinels (hard walls) or the periodic images of the last
+// and first kGhost particles, x - L and x + L, as the wrap of the window
+// computes them.
+template <bool PER>
+__device__ __forceinline__ void set_ghosts(float *xs, int n, float lf, int cl, int lanes) {
+  for (int k = cl; k < kGhost; k += lanes) {
+    if (PER) {
+      xs[-1 - k] = k < n ? __fsub_rn(xs[n - 1 - k], lf) : -kFar;
+      xs[n + k] = k < n ? __fadd_rn(xs[k], lf) : kFar;
+    } else {
+      xs[-1 - k] = -kFar;
+      xs[n + k] = kFar;
+    }
+  }
+}
+
 // Neighbours looked at on each side of a moved particle for G lanes per step:
 // 4 for G <= 8 (two lanes per side each take two offsets when G = 4), G/2
 // beyond.
@@ -283,9 +304,10 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
   const int side = wl < H2 ? -1 : 1;
   const int kb = wl % H2 + 1;  // this lane's offsets: kb, kb + H2, ...
   const int lane_shift = (int)(threadIdx.x & 31) - cl;  // first lane of the chain in the warp
+  constexpr unsigned kChainBits = (L == 32) ? 0xffffffffu : ((1u << L) - 1u);
   const bool writer = cl == 0;
-  uint32_t *ring_w0 = ring;
-  float *ring_u1 = reinterpret_cast<float *>(ring + kRingSteps);
+  int32_t *ring_nm = reinterpret_cast<int32_t *>(ring);
+  float *ring_md = reinterpret_cast<float *>(ring + kRingSteps);  // md, or u1 of a volume step
   float *ring_thr = reinterpret_cast<float *>(ring + 2 * kRingSteps);
   Hot H;
   H.eps4 = P.eps4;
@@ -325,8 +347,16 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       __syncwarp(gmask);
       for (int e = cl; e < kRingSteps; e += L) {
         const Words4 w = step_words(cfg.seed, step0 + pbase + e + 1, P.id);
-        ring_w0[e] = w.w[0];
-        ring_u1[e] = word_to_unit_f(w.w[1]);
+        const float u1 = word_to_unit_f(w.w[1]);
+        int nm_e;
+        if (npt && !per_sweep) {
+          nm_e = (int)word_to_index(w.w[0], (uint64_t)n + 1);
+        } else {
+          nm_e = (int)word_to_index(w.w[0], (uint64_t)n);
+          if (npt && (sweep_pos + (uint32_t)e + 1) % spsw == 0) nm_e = n;  // the sweep's volume step
+        }
+        ring_nm[e] = nm_e;
+        ring_md[e] = nm_e == n ? u1 : __fmul_rn(__fsub_rn(u1, 0.5f), H.two_max_step);
         ring_thr[e] = threshold_of(w.w[2]);
       }
       __syncwarp(gmask);
@@ -336,20 +366,12 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
     if (rem > (uint32_t)S) rem = S;
     if (rem > spsw - sweep_pos) rem = spsw - sweep_pos;
     const uint32_t ri = base + slot - pbase;  // < 32
-    const uint32_t w0 = ring_w0[ri];
-    const float u1 = ring_u1[ri];
+    const int nm = ring_nm[ri];
+    const float u1 = ring_md[ri];  // md of a displacement, u1 of a volume step
     const float thr = ring_thr[ri];
-    int nm;
-    bool isvol;
-    if (npt && !per_sweep) {
-      nm = (int)word_to_index(w0, (uint64_t)n + 1);
-      isvol = nm == n;
-    } else {
-      nm = (int)word_to_index(w0, (uint64_t)n);
-      isvol = npt && (sweep_pos + (uint32_t)slot + 1 == spsw);
-    }
+    const bool isvol = nm == n;
     const unsigned volbits =
-        __ballot_sync(gmask, isvol && wl == 0 && (uint32_t)slot < rem) >> lane_shift;
+        (__ballot_sync(gmask, isvol && wl == 0 && (uint32_t)slot < rem) >> lane_shift & kChainBits);
 
     if (volbits & 1u) {
       // ---- volume move (fav), ln L or linear: all L lanes ----
@@ -390,6 +412,10 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
         L_box = lnew;
         lf = (float)L_box;
         half_l = (float)__dmul_rn(L_box, 0.5);
+        if (PER) {
+          __syncwarp(gmask);
+          set_ghosts<PER>(xs, n, lf, cl, L);
+        }
         g.e0 = un;
         v_acc += 1;
       } else {
@@ -405,17 +431,10 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       if (volbits) rem = min(rem, (uint32_t)(__ffs(volbits) - 1) / G);
       // ---- S displacement steps (qad2) from the current positions ----
       const int nmc = nm < n ? nm : n - 1;
-      const float md = __fmul_rn(__fsub_rn(u1, 0.5f), H.two_max_step);
+      const float md = u1;
       const float xo = xs[nmc];
       const float xn = __fadd_rn(xo, md);
-      float left, right;
-      if (PER) {
-        left = nmc > 0 ? xs[nmc - 1] : __fsub_rn(xs[n - 1], lf);
-        right = nmc + 1 < n ? xs[nmc + 1] : __fadd_rn(xs[0], lf);
-      } else {
-        left = nmc > 0 ? xs[nmc - 1] : -INFINITY;
-        right = nmc + 1 < n ? xs[nmc + 1] : INFINITY;
-      }
+      const float left = xs[nmc - 1], right = xs[nmc + 1];  // ghosts at the ends
       bool ok = (xn > left) && (xn < right);
       if (!PER) ok = ok && !(fabsf(xn) > half_l);
       // this lane's KPL neighbours, summed in offset order
@@ -424,21 +443,17 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
 #pragma unroll
       for (int q = 0; q < KPL; ++q) {
         const int k = kb + q * H2;
-        bool inr;
-        float shift;
-        const int j = window_index<PER>(nmc, side, k, n, lf, inr, shift);
-        const float xj = __fadd_rn(xs[j], shift);
+        const float xj = xs[nmc + side * k];  // a ghost beyond either end
         const float dnw = side > 0 ? __fsub_rn(xj, xn) : __fsub_rn(xn, xj);
         const float dol = side > 0 ? __fsub_rn(xj, xo) : __fsub_rn(xo, xj);
         const float dn2 = __fmul_rn(dnw, dnw), do2 = __fmul_rn(dol, dol);
-        const float tq = inr ? __fsub_rn(pair_energy_h<POT, kExact>(dn2, H),
-                                         pair_energy_h<POT, kExact>(do2, H))
-                             : 0.0f;
+        const float tq =
+            __fsub_rn(pair_energy_h<POT, kExact>(dn2, H), pair_energy_h<POT, kExact>(do2, H));
         t_lane = q == 0 ? tq : __fadd_rn(t_lane, tq);
-        if (q == KPL - 1) sat = ok && inr && k == W && (dn2 <= H.rc2 || do2 <= H.rc2);
+        if (q == KPL - 1) sat = ok && k == W && (dn2 <= H.rc2 || do2 <= H.rc2);
       }
       float de = group_sum<G>(t_lane, gmask);
-      const unsigned satbits = __ballot_sync(gmask, sat) >> lane_shift;
+      const unsigned satbits = (__ballot_sync(gmask, sat) >> lane_shift & kChainBits);
       uint32_t f = rem;
       uint32_t extra_chunks = 0;
       if (satbits & kSlotBits) {
@@ -465,7 +480,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
           }
           de = __fadd_rn(de, group_sum<G>(t2, gmask));
           extra_chunks += 1;
-          if (!((__ballot_sync(gmask, sat2) >> lane_shift) & kSlotBits)) break;
+          if (!(((__ballot_sync(gmask, sat2) >> lane_shift & kChainBits)) & kSlotBits)) break;
           if (PER && 2 * (chunk + 2) * W > n - 1) {
             err = JMM_ERR_INVALID;
             break;
@@ -475,7 +490,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
         overflows += 1;
       }
       const bool acc = ok && ((de <= 0.0f) || (__fmul_rn(de, H.beta) < thr));
-      const unsigned accbits = __ballot_sync(gmask, acc) >> lane_shift;
+      const unsigned accbits = (__ballot_sync(gmask, acc) >> lane_shift & kChainBits);
       if (S > 1 && f > 1) {
         // lane w of slot s2 checks earlier slots s1 = w, w + G, ... for an
         // accepted move within W index positions of its own particle
@@ -489,14 +504,20 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
           if (PER) dist = min(dist, n - dist);
           conflict = conflict || (s1 < slot && ((accbits >> (s1 * G)) & 1u) && dist <= W);
         }
-        const unsigned cbits = (__ballot_sync(gmask, conflict) >> lane_shift) | satbits;
+        const unsigned cbits = ((__ballot_sync(gmask, conflict) >> lane_shift & kChainBits)) | satbits;
         const unsigned late = cbits & ~kSlotBits;  // slots 1 .. S-1
         if (late) f = min(f, (uint32_t)(__ffs(late) - 1) / G);
       }
       // commit steps 0 .. f-1 in order: positions by every slot leader at
       // once (their particles are distinct or unmoved), statistics in order
       const unsigned committed = f >= (uint32_t)S ? kLeaders : (kLeaders & ((1u << (f * G)) - 1u));
-      if (wl == 0 && (uint32_t)slot < f && acc) xs[nmc] = xn;
+      if (wl == 0 && (uint32_t)slot < f && acc) {
+        xs[nmc] = xn;
+        if (PER) {  // keep the periodic images of the first and last W particles
+          if (nmc < kGhost) xs[n + nmc] = __fadd_rn(xn, lf);
+          if (nmc >= n - kGhost) xs[nmc - n] = __fsub_rn(xn, lf);
+        }
+      }
       const float de_acc = acc ? de : 0.0f;
 #pragma unroll
       for (int s2 = 0; s2 < S; ++s2) {
@@ -508,7 +529,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
         }
       }
       __syncwarp(gmask);
-      const unsigned okbits = __ballot_sync(gmask, ok) >> lane_shift;
+      const unsigned okbits = (__ballot_sync(gmask, ok) >> lane_shift & kChainBits);
       d_acc += __popc(accbits & committed);
       pairs32 += (uint32_t)(4 * W) * (__popc(okbits & committed) + ((okbits & 1u) ? extra_chunks : 0u));
       d_att += f;
@@ -550,10 +571,11 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
 
 // One kernel per (shape, potential, boundary, precision): the chains of one
 // potential class, L lanes each, chains_per_block chains per block.
-// 72 registers keep 27 single-warp chains resident per SM (4096 chains on
-// 152 SMs in one wave).
+// A single-warp chain is held to 72 registers so that 27 of them stay
+// resident per SM (4096 chains on 152 SMs in one wave); chains that share a
+// warp (G*S < 32) may use 128.
 template <int G, int S, int POT, bool PER, bool kExact>
-__global__ void __maxnreg__(72) chains_kernel(const ChainParams *__restrict__ prm,
+__global__ void __maxnreg__(G * S == 32 ? 72 : 128) chains_kernel(const ChainParams *__restrict__ prm,
                                                      jmm_chain_result *__restrict__ res,
                                                      float *__restrict__ xg, KernelCfg cfg) {
   constexpr int L = G * S;
@@ -566,8 +588,10 @@ __global__ void __maxnreg__(72) chains_kernel(const ChainParams *__restrict__ pr
   if (slot >= cfg.n_chains) return;
   const ChainParams P = prm[slot];
   uint32_t *ring = reinterpret_cast<uint32_t *>(smem) + local * kRingWords;
-  float *xs = smem + P.s_off;
+  float *xs = smem + P.s_off + kGhost;
   for (int i = cl; i < (int)P.n; i += L) xs[i] = xg[P.x_off + i];
+  __syncwarp(gmask);
+  set_ghosts<PER>(xs, (int)P.n, (float)res[P.id].l, cl, L);
   __syncwarp(gmask);
   run_chain<G, S, POT, PER, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
 }

@@ -533,7 +533,7 @@ jmmo_batch *jmmo_batch_create(const jmm_batch_config *cfg, const jmm_chain_desc 
   b->cfg = *cfg;
   b->n_chains = n_chains;
   b->fp64 = fp64;
-  b->g = cfg->lanes_per_chain ? cfg->lanes_per_chain : 8;
+  b->g = cfg->lanes_per_chain ? cfg->lanes_per_chain : 4;
   b->lanes = b->g * (cfg->steps_per_round ? cfg->steps_per_round : 32 / b->g);
   b->chains = (jmm_chain_desc *)malloc(n_chains * sizeof(jmm_chain_desc));
   memcpy(b->chains, chains, n_chains * sizeof(jmm_chain_desc));
