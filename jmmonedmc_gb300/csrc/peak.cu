@@ -30,8 +30,8 @@ __global__ void rcp_kernel(float *out) {
   for (int it = 0; it < kIters / 4; ++it) {
 #pragma unroll
     for (int c = 0; c < kChains; ++c) {
-      float y;
-      asm volatile("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(acc[c]));
+      float y;  // x <- 1 / (x + 1): one reciprocal and one add per link
+      asm volatile("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(acc[c] + 1.0f));
       acc[c] = y;
     }
   }
