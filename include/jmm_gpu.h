@@ -268,6 +268,21 @@ int jmm_batch_run_host(const jmm_batch_config *cfg, const jmm_chain_desc *chains
 int jmm_rng_words(uint64_t seed, uint64_t block0, uint32_t chain, uint64_t count,
                   uint32_t *out);
 
+/* Full FP64 pair sums (the nine totals that fad and ECheck form) of N
+ * positions held in device memory by the caller, written as nine doubles to
+ * the caller's device buffer `out`, enqueued on `stream` (cudaStream_t as
+ * void*, NULL = the default stream); no device memory is allocated or freed.
+ * It has no counterpart in the reference: it is for callers that cannot
+ * allocate -- code capturing a CUDA graph, hosts that reserve all device
+ * memory up front, per-step loops that cannot afford allocation latency.
+ * The pair terms go through one fixed device array shared by all calls,
+ * sized for N <= 256 (2.35 MB per GPU, held until exit): larger N fails with
+ * JMM_ERR_INVALID, and calls that overlap on the GPU race on that array.
+ * The first call on a device looks the array's address up; make it before
+ * any stream capture. */
+int jmm_plain_full_energy_noalloc(const jmm_params *params, const double *r, uint64_t n,
+                                  double l, double *out, void *stream);
+
 /* Roofline denominators measured live on the current device: FP32 FMA
  * throughput (TFLOP/s, 2 FLOP per FMA) and MUFU reciprocal throughput
  * (T ops/s), each the best of several event-timed launches. */

@@ -28,7 +28,7 @@ UNITS = {
     "plain.cu": ["-fmad=false"],
     "batch.cu": [],
     "grad.cu": [],
-    "noalloc.cu": [],
+    "noalloc.cu": ["-fmad=false"],
     "peak.cu": [],
 }
 
