@@ -145,6 +145,11 @@ int jmm_plain_fad(jmm_plain *h, uint64_t nm, double d);
  * log: NULL, or room for n_steps records. */
 int jmm_plain_steps(jmm_plain *h, uint64_t n_steps, const jmm_draw *replay,
                     jmm_step_record *log);
+/* One trial outside Step (qad2 of particle nm with trial uniform rn, or the
+ * volume move fav / qavLJ with rn), as the reference's qad/qad2/fav/qav when
+ * called directly (src/jmmMCState.cpp:1154-1464, :1642-1730, :2161-2293):
+ * no step increment, energy check or thermo update.  rec: NULL or one record. */
+int jmm_plain_move(jmm_plain *h, int32_t kind, uint64_t nm, double rn, jmm_step_record *rec);
 /* updateThermo on its own (the driver's step-0 call, src/Main.cpp:95). */
 int jmm_plain_update_thermo(jmm_plain *h);
 /* Zero the 12 thermo accumulators (what printThermo does after printing,

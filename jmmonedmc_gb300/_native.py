@@ -36,6 +36,7 @@ SIGNATURES = {
     "jmm_plain_set_config": [vp, P(dbl), u64, dbl, u64],
     "jmm_plain_fad": [vp, u64, dbl],
     "jmm_plain_steps": [vp, u64, vp, vp],
+    "jmm_plain_move": [vp, i32, u64, dbl, vp],
     "jmm_plain_update_thermo": [vp],
     "jmm_plain_reset_thermo": [vp],
     "jmm_plain_echeck": [vp, P(dbl), P(i32)],

@@ -598,6 +598,44 @@ __global__ void __launch_bounds__(kThreads, 1) echeck_kernel(Args a) {
   echeck(a, ctl);
 }
 
+// One trial of a given kind outside Step: qad2 of particle nm with trial
+// uniform rn, or the volume move (fav / qavLJ) with rn; no step increment,
+// energy check or thermo update (those belong to Step).
+__global__ void __launch_bounds__(kThreads, 1)
+    move_kernel(Args a, int32_t kind, uint64_t nm, double rn, jmm_step_record *rec) {
+  extern __shared__ double smem[];
+  __shared__ Ctl ctl;
+  const uint64_t nm1 = a.n - 1;
+  if (threadIdx.x == 0) {
+    ctl.nm = kind == JMM_KIND_VOLUME ? a.n : nm;
+    ctl.rn = rn;
+    ctl.outcome = JMM_OUT_REJECT;
+    ctl.ran = NAN;
+    ctl.bf = NAN;
+  }
+  __syncthreads();
+  if (kind == JMM_KIND_DISPLACEMENT)
+    qad2(a, ctl, smem, smem + 9 * nm1, nullptr);
+  else if (a.use_qavlj)
+    qav_lj(a, ctl, nullptr);
+  else
+    fav(a, ctl, nullptr);
+  if (threadIdx.x == 0 && rec) {
+    Scalars *S = a.s;
+    rec->sn = S->sn;
+    rec->nm = ctl.nm;
+    rec->rn = ctl.rn;
+    rec->ran = ctl.ran;
+    rec->bf = ctl.bf;
+    rec->e = S->tot[JMM_Q_E];
+    rec->vir = S->tot[JMM_Q_VIR];
+    rec->hv = S->tot[JMM_Q_HV];
+    rec->l = S->l;
+    rec->kind = kind;
+    rec->outcome = ctl.outcome;
+  }
+}
+
 __global__ void separations_kernel(Args a) {
   const uint64_t n = a.n;
   for (uint64_t ind = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; ind < a.nn;
@@ -733,6 +771,9 @@ extern "C" int jmm_plain_create(const jmm_params *prm, jmm_plain **out) {
   if (e == cudaSuccess && h->smem_bytes > 48 * 1024)
     e = cudaFuncSetAttribute(steps_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)h->smem_bytes);
+  if (e == cudaSuccess && h->smem_bytes > 48 * 1024)
+    e = cudaFuncSetAttribute(move_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)h->smem_bytes);
   if (e != cudaSuccess) {
     rc = cuda_status(e, "jmm_plain_create set-up", __FILE__, __LINE__);
     plain_free(h);
@@ -836,6 +877,28 @@ extern "C" int jmm_plain_steps(jmm_plain *h, uint64_t n_steps, const jmm_draw *r
   int rc = get_scalars(h, &s);
   if (rc) return rc;
   if (s.error) return fail((int)s.error, "jmm_plain_steps: kernel reported error %u", s.error);
+  return JMM_OK;
+}
+
+extern "C" int jmm_plain_move(jmm_plain *h, int32_t kind, uint64_t nm, double rn,
+                              jmm_step_record *rec) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  JMM_CHECK_ARG(kind == JMM_KIND_DISPLACEMENT || kind == JMM_KIND_VOLUME, "unknown move kind");
+  JMM_CHECK_ARG(kind == JMM_KIND_VOLUME || nm < h->a.n, "particle index out of range");
+  JMM_CHECK_ARG(kind == JMM_KIND_DISPLACEMENT || h->prm.ensemble == JMM_NPT,
+                "volume moves need the NPT ensemble");
+  if (!h->initialised) return fail(JMM_ERR_STATE, "jmm_plain_move: run jmm_plain_fad first");
+  if (rec && h->log_cap < 1) {
+    cudaFree(h->d_log);
+    h->d_log = nullptr;
+    JMM_CUDA(cudaMalloc((void **)&h->d_log, sizeof(jmm_step_record)));
+    h->log_cap = 1;
+  }
+  move_kernel<<<1, kThreads, h->smem_bytes>>>(h->a, kind, nm, rn, rec ? h->d_log : nullptr);
+  int rc = plain_sync("move_kernel");
+  if (rc) return rc;
+  if (rec) JMM_CUDA(cudaMemcpy(rec, h->d_log, sizeof(jmm_step_record), cudaMemcpyDeviceToHost));
   return JMM_OK;
 }
 

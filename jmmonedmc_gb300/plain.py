@@ -65,6 +65,12 @@ class PlainChain:
             return np.frombuffer(rec, dtype=np.dtype(abi.STEP_RECORD_DTYPE)).copy()
         return None
 
+    def move(self, kind, nm, rn):
+        """One trial outside Step (qad2 of particle nm, or the volume move)."""
+        rec = abi.StepRecord()
+        _native.call("jmm_plain_move", self._h, kind, nm, rn, C.byref(rec))
+        return rec
+
     def set_config(self, r, l, sn=0):
         r = np.ascontiguousarray(r, dtype=np.float64)
         _native.call("jmm_plain_set_config", self._h,

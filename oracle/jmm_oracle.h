@@ -19,6 +19,7 @@ int jmmo_plain_set_config(jmmo_plain *h, const double *r, uint64_t n, double l, 
 int jmmo_plain_fad(jmmo_plain *h, uint64_t nm, double d);
 int jmmo_plain_steps(jmmo_plain *h, uint64_t n_steps, const jmm_draw *replay,
                      jmm_step_record *log);
+int jmmo_plain_move(jmmo_plain *h, int32_t kind, uint64_t nm, double rn, jmm_step_record *rec);
 int jmmo_plain_update_thermo(jmmo_plain *h);
 int jmmo_plain_reset_thermo(jmmo_plain *h);
 int jmmo_plain_echeck(jmmo_plain *h, double *e_test, int32_t *reset);

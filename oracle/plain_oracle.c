@@ -582,3 +582,19 @@ void jmmo_philox_raw(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[
 void jmmo_step_words_export(uint64_t seed, uint64_t block, uint32_t chain, uint32_t out[4]) {
   jmmo_step_words(seed, block, chain, out);
 }
+
+/* One trial outside Step (the reference's qad2/fav/qavLJ called directly). */
+int jmmo_plain_move(jmmo_plain *h, int32_t kind, uint64_t nm, double rn, jmm_step_record *rec) {
+  double ran = NAN, bf = NAN;
+  int outcome;
+  if (kind == JMM_KIND_DISPLACEMENT) {
+    if (nm >= h->n) return JMM_ERR_INVALID;
+    outcome = qad2(h, nm, rn, NULL, &ran, &bf);
+  } else if (h->prm.potential == JMM_POT_LJ && h->prm.nbn < 0) {
+    outcome = qav_lj(h, rn, NULL, &ran, &bf);
+  } else {
+    outcome = fav(h, rn, NULL, &ran, &bf);
+  }
+  set_record(rec, h, kind == JMM_KIND_VOLUME ? h->n : nm, rn, ran, bf, kind, outcome);
+  return JMM_OK;
+}

@@ -23,6 +23,7 @@ SIGS = {
     "jmmo_plain_set_config": ([vp, P(dbl), u64, dbl, u64], C.c_int),
     "jmmo_plain_fad": ([vp, u64, dbl], C.c_int),
     "jmmo_plain_steps": ([vp, u64, vp, vp], C.c_int),
+    "jmmo_plain_move": ([vp, i32, u64, dbl, vp], C.c_int),
     "jmmo_plain_update_thermo": ([vp], C.c_int),
     "jmmo_plain_reset_thermo": ([vp], C.c_int),
     "jmmo_plain_echeck": ([vp, P(dbl), P(i32)], C.c_int),
@@ -105,6 +106,11 @@ class OraclePlain:
         if rec is not None:
             return np.frombuffer(rec, dtype=np.dtype(abi.STEP_RECORD_DTYPE)).copy()
         return None
+
+    def move(self, kind, nm, rn):
+        rec = abi.StepRecord()
+        _ok(self.lib.jmmo_plain_move(self._h, kind, nm, rn, C.byref(rec)), "move")
+        return rec
 
     def set_config(self, r, l, sn=0):
         r = np.ascontiguousarray(r, dtype=np.float64)

@@ -127,3 +127,19 @@ def test_plain_gpu_rejects_bad_arguments(gpu):
         c.steps(1)  # before fad: out of order
     with pytest.raises(JmmError):
         c.fad(nm=10)
+
+
+def test_plain_gpu_direct_moves_match_oracle(gpu):
+    """qad2 / fav called outside Step (jmm_plain_move), draws from the stream."""
+    params = abi.make_params(n=50, ensemble=abi.JMM_NPT, p=1.0, t=1.0, cutoff=3.0,
+                             max_step=0.3, max_dl=1.0, seed=17)
+    g, o = PlainChain(params), oracle_lib.OraclePlain(params)
+    g.fad()
+    o.fad()
+    rng = np.random.default_rng(2)
+    for k in range(300):
+        kind = abi.JMM_KIND_VOLUME if k % 7 == 0 else abi.JMM_KIND_DISPLACEMENT
+        nm, rn = int(rng.integers(0, 50)), float(rng.random())
+        rg, ro = g.move(kind, nm, rn), o.move(kind, nm, rn)
+        assert rg.outcome == ro.outcome and rg.e == ro.e and rg.l == ro.l, k
+    np.testing.assert_array_equal(gc.bits(g.positions()), gc.bits(o.positions()))
