@@ -262,6 +262,46 @@ int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t *lanes_per_
                        uint32_t *steps_per_round, uint32_t *chains_per_block);
 int jmm_batch_destroy(jmm_batch *b);
 
+/* ---- energy gradients (the backward of U) ------------------------------ */
+
+/* One chain configuration for jmm_energy_grad. */
+typedef struct jmm_grad_chain {
+  uint64_t x_off;      /* float offset of the chain's positions                */
+  uint32_t n;
+  int32_t potential;   /* JMM_POT_LJCUT | JMM_POT_SOFTSPHERE | JMM_POT_GAUSS   */
+  double eps;
+  double sigma;
+  double cutoff;
+  double l;            /* box length                                          */
+} jmm_grad_chain;
+
+/* Per-chain gradient statistics of a sampled run (FP64): the moments the
+ * fluctuation formulas d<A>/dtheta = -beta(<A dU/dtheta> - <A><dU/dtheta>)
+ * need, for theta = eps, sigma, L (g[0], g[1], g[2]). */
+typedef struct jmm_grad_stats {
+  uint64_t samples;
+  double sum_u, sum_u2, sum_rho, sum_rho2, sum_l;
+  double sum_g[3];
+  double sum_u_g[3];
+  double sum_rho_g[3];
+  double sum_l_g[3];
+} jmm_grad_stats;
+
+/* U, dU/deps, dU/dsigma and dU/dL (positions scaled with the box) of every
+ * configuration, as out[4k .. 4k+3] (FP64), with FP32 pair terms and FP64
+ * sums; forces: NULL, or -dU/dx per particle at the chains' offsets.
+ * chains, x, out and forces are device pointers; enqueued on stream (a
+ * cudaStream_t as void*, NULL = the default stream), no wait. */
+int jmm_energy_grad(const jmm_grad_chain *chains, uint32_t n_chains, const float *x,
+                    int32_t boundary, double *out, float *forces, void *stream);
+/* The same for a batch's current configurations, into host memory. */
+int jmm_batch_energy_grad(jmm_batch *b, double *out, uint32_t n_chains);
+/* n_sweeps sweeps; after every sample_every sweeps the configuration of every
+ * chain and its energy gradient are added to the chain's jmm_grad_stats (one
+ * CUDA graph: chain kernel, gradient kernel, chain kernel, ...). */
+int jmm_batch_run_sampled(jmm_batch *b, uint64_t n_sweeps, uint32_t sample_every);
+int jmm_batch_grad_stats(jmm_batch *b, jmm_grad_stats *out, uint32_t n_chains);
+
 /* Host-buffer convenience: create, upload positions (NULL = the configured
  * initial lattice), run n_sweeps, copy results and positions back, destroy. */
 int jmm_batch_run_host(const jmm_batch_config *cfg, const jmm_chain_desc *chains,

@@ -244,3 +244,38 @@ def make_batch_config(seed=1, boundary=JMM_BOUNDARY_WALLS, vol_move=JMM_VOLMOVE_
     c.init = init
     c.jitter = jitter
     return c
+
+
+# ---- energy gradients -------------------------------------------------------
+class GradChain(C.Structure):
+    _fields_ = [
+        ("x_off", C.c_uint64),
+        ("n", C.c_uint32),
+        ("potential", C.c_int32),
+        ("eps", C.c_double),
+        ("sigma", C.c_double),
+        ("cutoff", C.c_double),
+        ("l", C.c_double),
+    ]
+
+
+class GradStats(C.Structure):
+    _fields_ = [
+        ("samples", C.c_uint64),
+        ("sum_u", C.c_double),
+        ("sum_u2", C.c_double),
+        ("sum_rho", C.c_double),
+        ("sum_rho2", C.c_double),
+        ("sum_l", C.c_double),
+        ("sum_g", C.c_double * 3),
+        ("sum_u_g", C.c_double * 3),
+        ("sum_rho_g", C.c_double * 3),
+        ("sum_l_g", C.c_double * 3),
+    ]
+
+
+GRAD_STATS_DTYPE = [
+    ("samples", "<u8"), ("sum_u", "<f8"), ("sum_u2", "<f8"), ("sum_rho", "<f8"),
+    ("sum_rho2", "<f8"), ("sum_l", "<f8"), ("sum_g", "<f8", (3,)), ("sum_u_g", "<f8", (3,)),
+    ("sum_rho_g", "<f8", (3,)), ("sum_l_g", "<f8", (3,)),
+]

@@ -116,6 +116,25 @@ class ChainBatch:
                      off.ctypes.data_as(P(C.c_uint64)), self.n_chains)
         return px.value, pr.value, off
 
+    def energy_grad(self):
+        """(U, dU/deps, dU/dsigma, dU/dL) of every chain's current configuration."""
+        from . import grad  # noqa: F401  (registers the entry points)
+        out = np.empty((self.n_chains, 4), dtype=np.float64)
+        _native.call("jmm_batch_energy_grad", self._h, out.ctypes.data_as(P(C.c_double)),
+                     self.n_chains)
+        return out
+
+    def run_sampled(self, n_sweeps, sample_every=10):
+        """n_sweeps sweeps, sampling U and its gradient every sample_every sweeps."""
+        from . import grad  # noqa: F401
+        _native.call("jmm_batch_run_sampled", self._h, n_sweeps, sample_every)
+
+    def grad_stats(self):
+        from . import grad  # noqa: F401
+        buf = (abi.GradStats * self.n_chains)()
+        _native.call("jmm_batch_grad_stats", self._h, buf, self.n_chains)
+        return np.frombuffer(buf, dtype=np.dtype(abi.GRAD_STATS_DTYPE)).copy()
+
     def autotune(self, trial_sweeps=4):
         """(lanes_per_chain, steps_per_round, chains_per_block) chosen."""
         g, s, c = C.c_uint32(), C.c_uint32(), C.c_uint32()

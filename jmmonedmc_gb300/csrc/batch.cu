@@ -16,6 +16,7 @@
 
 #include "batch_core.cuh"
 #include "common.cuh"
+#include "grad_core.cuh"
 
 using namespace jmm;
 using namespace jmm::batch;
@@ -86,11 +87,19 @@ struct jmm_batch {
   std::vector<PotClass> classes;
   cudaStream_t side[3] = {nullptr, nullptr, nullptr};  // concurrent classes in a graph
   cudaEvent_t fork = nullptr, join[3] = {nullptr, nullptr, nullptr};
+  // energy gradients and their sampled statistics
+  jmm_chain_desc *d_desc = nullptr;     // user order
+  uint64_t *d_xoff = nullptr;           // user order
+  double *d_gout = nullptr;             // 4 per chain
+  jmm_grad_stats *d_gstats = nullptr;   // user order
+  std::map<std::pair<uint64_t, uint32_t>, cudaGraphExec_t> sampled;  // (sweeps, every)
 };
 
 static void drop_graphs(jmm_batch *b) {
   for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
   b->graphs.clear();
+  for (auto &kv : b->sampled) cudaGraphExecDestroy(kv.second);
+  b->sampled.clear();
 }
 
 static void batch_free(jmm_batch *b) {
@@ -100,6 +109,10 @@ static void batch_free(jmm_batch *b) {
   cudaFree(b->d_res);
   cudaFree(b->d_x);
   cudaFree(b->d_e);
+  cudaFree(b->d_desc);
+  cudaFree(b->d_xoff);
+  cudaFree(b->d_gout);
+  cudaFree(b->d_gstats);
   for (int k = 0; k < 3; ++k) {
     if (b->side[k]) cudaStreamDestroy(b->side[k]);
     if (b->join[k]) cudaEventDestroy(b->join[k]);
@@ -320,6 +333,15 @@ extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_des
   if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_res, n_chains * sizeof(jmm_chain_result));
   if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_x, b->total_floats * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_e, n_chains * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_desc, n_chains * sizeof(jmm_chain_desc));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_xoff, n_chains * sizeof(uint64_t));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_gout, 4 * n_chains * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_gstats, n_chains * sizeof(jmm_grad_stats));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_desc, chains, n_chains * sizeof(jmm_chain_desc), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_xoff, b->x_off.data(), n_chains * sizeof(uint64_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(b->d_gstats, 0, n_chains * sizeof(jmm_grad_stats));
   if (e != cudaSuccess) {
     rc = cuda_status(e, "jmm_batch_create allocation", __FILE__, __LINE__);
     batch_free(b);
@@ -442,6 +464,7 @@ extern "C" int jmm_batch_reset_stats(jmm_batch *b) {
   JMM_CHECK_ARG(b, "null handle");
   reset_stats_kernel<<<(b->n_chains + 255) / 256, 256, 0, b->stream>>>(b->d_res, b->n_chains);
   JMM_CUDA(cudaGetLastError());
+  JMM_CUDA(cudaMemsetAsync(b->d_gstats, 0, b->n_chains * sizeof(jmm_grad_stats), b->stream));
   JMM_CUDA(cudaStreamSynchronize(b->stream));
   return JMM_OK;
 }
@@ -658,5 +681,111 @@ extern "C" int jmm_rng_words(uint64_t seed, uint64_t block0, uint32_t chain, uin
   if (e == cudaSuccess) e = cudaMemcpy(out, d, count * 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost);
   cudaFree(d);
   if (e != cudaSuccess) return cuda_status(e, "jmm_rng_words", __FILE__, __LINE__);
+  return JMM_OK;
+}
+
+// ---- energy gradients of the batch's configurations -------------------------
+
+// One warp per chain (user order): U and its derivatives into out (mode 0),
+// or added with the fluctuation moments to the chain's jmm_grad_stats.
+template <bool kAccumulate>
+__global__ void batch_grad_kernel(const jmm_chain_desc *__restrict__ desc,
+                                  const uint64_t *__restrict__ xoff, const float *__restrict__ x,
+                                  const jmm_chain_result *__restrict__ res, uint32_t n_chains,
+                                  int32_t boundary, double *__restrict__ out,
+                                  jmm_grad_stats *__restrict__ stats) {
+  const uint32_t c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (c >= n_chains) return;
+  const jmm_chain_desc d = desc[c];
+  const double l = res[c].l;
+  const grad::PotParams p = grad::make_pot(d.potential, d.eps, d.sigma, d.cutoff);
+  __shared__ double tmp[8][4];
+  double *o = kAccumulate ? tmp[(threadIdx.x / 32) % 8] : out + 4 * c;
+  grad::chain_grad(x + xoff[c], (int)d.n, p, l, boundary == JMM_BOUNDARY_PERIODIC, o, nullptr);
+  if (kAccumulate && (threadIdx.x & 31) == 0) {
+    jmm_grad_stats st = stats[c];
+    const double u = o[0];
+    const double rho = __ddiv_rn((double)d.n, l);
+    const double g[3] = {o[1], o[2], o[3]};
+    st.samples += 1;
+    st.sum_u = __dadd_rn(st.sum_u, u);
+    st.sum_u2 = __dadd_rn(st.sum_u2, __dmul_rn(u, u));
+    st.sum_rho = __dadd_rn(st.sum_rho, rho);
+    st.sum_rho2 = __dadd_rn(st.sum_rho2, __dmul_rn(rho, rho));
+    st.sum_l = __dadd_rn(st.sum_l, l);
+    for (int k = 0; k < 3; ++k) {
+      st.sum_g[k] = __dadd_rn(st.sum_g[k], g[k]);
+      st.sum_u_g[k] = __dadd_rn(st.sum_u_g[k], __dmul_rn(u, g[k]));
+      st.sum_rho_g[k] = __dadd_rn(st.sum_rho_g[k], __dmul_rn(rho, g[k]));
+      st.sum_l_g[k] = __dadd_rn(st.sum_l_g[k], __dmul_rn(l, g[k]));
+    }
+    stats[c] = st;
+  }
+}
+
+static int launch_grad(jmm_batch *b, bool accumulate, cudaStream_t s) {
+  const uint32_t per_block = 8;
+  const uint32_t blocks = (b->n_chains + per_block - 1) / per_block;
+  if (accumulate)
+    batch_grad_kernel<true><<<blocks, 32 * per_block, 0, s>>>(
+        b->d_desc, b->d_xoff, b->d_x, b->d_res, b->n_chains, b->cfg.boundary, nullptr, b->d_gstats);
+  else
+    batch_grad_kernel<false><<<blocks, 32 * per_block, 0, s>>>(
+        b->d_desc, b->d_xoff, b->d_x, b->d_res, b->n_chains, b->cfg.boundary, b->d_gout, nullptr);
+  JMM_CUDA(cudaGetLastError());
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_energy_grad(jmm_batch *b, double *out, uint32_t n_chains) {
+  clear_error();
+  JMM_CHECK_ARG(b && out, "null argument");
+  JMM_CHECK_ARG(n_chains == b->n_chains, "n_chains does not match the batch");
+  int rc = launch_grad(b, false, b->stream);
+  if (rc) return rc;
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  JMM_CUDA(cudaMemcpy(out, b->d_gout, 4 * n_chains * sizeof(double), cudaMemcpyDeviceToHost));
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_run_sampled(jmm_batch *b, uint64_t n_sweeps, uint32_t sample_every) {
+  clear_error();
+  JMM_CHECK_ARG(b, "null handle");
+  JMM_CHECK_ARG(sample_every > 0, "sample_every must be positive");
+  if (n_sweeps == 0) return JMM_OK;
+  const auto key = std::make_pair(n_sweeps, sample_every);
+  auto it = b->sampled.find(key);
+  cudaGraphExec_t exec;
+  if (it != b->sampled.end()) {
+    exec = it->second;
+  } else {
+    cudaGraph_t graph;
+    JMM_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = JMM_OK;
+    uint64_t done = 0;
+    while (rc == JMM_OK && done + sample_every <= n_sweeps) {
+      rc = launch(b, sample_every, b->stream);
+      if (rc == JMM_OK) rc = launch_grad(b, true, b->stream);
+      done += sample_every;
+    }
+    if (rc == JMM_OK && done < n_sweeps) rc = launch(b, n_sweeps - done, b->stream);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+    b->sampled[key] = exec;
+  }
+  JMM_CUDA(cudaGraphLaunch(exec, b->stream));
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  return check_errors(b);
+}
+
+extern "C" int jmm_batch_grad_stats(jmm_batch *b, jmm_grad_stats *out, uint32_t n_chains) {
+  clear_error();
+  JMM_CHECK_ARG(b && out, "null argument");
+  JMM_CHECK_ARG(n_chains == b->n_chains, "n_chains does not match the batch");
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  JMM_CUDA(cudaMemcpy(out, b->d_gstats, n_chains * sizeof(jmm_grad_stats), cudaMemcpyDeviceToHost));
   return JMM_OK;
 }

@@ -625,3 +625,61 @@ double jmmo_energy64(const jmm_chain_desc *c, const double *x, double l, int per
 
 float jmmo_portable_logf(float x) { return jmmo_logf(x); }
 float jmmo_portable_expf(float x) { return jmmo_expf(x); }
+
+/* U, dU/deps, dU/dsigma, dU/dL (positions scaled with the box) of one
+ * configuration in FP64: the reference for the gradient kernel. */
+void jmmo_energy_grad64(const jmm_chain_desc *c, const double *x, double l, int periodic,
+                        double out[4]) {
+  const int n = (int)c->n;
+  const double eps = c->eps, sig = c->sigma, rc2 = c->cutoff * c->cutoff;
+  double u = 0, ge = 0, gs = 0, rd = 0;
+  for (int i = 0; i < n; ++i) {
+    for (int k = 1;; ++k) {
+      int j = i + k;
+      double shift = 0;
+      if (!periodic) {
+        if (j >= n) break;
+      } else {
+        if (2 * k > n - 1) break;
+        if (j >= n) {
+          j -= n;
+          shift = l;
+        }
+      }
+      const double d = x[j] + shift - x[i];
+      const double r2 = d * d;
+      if (r2 > rc2) break;
+      double e, g_eps, r_dphi, g_sig;
+      if (c->potential == JMM_POT_GAUSS) {
+        const double a = r2 / (sig * sig);
+        const double ex = exp(-a);
+        g_eps = ex;
+        e = eps * ex;
+        r_dphi = -2.0 * e * a;
+        g_sig = 2.0 * e * a / sig;
+      } else {
+        const double inv2 = sig * sig / r2;
+        const double inv6 = inv2 * inv2 * inv2;
+        const double inv12 = inv6 * inv6;
+        if (c->potential == JMM_POT_SOFTSPHERE) {
+          g_eps = inv12;
+          e = eps * inv12;
+          r_dphi = -12.0 * e;
+        } else {
+          g_eps = 4.0 * (inv12 - inv6);
+          e = eps * g_eps;
+          r_dphi = -24.0 * eps * (2.0 * inv12 - inv6);
+        }
+        g_sig = -r_dphi / sig;
+      }
+      u += e;
+      ge += g_eps;
+      gs += g_sig;
+      rd += r_dphi;
+    }
+  }
+  out[0] = u;
+  out[1] = ge;
+  out[2] = gs;
+  out[3] = rd / l;
+}

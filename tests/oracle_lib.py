@@ -179,6 +179,7 @@ extra_sigs({
     "jmmo_batch_set_positions": ([vp, u32, P(dbl), u32, dbl], C.c_int),
     "jmmo_batch_energies": ([vp, P(dbl), u32], C.c_int),
     "jmmo_energy64": ([P(abi.ChainDesc), P(dbl), dbl, C.c_int], dbl),
+    "jmmo_energy_grad64": ([P(abi.ChainDesc), P(dbl), dbl, C.c_int, P(dbl)], None),
     "jmmo_portable_logf": ([C.c_float], C.c_float),
     "jmmo_portable_expf": ([C.c_float], C.c_float),
 })
@@ -245,3 +246,13 @@ def energy64(chain_desc, x, l, periodic=False):
     x = np.ascontiguousarray(x, dtype=np.float64)
     return lib.jmmo_energy64(C.byref(chain_desc), x.ctypes.data_as(P(dbl)), float(l),
                              1 if periodic else 0)
+
+
+def energy_grad64(chain_desc, x, l, periodic=False):
+    """FP64 (U, dU/deps, dU/dsigma, dU/dL) of one configuration."""
+    lib = load()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = (dbl * 4)()
+    lib.jmmo_energy_grad64(C.byref(chain_desc), x.ctypes.data_as(P(dbl)), float(l),
+                           1 if periodic else 0, out)
+    return np.array(out)
