@@ -55,7 +55,35 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=1.5,
                     help="wall seconds per host core for the CPU baseline sample")
     ap.add_argument("--no-autotune", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--workload", choices=("npt", "uneven"), default="npt",
+                    help="npt: the batched NPT headline workload; uneven: 1024 chains of "
+                         "N ~ U{32..2048}, rho ~ U(0.3, 0.9), LJ / soft sphere / Gaussian core, "
+                         "T ~ U(0.5, 2), NVT")
+    args = ap.parse_args()
+    if args.workload == "uneven":
+        if args.chains == 4096:
+            args.chains = 1024
+        if args.sweeps_per_step == 1000:
+            args.sweeps_per_step = 500
+    return args
+
+
+def uneven_workload(args, seed):
+    """1024 chains of uneven N, density, potential and temperature (NVT)."""
+    from jmmonedmc_gb300 import abi
+    from jmmonedmc_gb300.philox_host import uniforms
+    n_ch = args.chains
+    un, ur, ut = (uniforms(seed, n_ch, stream=s) for s in (0xC1, 0xC2, 0xC3))
+    pots = [(abi.JMM_POT_LJCUT, 3.0), (abi.JMM_POT_SOFTSPHERE, 2.5), (abi.JMM_POT_GAUSS, 4.0)]
+    chains = []
+    for c in range(n_ch):
+        n = 32 + int(un[c] * (2048 - 32 + 1))
+        pot, rc = pots[c % 3]
+        chains.append(abi.make_chain(n, potential=pot, ensemble=abi.JMM_NLT, eps=1.0, sigma=1.0,
+                                     cutoff=rc, t=0.5 + 1.5 * ut[c], rho=0.3 + 0.6 * ur[c],
+                                     max_step=0.3))
+    cfg = abi.make_batch_config(seed=seed, precision=abi.JMM_PREC_FAST, resum_sweeps=100)
+    return cfg, chains
 
 
 def workload(args, rank=0):
@@ -64,6 +92,8 @@ def workload(args, rank=0):
     from jmmonedmc_gb300.philox_host import uniforms
     n_ch = args.chains
     seed = args.seed + 1000003 * rank
+    if args.workload == "uneven":
+        return uneven_workload(args, seed)
     temps = [0.5 * 4.0 ** (c / max(1, n_ch - 1)) for c in range(n_ch)]
     press = [0.5 + 1.5 * u for u in uniforms(seed, n_ch, stream=0xB0)]
     chains = [abi.make_chain(args.n, potential=abi.JMM_POT_LJCUT, ensemble=abi.JMM_NPT,
@@ -76,6 +106,17 @@ def workload(args, rank=0):
 
 
 def config_dict(args, extra=None):
+    if args.workload == "uneven":
+        d = {"workload": (f"uneven batch: {args.chains} chains, N ~ U{{32..2048}}, rho ~ "
+                          "U(0.3,0.9), potential cycling LJ rc=3 / soft sphere rc=2.5 / Gaussian "
+                          "core rc=4 (eps=sigma=1), T ~ U(0.5,2.0), NVT, hard walls, max "
+                          "displacement 0.3"),
+             "chains": args.chains, "sweeps_per_step": args.sweeps_per_step,
+             "l2": "flushed between timed steps (256 MiB device write)",
+             "precision": "FP32 pair energies, FP64 running totals and accumulators"}
+        if extra:
+            d.update(extra)
+        return d
     d = {
         "workload": (f"batched NPT: {args.chains} chains x N={args.n}, LJ 12-6 eps=sigma=1 rc=3, "
                      "hard walls, T log-spaced 0.5-2.0, P U(0.5,2.0), ln L moves delta=0.01 "
@@ -152,13 +193,13 @@ class ClockSampler:
 def _cpu_worker(job):
     """One host core: the reference's chain (plain FP64, pair-state arrays)
     for the workload's chain `k`, run for `seconds` wall seconds."""
-    k, n, t, p, seed, seconds, repo = job
+    k, n, t, p, seed, seconds, repo, npt, l = job
     sys.path.insert(0, repo)
     from jmmonedmc_gb300 import abi
     from tests import oracle_lib
-    params = abi.make_params(n=n, ensemble=abi.JMM_NPT, potential=abi.JMM_POT_LJCUT, p=p, t=t,
-                             cutoff=3.0, max_step=0.3, max_dl=0.01 * n / 0.6, seed=seed + k,
-                             eci=0)
+    params = abi.make_params(n=n, ensemble=abi.JMM_NPT if npt else abi.JMM_NLT,
+                             potential=abi.JMM_POT_LJCUT, p=p, t=t, l=l, cutoff=3.0,
+                             max_step=0.3, max_dl=0.01 * n / 0.6, seed=seed + k, eci=0)
     chain = oracle_lib.OraclePlain(params)
     chain.fad()
     chunk = n + 1
@@ -179,8 +220,9 @@ def cpu_reference_sample(chains, seconds, seed):
     oracle_lib.load()  # build the oracle library before the workers start
     cores = os.cpu_count() or 1
     picks = [int(i * len(chains) / cores) for i in range(cores)]
-    jobs = [(k, int(chains[k].n), float(chains[k].t), float(chains[k].p), seed, seconds, REPO)
-            for k in picks]
+    from jmmonedmc_gb300 import abi
+    jobs = [(k, int(chains[k].n), float(chains[k].t), float(chains[k].p), seed, seconds, REPO,
+             chains[k].ensemble == abi.JMM_NPT, float(chains[k].l0)) for k in picks]
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
@@ -193,10 +235,11 @@ def cpu_reference_sample(chains, seconds, seed):
         "unit": UNIT,
         "cores": cores,
         "kind": "port",
-        "sample": (f"{cores} chains of the workload (N={chains[0].n}, NPT, LJcut 3.0), one per "
-                   f"host core, each run for {seconds:.1f} s with the reference's algorithm "
-                   "(oracle/plain_oracle.c: FP64, per-pair state, O(N) displacement, "
-                   "O(N^2) volume move, linear dL); aggregate attempted moves / wall"),
+        "sample": (f"{cores} chains of the workload (sizes {sorted(int(chains[k].n) for k in picks)}"
+                   f", LJcut 3.0 for every chain: the reference has no soft-sphere or Gaussian "
+                   f"potential), one per host core, each run for {seconds:.1f} s with the "
+                   "reference's algorithm (oracle/plain_oracle.c: FP64, per-pair state, O(N) "
+                   "displacement, O(N^2) volume move, linear dL); aggregate attempted moves / wall"),
         "steps": steps,
         "wall_s": wall,
     }
@@ -297,12 +340,12 @@ def run_ours(args, rank, world, local_rank):
         moves_all, pairs_all = moves, pairs
 
     # e2e: host buffers through the C ABI (jmm_batch_run_host), H2D and D2H inside
-    n_tot = args.chains * args.n
+    n_tot = sum(int(c.n) for c in chains)
     x_host = torch.empty(n_tot, dtype=torch.float32, pin_memory=True).numpy()
     x_off = 0
-    for k in range(args.chains):
-        x_host[x_off:x_off + args.n] = b.positions(k)
-        x_off += args.n
+    for k, c in enumerate(chains):
+        x_host[x_off:x_off + c.n] = b.positions(k)
+        x_off += c.n
     lbox = after["l"].copy()
     for k, c in enumerate(chains):
         c.l0 = float(lbox[k])
@@ -327,7 +370,7 @@ def run_ours(args, rank, world, local_rank):
     launch_ms = total_ms / args.steps
     flop_per_launch = pairs / args.steps * FLOP_PER_PAIR
     achieved = flop_per_launch / (launch_ms * 1e-3) / 1e12
-    traffic = profile_traffic(args, pairs / args.steps, S)
+    traffic = profile_traffic(args, pairs / args.steps, S) if args.workload == "npt" else None
     line = {
         "metric": METRIC,
         "value": moves_all / (total_ms * 1e-3),

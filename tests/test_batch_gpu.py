@@ -175,3 +175,26 @@ def test_batch_rejects_bad_input(gpu):
     b = ChainBatch(abi.make_batch_config(), [abi.make_chain(16)])
     with pytest.raises(JmmError):
         b.set_positions(0, np.linspace(1, -1, 16), 30.0)  # not increasing
+
+
+def test_uneven_batch_at_full_size(gpu):
+    """The uneven workload (1024 chains, N 32..2048, three potentials,
+    rho 0.3-0.9, T 0.5-2, NVT) runs error-free in one graph of parallel
+    per-potential kernels; the energies of a sample of chains agree with the
+    FP64 oracle of the GPU's own configurations."""
+    import argparse
+    import bench
+    args = argparse.Namespace(chains=1024, seed=1, workload="uneven", n=256)
+    cfg, chains = bench.uneven_workload(args, 1)
+    b = ChainBatch(cfg, chains)
+    b.autotune(trial_sweeps=1)
+    b.run(20)
+    res = b.results()
+    assert np.all(res["error"] == 0)
+    assert np.all(res["steps"] == 20 * np.array([c.n for c in chains]))
+    fresh = b.energies()
+    for k in range(0, 1024, 97):
+        x = b.positions(k).astype(np.float64)
+        e64 = oracle_lib.energy64(chains[k], x, res["l"][k])
+        assert abs(fresh[k] - e64) <= 1e-6 * max(1.0, abs(e64)), (k, fresh[k], e64)
+        assert np.all(np.diff(x) > 0)
