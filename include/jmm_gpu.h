@@ -308,6 +308,52 @@ int jmm_batch_run_host(const jmm_batch_config *cfg, const jmm_chain_desc *chains
                        uint32_t n_chains, const float *x_in, uint64_t n_sweeps,
                        jmm_chain_result *results, float *x_out);
 
+/* ---- large chains (N up to 2^24): the alternating-domain sweep ---------- */
+/* No counterpart in the reference, which holds O(N^2) pair arrays per chain
+ * (src/jmmMCState.cpp:308-328,439-455) and cannot run N = 2^20.  Constant-L
+ * chains with hard walls, FP64 positions in HBM, FP32 step arithmetic. */
+
+#define JMM_LARGE_DOMAINS 0     /* alternating-domain sweep: domains of B
+                                   particles from a random offset, two colours
+                                   in random order, one warp per domain       */
+#define JMM_LARGE_SEQUENTIAL 1  /* plain sweep: one warp per chain, N steps in
+                                   order on the HBM positions                 */
+
+typedef struct jmm_large_result {
+  double e;              /* running total energy                               */
+  double l;              /* box length                                         */
+  uint64_t sweeps;       /* sweeps since creation                              */
+  uint64_t samples;      /* sweeps accumulated since the last reset            */
+  double sum_e, sum_e2;  /* one sample of E per sweep                          */
+  uint64_t moves, accepted, pair_evals, window_overflows;
+  double max_drift;      /* largest |running E - fresh FP64 sum| at a re-sum   */
+  uint32_t error;        /* JMM_ERR_* seen by a kernel (JMM_ERR_INVALID: a
+                            domain's 16-particle halo did not reach beyond the
+                            cut-off; the domain was skipped that sweep)        */
+  uint32_t reserved;
+} jmm_large_result;
+
+typedef struct jmm_large jmm_large;
+
+/* Chains as jmm_chain_desc (ensemble JMM_NLT, potential LJCUT, SOFTSPHERE or
+ * GAUSS, domain_size <= N <= 2^24); cfg gives seed, init/jitter and
+ * resum_sweeps (boundary JMM_BOUNDARY_WALLS, precision JMM_PREC_FAST);
+ * domain_size B in [32, 8192]. */
+int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                     uint32_t n_chains, uint32_t domain_size, jmm_large **out);
+/* n_sweeps sweeps (N steps each) in mode JMM_LARGE_*, then wait. */
+int jmm_large_run(jmm_large *h, uint64_t n_sweeps, int32_t mode);
+/* Same, enqueued on stream (cudaStream_t as void*, NULL = the handle's), no wait. */
+int jmm_large_run_async(jmm_large *h, uint64_t n_sweeps, int32_t mode, void *stream);
+int jmm_large_results(jmm_large *h, jmm_large_result *out, uint32_t n_chains);
+int jmm_large_reset_stats(jmm_large *h);
+/* Fresh energies of the current positions (FP32 pair terms, FP64 sums). */
+int jmm_large_energies(jmm_large *h, double *e, uint32_t n_chains);
+int jmm_large_get_positions(jmm_large *h, uint32_t chain, double *x, uint64_t n);
+/* Positions must increase and lie within +-L/2; energies are re-summed. */
+int jmm_large_set_positions(jmm_large *h, uint32_t chain, const double *x, uint64_t n);
+int jmm_large_destroy(jmm_large *h);
+
 /* The Philox words of steps [block0, block0 + count) of one chain, computed
  * on the device (4 words per step), for RNG verification tooling. */
 int jmm_rng_words(uint64_t seed, uint64_t block0, uint32_t chain, uint64_t count,

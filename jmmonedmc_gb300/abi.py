@@ -279,3 +279,32 @@ GRAD_STATS_DTYPE = [
     ("sum_rho2", "<f8"), ("sum_l", "<f8"), ("sum_g", "<f8", (3,)), ("sum_u_g", "<f8", (3,)),
     ("sum_rho_g", "<f8", (3,)), ("sum_l_g", "<f8", (3,)),
 ]
+
+
+JMM_LARGE_DOMAINS = 0
+JMM_LARGE_SEQUENTIAL = 1
+
+
+class LargeResult(C.Structure):
+    _fields_ = [
+        ("e", C.c_double),
+        ("l", C.c_double),
+        ("sweeps", C.c_uint64),
+        ("samples", C.c_uint64),
+        ("sum_e", C.c_double),
+        ("sum_e2", C.c_double),
+        ("moves", C.c_uint64),
+        ("accepted", C.c_uint64),
+        ("pair_evals", C.c_uint64),
+        ("window_overflows", C.c_uint64),
+        ("max_drift", C.c_double),
+        ("error", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
+LARGE_RESULT_DTYPE = [
+    ("e", "<f8"), ("l", "<f8"), ("sweeps", "<u8"), ("samples", "<u8"), ("sum_e", "<f8"),
+    ("sum_e2", "<f8"), ("moves", "<u8"), ("accepted", "<u8"), ("pair_evals", "<u8"),
+    ("window_overflows", "<u8"), ("max_drift", "<f8"), ("error", "<u4"), ("reserved", "<u4"),
+]

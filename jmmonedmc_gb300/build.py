@@ -30,6 +30,7 @@ UNITS = {
     "grad.cu": [],
     "noalloc.cu": ["-fmad=false"],
     "peak.cu": [],
+    "large.cu": [],
 }
 
 

@@ -238,13 +238,17 @@ __device__ __forceinline__ float threshold_of(uint32_t w) {
 }
 
 // Neighbour index of window lane (side, k), clamped for loads, and its
-// periodic shift.
-template <bool PER>
+// periodic shift.  With HALO the chain is one domain of a longer chain and
+// the kGhost slots on each side hold the neighbouring domains' particles.
+template <bool PER, bool HALO = false>
 __device__ __forceinline__ int window_index(int nm, int side, int k, int n, float lf, bool &inr,
                                             float &shift) {
   int j = nm + side * k;
   shift = 0.0f;
-  if (!PER) {
+  if (HALO) {
+    inr = j >= -kGhost && j < n + kGhost;
+    j = j < -kGhost ? -kGhost : (j >= n + kGhost ? n + kGhost - 1 : j);
+  } else if (!PER) {
     inr = j >= 0 && j < n;
     j = j < 0 ? 0 : (j >= n ? n - 1 : j);
   } else {
@@ -288,7 +292,7 @@ __host__ __device__ constexpr unsigned leader_bits(int g, int s) {
 }
 
 // One chain for one launch: n_sweeps sweeps in speculative rounds of S steps.
-template <int G, int S, int POT, bool PER, bool kExact>
+template <int G, int S, int POT, bool PER, bool kExact, bool HALO = false>
 __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result *__restrict__ res,
                                           float *__restrict__ xg, float *xs, uint32_t *ring,
                                           const KernelCfg &cfg, int cl, unsigned gmask) {
@@ -466,7 +470,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
             const int k = chunk * W + kb + q * H2;
             bool inr2;
             float shift2;
-            const int j2 = window_index<PER>(nmc, side, k, n, lf, inr2, shift2);
+            const int j2 = window_index<PER, HALO>(nmc, side, k, n, lf, inr2, shift2);
             const float xj2 = __fadd_rn(xs[j2], shift2);
             const float dn_2 = side > 0 ? __fsub_rn(xj2, xn) : __fsub_rn(xn, xj2);
             const float do_2 = side > 0 ? __fsub_rn(xj2, xo) : __fsub_rn(xo, xj2);
@@ -566,7 +570,8 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
     rp->error = err;
   }
   __syncwarp(gmask);
-  for (int i = cl; i < n; i += L) xg[P.x_off + i] = xs[i];
+  if (!HALO)  // a domain's caller writes back its own (moved) particles
+    for (int i = cl; i < n; i += L) xg[P.x_off + i] = xs[i];
 }
 
 // One kernel per (shape, potential, boundary, precision): the chains of one

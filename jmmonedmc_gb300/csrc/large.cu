@@ -1,0 +1,700 @@
+// large.cu -- chains too long for one SM's shared memory (N up to 2^24),
+// behind the jmm_large_* entry points of include/jmm_gpu.h.  Constant L,
+// hard walls at +-L/2, ordered particles (LJ, soft sphere or Gaussian with
+// the cut-off window of the batched kernel).
+//
+// Positions live in HBM as FP64: on a chain 1.5e6 long an absolute FP32
+// coordinate has an ulp of 0.0625.  The step arithmetic is FP32 on
+// separations, as in the batched kernel.  Two ways to run the same chain:
+//
+//  * Sequential plain sweep (sequential_kernel).  One warp per chain makes
+//    the chain's N single-particle Metropolis steps in order on the HBM
+//    positions: separations are taken in FP64 and rounded to FP32, 16
+//    neighbours per side per pass.  This is the conventional sweep, latency
+//    bound (one dependent HBM round trip per step).
+//  * Alternating-domain sweep (domain_kernel).  Per sweep the index range
+//    is cut into domains of B particles from a random offset o in [0, B):
+//    domain d = [o + (d-1)B, o + dB) clipped to [0, N).  The domains of one
+//    colour (d even, or d odd; which colour goes first is random per sweep)
+//    run at the same time, one warp each, then the other colour.  A domain
+//    copies its particles and kGhost = 16 of each neighbour's (frozen for
+//    the phase; far sentinels beyond the chain's ends) into shared memory,
+//    as FP32 coordinates about a local origin, and makes B single-particle
+//    Metropolis steps on its own particles with the batched kernel's step
+//    loop; it writes back, in FP64, only the particles it moved.  Two active
+//    domains are separated by a frozen interior domain of B >= 2 kGhost
+//    particles, and the kernel checks that the halo reaches beyond the
+//    cut-off (else it flags JMM_ERR_INVALID and skips the domain), so they
+//    share no pair: a phase is a product of independent Metropolis chains
+//    on the conditional distribution of each domain given the rest, which
+//    leaves the Boltzmann distribution invariant, and the random offset and
+//    colour order make every particle's position in the layout random.
+//
+// Energies: each step-loop record accumulates its own energy changes (FP32
+// within a launch, FP64 across launches); a chain's running energy is its
+// last FP64 re-summation plus its records' changes, sampled once per sweep
+// into FP64 sums of E and E^2.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "batch_core.cuh"
+#include "common.cuh"
+
+using namespace jmm;
+using namespace jmm::batch;
+
+namespace {
+
+constexpr int kG = 4, kS = 8;  // the batched kernel's default launch shape
+constexpr int kWarpsPerBlock = 4;
+constexpr int kSeqSide = 16;   // neighbours per side per pass, sequential sweep
+constexpr uint32_t kStatWarps = 8;
+
+struct LargeChain {
+  uint64_t x_base;  // double offset of the chain's particle 0 in the padded buffer
+  uint32_t n;
+  uint32_t pot;
+  uint32_t rec0;    // first domain record of the chain
+  uint32_t n_dom;   // domain records: N/B rounded up, plus one for the offset
+  float eps4, sigma2, inv_sigma2, rc2, beta, two_max_step, rc;
+  uint32_t pad;
+  double l;
+};
+
+struct LargeState {
+  double e_base;    // FP64 energy at the last re-summation
+  double sum_e, sum_e2;
+  double max_drift; // largest |running E - fresh FP64 sum| at a re-summation
+  uint64_t sweeps;  // sweeps done: the index of the sweep's layout draw
+  uint64_t samples;
+};
+
+__device__ __forceinline__ ChainParams domain_params(const LargeChain &c, uint32_t id, uint32_t n) {
+  ChainParams P;
+  P.id = id;
+  P.n = n;
+  P.pot = c.pot;
+  P.ensemble = JMM_NLT;
+  P.steps_per_sweep = n;
+  P.s_off = 0;
+  P.x_off = 0;
+  P.eps4 = c.eps4;
+  P.sigma2 = c.sigma2;
+  P.inv_sigma2 = c.inv_sigma2;
+  P.rc2 = c.rc2;
+  P.beta = c.beta;
+  P.two_max_step = c.two_max_step;
+  P.vol_step = 0.0f;
+  P.rc = c.rc;
+  P.beta_d = 0.0;
+  P.p = 0.0;
+  return P;
+}
+
+__device__ __forceinline__ Hot hot_of(const LargeChain &c) {
+  Hot H;
+  H.eps4 = c.eps4;
+  H.sigma2 = c.sigma2;
+  H.inv_sigma2 = c.inv_sigma2;
+  H.rc2 = c.rc2;
+  H.beta = c.beta;
+  H.two_max_step = c.two_max_step;
+  return H;
+}
+
+// Offset and first colour of sweep `s` of chain `chain`: Philox block
+// 2^62 + s of stream `chain` (step counters stay below 2^62).
+__device__ __forceinline__ void sweep_layout(uint64_t seed, uint32_t chain, uint64_t s,
+                                             uint32_t b, uint32_t *off, uint32_t *first) {
+  const Words4 w = step_words(seed, (1ull << 62) | s, chain);
+  *off = (uint32_t)word_to_index(w.w[0], b);
+  *first = w.w[1] & 1u;
+}
+
+template <int POT>
+__global__ void __maxnreg__(72)
+    domain_kernel(const LargeChain *__restrict__ chains, const LargeState *__restrict__ states,
+                  jmm_chain_result *__restrict__ rec, double *__restrict__ x, uint32_t n_chains,
+                  uint32_t b, uint32_t phase, uint32_t doms_per_chain, KernelCfg cfg) {
+  extern __shared__ float smem[];
+  const uint32_t wib = threadIdx.x / 32;
+  const uint64_t warp = (uint64_t)blockIdx.x * kWarpsPerBlock + wib;
+  const uint32_t c = (uint32_t)(warp / doms_per_chain);
+  if (c >= n_chains) return;
+  const LargeChain ch = chains[c];
+  if (ch.pot != (uint32_t)POT) return;
+  uint32_t off, first;
+  sweep_layout(cfg.seed, c, states[c].sweeps, b, &off, &first);
+  const uint32_t d = 2 * (uint32_t)(warp % doms_per_chain) + ((first + phase) & 1u);
+  if (d >= ch.n_dom) return;
+  const int64_t lo = max((int64_t)0, (int64_t)off + ((int64_t)d - 1) * (int64_t)b);
+  const int64_t hi = min((int64_t)ch.n, (int64_t)off + (int64_t)d * (int64_t)b);
+  if (hi <= lo) return;
+  const int n = (int)(hi - lo);
+  const int cl = threadIdx.x & 31;
+  double *xc = x + ch.x_base + lo;  // xc[-kGhost .. n + kGhost - 1] are valid (padding)
+  jmm_chain_result *rp = rec + ch.rec0 + d;
+
+  // the halo must reach beyond the cut-off: unloaded neighbours are farther
+  // than the last halo particle from every particle of the domain
+  const double reach = 1.0001 * (double)ch.rc;
+  const bool right_ok = hi == ch.n || __dsub_rn(xc[n + kGhost - 1], xc[n]) > reach;
+  const bool left_ok = lo == 0 || __dsub_rn(xc[-1], xc[-kGhost]) > reach;
+  if (!(right_ok && left_ok)) {
+    if (cl == 0) rp->error |= JMM_ERR_INVALID;
+    return;
+  }
+  // local origin O and half-width h: the walls at +-L/2 map to +-h in the
+  // step loop's symmetric wall test; an interior domain has no wall
+  const double half = __dmul_rn(0.5, ch.l);
+  double O, h;
+  if (lo == 0 && hi == ch.n) {
+    O = 0.0;
+    h = half;
+  } else if (lo == 0) {
+    O = __dmul_rn(0.5, __dsub_rn(xc[n], half));
+    h = __dmul_rn(0.5, __dadd_rn(xc[n], half));
+  } else if (hi == ch.n) {
+    O = __dmul_rn(0.5, __dadd_rn(xc[-1], half));
+    h = __dmul_rn(0.5, __dsub_rn(half, xc[-1]));
+  } else {
+    O = __dmul_rn(0.5, __dadd_rn(xc[0], xc[n - 1]));
+    h = 1e30;
+  }
+  uint32_t *ring = reinterpret_cast<uint32_t *>(smem) + wib * (kRingWords + b + 2 * kGhost);
+  float *xs = reinterpret_cast<float *>(ring + kRingWords) + kGhost;
+  for (int i = cl - kGhost; i < n + kGhost; i += 32) xs[i] = (float)__dsub_rn(xc[i], O);
+  if (cl == 0) rp->l = __dmul_rn(2.0, h);
+  __syncwarp();
+  const ChainParams P = domain_params(ch, ch.rec0 + d, (uint32_t)n);
+  run_chain<kG, kS, POT, false, false, true>(P, rec, nullptr, xs, ring, cfg, cl, 0xffffffffu);
+  __syncwarp();
+  for (int i = cl; i < n; i += 32) {
+    const float xl = (float)__dsub_rn(xc[i], O);
+    if (xs[i] != xl) xc[i] = __dadd_rn(O, (double)xs[i]);
+  }
+}
+
+template <int POT>
+__global__ void __launch_bounds__(32)
+    sequential_kernel(const LargeChain *__restrict__ chains, jmm_chain_result *__restrict__ rec,
+                      double *__restrict__ x, uint32_t n_chains, uint32_t id_base, KernelCfg cfg) {
+  const uint32_t c = blockIdx.x;
+  if (c >= n_chains) return;
+  const LargeChain ch = chains[c];
+  if (ch.pot != (uint32_t)POT) return;
+  const int lane = threadIdx.x & 31;
+  const int side = lane < kSeqSide ? -1 : 1;
+  const int k0 = (lane % kSeqSide) + 1;
+  const int n = (int)ch.n;
+  const uint32_t id = id_base + c;
+  jmm_chain_result *rp = rec + id;
+  double *xc = x + ch.x_base;  // xc[-kGhost .. n + kGhost - 1] are valid (padding)
+  const Hot H = hot_of(ch);
+  const double half = __dmul_rn(0.5, ch.l);
+  const uint64_t step0 = rp->steps;
+  double e_acc = 0.0;
+  uint32_t n_acc = 0, chunks = 0;
+  uint32_t err = rp->error;
+  __syncwarp();
+  for (int s = 0; s < n; ++s) {
+    const Words4 w = step_words(cfg.seed, step0 + (uint64_t)s + 1, id);
+    const int nm = (int)word_to_index(w.w[0], (uint64_t)n);
+    const float md = __fmul_rn(__fsub_rn(word_to_unit_f(w.w[1]), 0.5f), H.two_max_step);
+    const float thr = threshold_of(w.w[2]);
+    const double xo = xc[nm];
+    const double xn = __dadd_rn(xo, (double)md);
+    const double xj = xc[nm + side * k0];  // a padding sentinel beyond either end
+    const float dn = (float)(side > 0 ? __dsub_rn(xj, xn) : __dsub_rn(xn, xj));
+    const float dd = (float)(side > 0 ? __dsub_rn(xj, xo) : __dsub_rn(xo, xj));
+    const float dn2 = __fmul_rn(dn, dn), do2 = __fmul_rn(dd, dd);
+    const float t = __fsub_rn(pair_energy_h<POT, false>(dn2, H), pair_energy_h<POT, false>(do2, H));
+    bool sat = k0 == kSeqSide && (dn2 <= H.rc2 || do2 <= H.rc2);
+    float de = group_sum<32>(t, 0xffffffffu);
+    for (int chunk = 1; __any_sync(0xffffffffu, sat); ++chunk) {
+      const int k = chunk * kSeqSide + k0;
+      const int j = nm + side * k;
+      float t2 = 0.0f;
+      sat = false;
+      if (j >= 0 && j < n) {
+        const double xj2 = xc[j];
+        const float dn_2 = (float)(side > 0 ? __dsub_rn(xj2, xn) : __dsub_rn(xn, xj2));
+        const float do_2 = (float)(side > 0 ? __dsub_rn(xj2, xo) : __dsub_rn(xo, xj2));
+        const float dn22 = __fmul_rn(dn_2, dn_2), do22 = __fmul_rn(do_2, do_2);
+        t2 = __fsub_rn(pair_energy_h<POT, false>(dn22, H), pair_energy_h<POT, false>(do22, H));
+        sat = k0 == kSeqSide && (dn22 <= H.rc2 || do22 <= H.rc2);
+      }
+      de = __fadd_rn(de, group_sum<32>(t2, 0xffffffffu));
+      chunks += 1;
+    }
+    const bool ok = (xn > xc[nm - 1]) && (xn < xc[nm + 1]) && !(fabs(xn) > half);
+    const bool acc = ok && ((de <= 0.0f) || (__fmul_rn(de, H.beta) < thr));
+    if (acc) {
+      e_acc = __dadd_rn(e_acc, (double)de);
+      n_acc += 1;
+      __syncwarp();  // every lane has read x[nm] before it changes
+      if (lane == 0) xc[nm] = xn;
+    }
+    __syncwarp();
+  }
+  if (!isfinite(e_acc)) err = JMM_ERR_NUMERIC;
+  if (lane == 0) {
+    rp->e = __dadd_rn(rp->e, e_acc);
+    rp->steps = step0 + (uint64_t)n;
+    rp->disp_acc += n_acc;
+    rp->disp_att += (uint64_t)n;
+    rp->pair_evals += (uint64_t)(4 * kSeqSide) * ((uint64_t)n + chunks);
+    rp->window_overflows += chunks;
+    rp->error = err;
+  }
+}
+
+// Sum of a chain's open energy changes over its records (32 lanes).
+__device__ __forceinline__ double open_changes(const jmm_chain_result *__restrict__ rec, uint32_t r0,
+                                               uint32_t nr, int lane) {
+  double s = 0.0;
+  for (uint32_t r = lane; r < nr; r += 32) s = __dadd_rn(s, rec[r0 + r].e);
+  return group_sum_d<32>(s, 0xffffffffu);
+}
+
+// Once per sweep: the chain's running energy into its sums.
+__global__ void sweep_stats_kernel(const LargeChain *__restrict__ chains,
+                                   LargeState *__restrict__ states,
+                                   const jmm_chain_result *__restrict__ rec, uint32_t n_chains,
+                                   int32_t seq_base) {
+  const uint32_t c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (c >= n_chains) return;
+  const LargeChain ch = chains[c];
+  const int lane = threadIdx.x & 31;
+  const double s = seq_base < 0 ? open_changes(rec, ch.rec0, ch.n_dom, lane)
+                                : open_changes(rec, (uint32_t)seq_base + c, 1, lane);
+  if (lane == 0) {
+    LargeState st = states[c];
+    const double e = __dadd_rn(st.e_base, s);
+    st.sum_e = __dadd_rn(st.sum_e, e);
+    st.sum_e2 = __dadd_rn(st.sum_e2, __dmul_rn(e, e));
+    st.samples += 1;
+    st.sweeps += 1;
+    states[c] = st;
+  }
+}
+
+// Fresh energy of each chain from the FP64 positions: FP32 pair terms of the
+// FP64 separations, FP32 per-particle sums, FP64 lane and chain sums.
+__global__ void large_energy_kernel(const LargeChain *__restrict__ chains,
+                                    const double *__restrict__ x, double *__restrict__ e_out,
+                                    uint32_t n_chains) {
+  const uint32_t c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (c >= n_chains) return;
+  const LargeChain ch = chains[c];
+  const ChainParams P = domain_params(ch, 0, ch.n);
+  const double *xc = x + ch.x_base;
+  const int lane = threadIdx.x & 31;
+  const int n = (int)ch.n;
+  double u = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    const double xi = xc[i];
+    float e = 0.0f;
+    for (int j = i + 1; j < n; ++j) {
+      const float d = (float)__dsub_rn(xc[j], xi);
+      const float d2 = __fmul_rn(d, d);
+      if (d2 > P.rc2) break;
+      e = __fadd_rn(e, pair_energy<false>(d2, P));
+    }
+    u = __dadd_rn(u, (double)e);
+  }
+  u = group_sum_d<32>(u, 0xffffffffu);
+  if (lane == 0) e_out[c] = u;
+}
+
+// After a re-summation: the new base; the records' open changes back to 0.
+__global__ void rebase_kernel(const LargeChain *__restrict__ chains, LargeState *__restrict__ states,
+                              jmm_chain_result *__restrict__ rec, const double *__restrict__ e,
+                              uint32_t n_chains, int32_t seq_base, bool note) {
+  const uint32_t c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (c >= n_chains) return;
+  const LargeChain ch = chains[c];
+  const int lane = threadIdx.x & 31;
+  const uint32_t r0 = seq_base < 0 ? ch.rec0 : (uint32_t)seq_base + c;
+  const uint32_t nr = seq_base < 0 ? ch.n_dom : 1;
+  const double s = open_changes(rec, r0, nr, lane);
+  __syncwarp();
+  for (uint32_t r = lane; r < nr; r += 32) rec[r0 + r].e = 0.0;
+  if (lane == 0) {
+    const double drift = fabs(__dsub_rn(__dadd_rn(states[c].e_base, s), e[c]));
+    if (note && drift > states[c].max_drift) states[c].max_drift = drift;
+    states[c].e_base = e[c];
+  }
+}
+
+template <int POT>
+void launch_phase(const LargeChain *d_chains, const LargeState *d_states, jmm_chain_result *d_rec,
+                  double *d_x, uint32_t n_chains, uint32_t b, uint32_t phase, uint32_t doms_per_chain,
+                  const KernelCfg &kc, cudaStream_t s) {
+  const uint64_t warps = (uint64_t)n_chains * doms_per_chain;
+  const uint32_t blocks = (uint32_t)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  const size_t smem = (size_t)kWarpsPerBlock * (kRingWords + b + 2 * kGhost) * sizeof(float);
+  domain_kernel<POT><<<blocks, 32 * kWarpsPerBlock, smem, s>>>(d_chains, d_states, d_rec, d_x,
+                                                               n_chains, b, phase, doms_per_chain, kc);
+}
+
+}  // namespace
+
+struct jmm_large {
+  jmm_batch_config cfg;
+  uint32_t n_chains = 0, b = 0, doms_per_chain = 0, records = 0;
+  std::vector<LargeChain> host_chains;
+  uint64_t total = 0;        // doubles in the padded position buffer
+  bool pots[3] = {false, false, false};
+  LargeChain *d_chains = nullptr;
+  LargeState *d_states = nullptr;
+  jmm_chain_result *d_rec = nullptr;  // domain records, then one per chain for the sequential sweep
+  double *d_x = nullptr;
+  double *d_e = nullptr;
+  cudaStream_t stream = nullptr;
+  uint64_t sweeps_since_resum = 0;
+  int mode = 0;              // records holding the open changes: 0 domains, 1 sequential
+};
+
+static void large_free(jmm_large *h) {
+  if (!h) return;
+  cudaFree(h->d_chains);
+  cudaFree(h->d_states);
+  cudaFree(h->d_rec);
+  cudaFree(h->d_x);
+  cudaFree(h->d_e);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+static KernelCfg large_cfg(const jmm_large *h) {
+  KernelCfg kc;
+  kc.seed = h->cfg.seed;
+  kc.n_sweeps = 1;
+  kc.boundary = JMM_BOUNDARY_WALLS;
+  kc.vol_move = JMM_VOLMOVE_LNL;
+  kc.vol_schedule = JMM_VOLSCHED_SWEEP;
+  kc.resum_sweeps = 0;
+  kc.n_chains = h->n_chains;
+  kc.chains_per_block = 1;
+  return kc;
+}
+
+static int32_t seq_base_of(const jmm_large *h, int mode) {
+  return mode == 0 ? -1 : (int32_t)h->records;
+}
+
+// FP64 re-summation on stream s: new base energies, open changes folded.
+static int resum(jmm_large *h, cudaStream_t s, bool note) {
+  const uint32_t blocks = (h->n_chains + kStatWarps - 1) / kStatWarps;
+  large_energy_kernel<<<blocks, 32 * kStatWarps, 0, s>>>(h->d_chains, h->d_x, h->d_e, h->n_chains);
+  rebase_kernel<<<blocks, 32 * kStatWarps, 0, s>>>(h->d_chains, h->d_states, h->d_rec, h->d_e,
+                                                   h->n_chains, seq_base_of(h, h->mode), note);
+  JMM_CUDA(cudaGetLastError());
+  h->sweeps_since_resum = 0;
+  return JMM_OK;
+}
+
+static int enqueue(jmm_large *h, uint64_t n_sweeps, int mode, cudaStream_t s) {
+  if (h->mode != mode) {
+    const int rc = resum(h, s, true);  // fold the other records' changes into the base
+    if (rc) return rc;
+    h->mode = mode;
+  }
+  const KernelCfg kc = large_cfg(h);
+  const uint32_t sblocks = (h->n_chains + kStatWarps - 1) / kStatWarps;
+  for (uint64_t sw = 0; sw < n_sweeps; ++sw) {
+    if (mode == 0) {
+      for (uint32_t phase = 0; phase < 2; ++phase) {
+        if (h->pots[0])
+          launch_phase<JMM_POT_LJCUT>(h->d_chains, h->d_states, h->d_rec, h->d_x, h->n_chains, h->b,
+                                      phase, h->doms_per_chain, kc, s);
+        if (h->pots[1])
+          launch_phase<JMM_POT_SOFTSPHERE>(h->d_chains, h->d_states, h->d_rec, h->d_x, h->n_chains,
+                                           h->b, phase, h->doms_per_chain, kc, s);
+        if (h->pots[2])
+          launch_phase<JMM_POT_GAUSS>(h->d_chains, h->d_states, h->d_rec, h->d_x, h->n_chains, h->b,
+                                      phase, h->doms_per_chain, kc, s);
+      }
+    } else {
+      const uint32_t base = h->records;
+      if (h->pots[0])
+        sequential_kernel<JMM_POT_LJCUT><<<h->n_chains, 32, 0, s>>>(h->d_chains, h->d_rec, h->d_x,
+                                                                   h->n_chains, base, kc);
+      if (h->pots[1])
+        sequential_kernel<JMM_POT_SOFTSPHERE><<<h->n_chains, 32, 0, s>>>(h->d_chains, h->d_rec,
+                                                                        h->d_x, h->n_chains, base, kc);
+      if (h->pots[2])
+        sequential_kernel<JMM_POT_GAUSS><<<h->n_chains, 32, 0, s>>>(h->d_chains, h->d_rec, h->d_x,
+                                                                   h->n_chains, base, kc);
+    }
+    sweep_stats_kernel<<<sblocks, 32 * kStatWarps, 0, s>>>(h->d_chains, h->d_states, h->d_rec,
+                                                           h->n_chains, seq_base_of(h, mode));
+    JMM_CUDA(cudaGetLastError());
+    if (h->cfg.resum_sweeps && ++h->sweeps_since_resum >= h->cfg.resum_sweeps) {
+      const int rc = resum(h, s, true);
+      if (rc) return rc;
+    }
+  }
+  return JMM_OK;
+}
+
+extern "C" int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                                uint32_t n_chains, uint32_t domain_size, jmm_large **out) {
+  clear_error();
+  JMM_CHECK_ARG(cfg && chains && out && n_chains > 0, "null argument or no chains");
+  *out = nullptr;
+  JMM_CHECK_ARG(domain_size >= 2 * kGhost && domain_size <= 8192,
+                "domain_size must be in [32, 8192]");
+  JMM_CHECK_ARG(cfg->boundary == JMM_BOUNDARY_WALLS, "hard walls only");
+  JMM_CHECK_ARG(cfg->precision == JMM_PREC_FAST, "JMM_PREC_FAST only");
+  for (uint32_t k = 0; k < n_chains; ++k) {
+    const jmm_chain_desc &c = chains[k];
+    if (c.n < domain_size || c.n > (1u << 24))
+      return fail(JMM_ERR_INVALID, "jmm_large_create: chain %u: N must be in [domain_size, 2^24]", k);
+    if (c.ensemble != JMM_NLT)
+      return fail(JMM_ERR_INVALID, "jmm_large_create: chain %u: constant-L chains only", k);
+    if (c.potential != JMM_POT_LJCUT && c.potential != JMM_POT_SOFTSPHERE &&
+        c.potential != JMM_POT_GAUSS)
+      return fail(JMM_ERR_INVALID, "jmm_large_create: chain %u: unknown potential", k);
+    if (!(c.t > 0) || !(c.l0 > 0) || !(c.sigma > 0) || !(c.cutoff > 0) || !(c.max_step > 0))
+      return fail(JMM_ERR_INVALID,
+                  "jmm_large_create: chain %u: T, L, sigma, cut-off and step must be positive", k);
+  }
+  if (!jmm_device_available()) return fail(JMM_ERR_CUDA, "jmm_large_create: no CUDA device");
+  jmm_large *h = new (std::nothrow) jmm_large();
+  if (!h) return fail(JMM_ERR_NOMEM, "jmm_large_create: host allocation failed");
+  h->cfg = *cfg;
+  h->n_chains = n_chains;
+  h->b = domain_size;
+  uint32_t max_dom = 0;
+  uint64_t off = 0;
+  uint64_t rec = 0;
+  for (uint32_t k = 0; k < n_chains; ++k) {
+    const jmm_chain_desc &c = chains[k];
+    LargeChain lc;
+    memset(&lc, 0, sizeof(lc));
+    lc.x_base = off + kGhost;
+    lc.n = c.n;
+    lc.pot = (uint32_t)c.potential;
+    lc.n_dom = (c.n + domain_size - 1) / domain_size + 1;
+    lc.rec0 = (uint32_t)rec;
+    lc.eps4 = c.potential == JMM_POT_LJCUT ? (float)(4.0 * c.eps) : (float)c.eps;
+    lc.sigma2 = (float)(c.sigma * c.sigma);
+    lc.inv_sigma2 = (float)(1.0 / (c.sigma * c.sigma));
+    lc.rc2 = (float)(c.cutoff * c.cutoff);
+    lc.rc = (float)c.cutoff;
+    lc.beta = (float)(1.0 / c.t);
+    lc.two_max_step = (float)(2.0 * c.max_step);
+    lc.l = c.l0;
+    h->host_chains.push_back(lc);
+    h->pots[c.potential == JMM_POT_LJCUT ? 0 : (c.potential == JMM_POT_SOFTSPHERE ? 1 : 2)] = true;
+    rec += lc.n_dom;
+    max_dom = std::max(max_dom, lc.n_dom);
+    off += (uint64_t)c.n + 2 * kGhost;
+  }
+  if (rec + n_chains > 0x7fffffffull) {
+    large_free(h);
+    return fail(JMM_ERR_INVALID, "jmm_large_create: too many domains");
+  }
+  h->records = (uint32_t)rec;
+  h->doms_per_chain = (max_dom + 1) / 2;
+  h->total = off;
+
+  const uint64_t n_rec = rec + n_chains;
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_chains, n_chains * sizeof(LargeChain));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_states, n_chains * sizeof(LargeState));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_rec, n_rec * sizeof(jmm_chain_result));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_x, off * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_e, n_chains * sizeof(double));
+  if (e != cudaSuccess) {
+    const int rc = cuda_status(e, "jmm_large_create allocation", __FILE__, __LINE__);
+    large_free(h);
+    return rc;
+  }
+  // lattice (plus jitter, the batched chains' draw), far sentinels in the padding
+  std::vector<double> x(off, 0.0);
+  for (uint32_t k = 0; k < n_chains; ++k) {
+    const jmm_chain_desc &c = chains[k];
+    double *xc = x.data() + h->host_chains[k].x_base;
+    for (int g = 1; g <= kGhost; ++g) {
+      xc[-g] = -(double)kFar;
+      xc[c.n - 1 + g] = (double)kFar;
+    }
+    for (uint32_t i = 0; i < c.n; ++i) {
+      double r = ((i + 0.5) / c.n - 0.5) * c.l0;
+      if (cfg->init == JMM_INIT_JITTER) {
+        const Words4 w = step_words(cfg->seed, (1ull << 63) | i, k);
+        r += cfg->jitter * (2.0 * word_to_unit(w.w[0]) - 1.0);
+      }
+      xc[i] = r;
+    }
+  }
+  std::vector<jmm_chain_result> recs(n_rec);
+  memset(recs.data(), 0, recs.size() * sizeof(jmm_chain_result));
+  std::vector<LargeState> st(n_chains);
+  memset(st.data(), 0, st.size() * sizeof(LargeState));
+  e = cudaMemcpy(h->d_chains, h->host_chains.data(), n_chains * sizeof(LargeChain),
+                 cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(h->d_x, x.data(), off * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(h->d_rec, recs.data(), n_rec * sizeof(jmm_chain_result), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(h->d_states, st.data(), n_chains * sizeof(LargeState), cudaMemcpyHostToDevice);
+  const size_t smem = (size_t)kWarpsPerBlock * (kRingWords + domain_size + 2 * kGhost) * sizeof(float);
+  if (e == cudaSuccess && smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(domain_kernel<JMM_POT_LJCUT>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(domain_kernel<JMM_POT_SOFTSPHERE>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(domain_kernel<JMM_POT_GAUSS>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  }
+  if (e != cudaSuccess) {
+    const int rc = cuda_status(e, "jmm_large_create upload", __FILE__, __LINE__);
+    large_free(h);
+    return rc;
+  }
+  int rc = resum(h, h->stream, false);  // initial energies
+  if (rc == JMM_OK) {
+    e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) rc = cuda_status(e, "jmm_large_create energies", __FILE__, __LINE__);
+  }
+  if (rc) {
+    large_free(h);
+    return rc;
+  }
+  *out = h;
+  return JMM_OK;
+}
+
+extern "C" int jmm_large_destroy(jmm_large *h) {
+  large_free(h);
+  return JMM_OK;
+}
+
+extern "C" int jmm_large_run_async(jmm_large *h, uint64_t n_sweeps, int32_t mode, void *stream) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  JMM_CHECK_ARG(mode == JMM_LARGE_DOMAINS || mode == JMM_LARGE_SEQUENTIAL, "unknown sweep mode");
+  return enqueue(h, n_sweeps, mode == JMM_LARGE_DOMAINS ? 0 : 1,
+                 stream ? (cudaStream_t)stream : h->stream);
+}
+
+extern "C" int jmm_large_run(jmm_large *h, uint64_t n_sweeps, int32_t mode) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  JMM_CHECK_ARG(mode == JMM_LARGE_DOMAINS || mode == JMM_LARGE_SEQUENTIAL, "unknown sweep mode");
+  const int rc = enqueue(h, n_sweeps, mode == JMM_LARGE_DOMAINS ? 0 : 1, h->stream);
+  if (rc) return rc;
+  JMM_CUDA(cudaStreamSynchronize(h->stream));
+  return JMM_OK;
+}
+
+extern "C" int jmm_large_results(jmm_large *h, jmm_large_result *out, uint32_t n_chains) {
+  clear_error();
+  JMM_CHECK_ARG(h && out, "null argument");
+  JMM_CHECK_ARG(n_chains == h->n_chains, "n_chains does not match");
+  JMM_CUDA(cudaDeviceSynchronize());
+  const uint64_t n_rec = (uint64_t)h->records + n_chains;
+  std::vector<LargeState> st(n_chains);
+  std::vector<jmm_chain_result> rec(n_rec);
+  JMM_CUDA(cudaMemcpy(st.data(), h->d_states, n_chains * sizeof(LargeState), cudaMemcpyDeviceToHost));
+  JMM_CUDA(cudaMemcpy(rec.data(), h->d_rec, n_rec * sizeof(jmm_chain_result), cudaMemcpyDeviceToHost));
+  for (uint32_t k = 0; k < n_chains; ++k) {
+    jmm_large_result &r = out[k];
+    memset(&r, 0, sizeof(r));
+    const LargeChain &lc = h->host_chains[k];
+    double open = 0.0;
+    for (uint32_t d = 0; d <= lc.n_dom; ++d) {
+      const jmm_chain_result &x = rec[d < lc.n_dom ? lc.rec0 + d : h->records + k];
+      open += x.e;
+      r.moves += x.disp_att;
+      r.accepted += x.disp_acc;
+      r.pair_evals += x.pair_evals;
+      r.window_overflows += x.window_overflows;
+      r.error |= x.error;
+    }
+    r.e = st[k].e_base + open;
+    r.l = lc.l;
+    r.sweeps = st[k].sweeps;
+    r.samples = st[k].samples;
+    r.sum_e = st[k].sum_e;
+    r.sum_e2 = st[k].sum_e2;
+    r.max_drift = st[k].max_drift;
+  }
+  return JMM_OK;
+}
+
+extern "C" int jmm_large_reset_stats(jmm_large *h) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  JMM_CUDA(cudaDeviceSynchronize());
+  std::vector<LargeState> st(h->n_chains);
+  JMM_CUDA(cudaMemcpy(st.data(), h->d_states, h->n_chains * sizeof(LargeState),
+                      cudaMemcpyDeviceToHost));
+  for (auto &s : st) {
+    s.sum_e = s.sum_e2 = 0.0;
+    s.samples = 0;
+    s.max_drift = 0.0;
+  }
+  JMM_CUDA(cudaMemcpy(h->d_states, st.data(), h->n_chains * sizeof(LargeState),
+                      cudaMemcpyHostToDevice));
+  return JMM_OK;
+}
+
+extern "C" int jmm_large_energies(jmm_large *h, double *e, uint32_t n_chains) {
+  clear_error();
+  JMM_CHECK_ARG(h && e, "null argument");
+  JMM_CHECK_ARG(n_chains == h->n_chains, "n_chains does not match");
+  JMM_CUDA(cudaDeviceSynchronize());
+  const uint32_t blocks = (h->n_chains + kStatWarps - 1) / kStatWarps;
+  large_energy_kernel<<<blocks, 32 * kStatWarps, 0, h->stream>>>(h->d_chains, h->d_x, h->d_e,
+                                                                 h->n_chains);
+  JMM_CUDA(cudaGetLastError());
+  JMM_CUDA(cudaStreamSynchronize(h->stream));
+  JMM_CUDA(cudaMemcpy(e, h->d_e, n_chains * sizeof(double), cudaMemcpyDeviceToHost));
+  return JMM_OK;
+}
+
+extern "C" int jmm_large_get_positions(jmm_large *h, uint32_t chain, double *x, uint64_t n) {
+  clear_error();
+  JMM_CHECK_ARG(h && x, "null argument");
+  JMM_CHECK_ARG(chain < h->n_chains, "chain index out of range");
+  JMM_CHECK_ARG(n == h->host_chains[chain].n, "N does not match the chain");
+  JMM_CUDA(cudaDeviceSynchronize());
+  JMM_CUDA(cudaMemcpy(x, h->d_x + h->host_chains[chain].x_base, n * sizeof(double),
+                      cudaMemcpyDeviceToHost));
+  return JMM_OK;
+}
+
+extern "C" int jmm_large_set_positions(jmm_large *h, uint32_t chain, const double *x, uint64_t n) {
+  clear_error();
+  JMM_CHECK_ARG(h && x, "null argument");
+  JMM_CHECK_ARG(chain < h->n_chains, "chain index out of range");
+  JMM_CHECK_ARG(n == h->host_chains[chain].n, "N does not match the chain");
+  const double half = 0.5 * h->host_chains[chain].l;
+  for (uint64_t i = 0; i < n; ++i) {
+    if (!(fabs(x[i]) <= half))
+      return fail(JMM_ERR_INVALID, "jmm_large_set_positions: x[%llu] outside the walls",
+                  (unsigned long long)i);
+    if (i > 0 && !(x[i] > x[i - 1]))
+      return fail(JMM_ERR_INVALID, "jmm_large_set_positions: positions must increase (x[%llu])",
+                  (unsigned long long)i);
+  }
+  JMM_CUDA(cudaDeviceSynchronize());
+  JMM_CUDA(cudaMemcpy(h->d_x + h->host_chains[chain].x_base, x, n * sizeof(double),
+                      cudaMemcpyHostToDevice));
+  // fresh base energies for every chain; open changes folded
+  const int rc = resum(h, h->stream, false);
+  if (rc) return rc;
+  JMM_CUDA(cudaStreamSynchronize(h->stream));
+  return JMM_OK;
+}

@@ -52,7 +52,10 @@ def _c_sizeof(type_name):
 
 @pytest.mark.parametrize("cname,pytype", [
     ("jmm_params", abi.Params), ("jmm_state", abi.State), ("jmm_draw", abi.Draw),
-    ("jmm_step_record", abi.StepRecord),
+    ("jmm_step_record", abi.StepRecord), ("jmm_chain_desc", abi.ChainDesc),
+    ("jmm_batch_config", abi.BatchConfig), ("jmm_chain_result", abi.ChainResult),
+    ("jmm_grad_chain", abi.GradChain), ("jmm_grad_stats", abi.GradStats),
+    ("jmm_large_result", abi.LargeResult),
 ])
 def test_struct_layouts_match_header(cname, pytype):
     assert _c_sizeof(cname) == C.sizeof(pytype)

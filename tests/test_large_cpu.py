@@ -1,0 +1,33 @@
+"""Argument checks of the large-chain entry points (jmm_large_*): every bad
+combination is refused with JMM_ERR_INVALID before any device work, so these
+run without a GPU."""
+import pytest
+
+from jmmonedmc_gb300 import _native, abi
+from jmmonedmc_gb300.large import LargeChains
+
+
+def _expect_invalid(cfg, chains, b):
+    with pytest.raises(_native.JmmError) as ei:
+        LargeChains(cfg, chains, domain_size=b)
+    assert ei.value.code == abi.JMM_ERR_INVALID
+
+
+def _chain(n=4096, **kw):
+    return abi.make_chain(n, rho=0.7, t=1.2, cutoff=2.5, max_step=0.4, **kw)
+
+
+def test_domain_size_bounds(native):
+    cfg = abi.make_batch_config(seed=1)
+    _expect_invalid(cfg, [_chain()], 16)       # below 2 x 16 halo particles
+    _expect_invalid(cfg, [_chain()], 16384)    # above 8192
+    _expect_invalid(cfg, [_chain(n=100)], 128)  # N below the domain size
+
+
+def test_unsupported_chains(native):
+    cfg = abi.make_batch_config(seed=1)
+    _expect_invalid(cfg, [_chain(ensemble=abi.JMM_NPT)], 256)
+    _expect_invalid(cfg, [_chain(potential=abi.JMM_POT_HARMONIC)], 256)
+    _expect_invalid(abi.make_batch_config(seed=1, boundary=abi.JMM_BOUNDARY_PERIODIC),
+                    [_chain()], 256)
+    _expect_invalid(abi.make_batch_config(seed=1, precision=abi.JMM_PREC_EXACT), [_chain()], 256)
