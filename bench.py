@@ -55,16 +55,26 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=1.5,
                     help="wall seconds per host core for the CPU baseline sample")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--workload", choices=("npt", "uneven"), default="npt",
+    ap.add_argument("--workload", choices=("npt", "uneven", "large"), default="npt",
                     help="npt: the batched NPT headline workload; uneven: 1024 chains of "
                          "N ~ U{32..2048}, rho ~ U(0.3, 0.9), LJ / soft sphere / Gaussian core, "
-                         "T ~ U(0.5, 2), NVT")
+                         "T ~ U(0.5, 2), NVT; large: 64 chains of N = 2^20 LJ particles, "
+                         "rho 0.7, rc 2.5, T 1.2, alternating-domain sweep")
+    ap.add_argument("--domain-size", type=int, default=1024,
+                    help="large workload: particles per domain")
     args = ap.parse_args()
     if args.workload == "uneven":
         if args.chains == 4096:
             args.chains = 1024
         if args.sweeps_per_step == 1000:
             args.sweeps_per_step = 500
+    if args.workload == "large":
+        if args.chains == 4096:
+            args.chains = 64
+        if args.n == 256:
+            args.n = 1 << 20
+        if args.sweeps_per_step == 1000:
+            args.sweeps_per_step = 20
     return args
 
 
@@ -264,6 +274,241 @@ def profile_traffic(args, pair_evals_per_launch, sweeps):
     return args.chains * (per * sweeps + fixed)
 
 
+# ---- the large-chain workload -------------------------------------------------------
+
+LARGE_METRIC = "attempted MC moves/s (large chains, alternating-domain sweep, FP32 pairs)"
+
+
+def large_workload(args, seed):
+    """64 chains of N = 2^20 LJ 12-6 particles, rho 0.7, rc 2.5, T 1.2, NVT."""
+    from jmmonedmc_gb300 import abi
+    chains = [abi.make_chain(args.n, potential=abi.JMM_POT_LJCUT, ensemble=abi.JMM_NLT,
+                             cutoff=2.5, t=1.2, rho=0.7, max_step=0.3)
+              for _ in range(args.chains)]
+    cfg = abi.make_batch_config(seed=seed, resum_sweeps=0)
+    return cfg, chains
+
+
+def large_config(args, extra=None):
+    d = {"workload": (f"large chains: {args.chains} chains x N={args.n}, LJ 12-6 eps=sigma=1 "
+                      "rc=2.5, rho=0.7, T=1.2, NVT, hard walls, max displacement 0.3, lattice "
+                      f"start; alternating-domain sweep, domains of {args.domain_size}"),
+         "chains": args.chains, "particles_per_chain": args.n,
+         "sweeps_per_step": args.sweeps_per_step, "domain_size": args.domain_size,
+         "l2": f"inputs larger than L2 ({args.chains * (args.n + 32) * 8 >> 20} MiB of int64 "
+               "positions), no flush",
+         "precision": "positions int64 on a 2^-k grid, FP32 step arithmetic in domain frames, "
+                      "FP64 energies"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def _cpu_large_worker(job):
+    """One host core: one chain of the large workload with the FP64 CPU
+    restatement (cut-off window, sequential Metropolis), `seconds` of wall."""
+    n, seed, seconds, repo, k = job
+    sys.path.insert(0, repo)
+    from jmmonedmc_gb300 import abi
+    from tests import oracle_lib
+    chain = abi.make_chain(n, potential=abi.JMM_POT_LJCUT, ensemble=abi.JMM_NLT, cutoff=2.5,
+                           t=1.2, rho=0.7, max_step=0.3)
+    ob = oracle_lib.OracleBatch(abi.make_batch_config(seed=seed + k, resum_sweeps=0), [chain],
+                                fp64=True)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        ob.run(1)
+        steps += n
+        if time.perf_counter() - t0 >= seconds:
+            break
+    return steps, time.perf_counter() - t0
+
+
+def cpu_large_sample(args, seconds):
+    import multiprocessing as mp
+    from tests import oracle_lib
+    oracle_lib.load()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        out = pool.map(_cpu_large_worker, [(args.n, args.seed, seconds, REPO, k)
+                                           for k in range(cores)])
+    wall = time.perf_counter() - t0
+    steps = sum(s for s, _ in out)
+    per_core_wall = max(w for _, w in out)
+    return {"value": steps / per_core_wall, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"{cores} chains of the workload (N={args.n} each), one per host core, "
+                       f"whole sweeps for {seconds:.1f} s each with the FP64 CPU restatement "
+                       "(oracle/batch_oracle.c in FP64: sequential Metropolis with the cut-off "
+                       "window; the reference itself cannot hold N=2^20, its pair arrays are "
+                       "O(N^2)); aggregate attempted moves / wall"),
+            "steps": steps, "wall_s": wall}
+
+
+def run_large(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import ctypes as C
+
+    from jmmonedmc_gb300 import _native, build
+    if not os.path.exists(_native.lib_path()):
+        build.build_native()
+    from jmmonedmc_gb300.large import LargeChains, run_host
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    cfg, chains = large_workload(args, args.seed + 1000003 * rank)
+    cpu = cpu_large_sample(args, args.cpu_seconds) if rank == 0 and world == 1 else None
+    fp32_peak, rcp_peak = C.c_double(), C.c_double()
+    _native.call("jmm_measure_peaks", C.byref(fp32_peak), C.byref(rcp_peak))
+
+    h = LargeChains(cfg, chains, domain_size=args.domain_size)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    S = args.sweeps_per_step
+    for _ in range(args.warmup):
+        h.run_async(S, "domains", stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    before = h.results()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        starts[k].record(stream)
+        h.run_async(S, "domains", stream.cuda_stream)
+        ends[k].record(stream)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    after = h.results()
+    if np.any(after["error"] != 0):
+        raise RuntimeError(f"chain errors: {np.unique(after['error'])}")
+    moves = int((after["moves"] - before["moves"]).sum())
+    pairs = int((after["pair_evals"] - before["pair_evals"]).sum())
+    total_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms, moves], dtype=torch.float64, device=dev)
+        tmax, tsum = t.clone(), t.clone()
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
+        total_ms, moves_all = float(tmax[0]), float(tsum[1])
+    else:
+        moves_all = moves
+
+    # the sequential plain sweep of the same chains, one sweep, beside
+    seq_start, seq_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r0 = h.results()
+    seq_start.record(stream)
+    h.run_async(1, "sequential", stream.cuda_stream)
+    seq_end.record(stream)
+    torch.cuda.synchronize(dev)
+    seq_ms = seq_start.elapsed_time(seq_end)
+    r1 = h.results()
+    seq_moves = int((r1["moves"] - r0["moves"]).sum())
+
+    # e2e: host buffers through the C ABI (jmm_large_run_host), H2D and D2H inside
+    n_tot = args.chains * args.n
+    x_host = torch.empty(n_tot, dtype=torch.float64, pin_memory=True).numpy()
+    x_back = torch.empty(n_tot, dtype=torch.float64, pin_memory=True).numpy()
+    for k in range(args.chains):
+        x_host[k * args.n:(k + 1) * args.n] = h.positions(k)
+    h.close()
+    e2e_times, e2e_moves = [], 0
+    for j in range(args.e2e_steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        res_h, _ = run_host(cfg, chains, S, domain_size=args.domain_size, mode="domains",
+                            x_in=x_host, x_out=x_back)
+        e2e_times.append(time.perf_counter() - t0)
+        e2e_moves += int(res_h["moves"].sum())
+        x_host, x_back = x_back, x_host
+    e2e_value = e2e_moves / sum(e2e_times) * world
+    h2d = n_tot * 8 + args.chains * C.sizeof(chains[0]) + 64
+    d2h = n_tot * 8 + args.chains * 120
+
+    launches_per_step = 3 * S
+    launch_ms = total_ms / (args.steps * 2 * S)  # the two domain launches of a sweep dominate
+    pairs_per_launch = pairs / (args.steps * 2 * S)
+    achieved = pairs_per_launch * FLOP_PER_PAIR / (launch_ms * 1e-3) / 1e12
+    line = {
+        "metric": LARGE_METRIC,
+        "value": moves_all / (total_ms * 1e-3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (lattice start, seeded Philox moves)",
+        "config": large_config(args, {"parallelism": f"replicas{world}", "wall_s_timed": wall,
+                                      "grid": float(after["grid"][0])}),
+        "roofline": {
+            "bound": "fp32",
+            "achieved": achieved,
+            "peak": fp32_peak.value,
+            "unit": "TFLOP/s",
+            "frac": achieved / fp32_peak.value,
+            "traffic": None,
+            "peak_source": "measured live by jmm_measure_peaks (FP32 FMA kernel; "
+                           "MEASURED_PEAKS.json holds no FP32 figure)",
+            "pair_evals_per_launch": pairs_per_launch,
+            "flop_per_pair": FLOP_PER_PAIR,
+            "mufu_rcp_frac": pairs_per_launch / (launch_ms * 1e-3) / (rcp_peak.value * 1e12),
+            "kernel": "domain_kernel (one colour phase of one sweep)",
+        },
+        "sequential": {"value": seq_moves / (seq_ms * 1e-3), "unit": UNIT, "ms_per_sweep": seq_ms,
+                       "how": "jmm_large_run(mode SEQUENTIAL): one warp per chain, one sweep of "
+                              "the same chains after the timed region"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "how": "jmm_large_run_host per step: pinned float64 host positions in, results "
+                       "and positions out, handle set-up inside the timed region"},
+        "gpu_launches": args.steps * launches_per_step,
+        "clocks": clocks,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    return line
+
+
+def run_reference_large(args):
+    cores = os.cpu_count() or 1
+    per_step = max(0.3, args.cpu_seconds / 2)
+    for _ in range(args.warmup):
+        cpu_large_sample(args, 0.2)
+    t_total, steps_total, last = 0.0, 0, None
+    for _ in range(args.steps):
+        last = cpu_large_sample(args, per_step)
+        t_total += last["steps"] / last["value"]
+        steps_total += last["steps"]
+    value = steps_total / t_total
+    return {
+        "metric": LARGE_METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_total / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (same chains as the GPU arm)",
+        "config": large_config(args, {"parallelism": f"host cores x{cores}"}),
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": last["sample"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
 # ---- our implementation ----------------------------------------------------------
 
 def run_ours(args, rank, world, local_rank):
@@ -461,13 +706,14 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        print(json.dumps(run_reference(args)), flush=True)
+        ref = run_reference_large if args.workload == "large" else run_reference
+        print(json.dumps(ref(args)), flush=True)
         return 0
     if world > 1:
         import torch
         torch.cuda.set_device(local_rank)
         torch.distributed.init_process_group("nccl")
-    line = run_ours(args, rank, world, local_rank)
+    line = (run_large if args.workload == "large" else run_ours)(args, rank, world, local_rank)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

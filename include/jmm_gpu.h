@@ -311,7 +311,9 @@ int jmm_batch_run_host(const jmm_batch_config *cfg, const jmm_chain_desc *chains
 /* ---- large chains (N up to 2^24): the alternating-domain sweep ---------- */
 /* No counterpart in the reference, which holds O(N^2) pair arrays per chain
  * (src/jmmMCState.cpp:308-328,439-455) and cannot run N = 2^20.  Constant-L
- * chains with hard walls, FP64 positions in HBM, FP32 step arithmetic. */
+ * chains with hard walls; positions are int64 multiples of a grid step 2^-k
+ * per chain (chosen so that a domain spans < 2^23 steps), exact in the FP32
+ * step arithmetic; trial displacements are snapped to the grid. */
 
 #define JMM_LARGE_DOMAINS 0     /* alternating-domain sweep: domains of B
                                    particles from a random offset, two colours
@@ -327,9 +329,11 @@ typedef struct jmm_large_result {
   double sum_e, sum_e2;  /* one sample of E per sweep                          */
   uint64_t moves, accepted, pair_evals, window_overflows;
   double max_drift;      /* largest |running E - fresh FP64 sum| at a re-sum   */
+  double grid;           /* positions are multiples of this step (2^-k)        */
   uint32_t error;        /* JMM_ERR_* seen by a kernel (JMM_ERR_INVALID: a
                             domain's 16-particle halo did not reach beyond the
-                            cut-off; the domain was skipped that sweep)        */
+                            cut-off, or the domain spanned more than 2^24 grid
+                            steps; the domain was skipped that sweep)         */
   uint32_t reserved;
 } jmm_large_result;
 
@@ -350,9 +354,17 @@ int jmm_large_reset_stats(jmm_large *h);
 /* Fresh energies of the current positions (FP32 pair terms, FP64 sums). */
 int jmm_large_energies(jmm_large *h, double *e, uint32_t n_chains);
 int jmm_large_get_positions(jmm_large *h, uint32_t chain, double *x, uint64_t n);
-/* Positions must increase and lie within +-L/2; energies are re-summed. */
+/* Positions are snapped to the grid, must then increase and lie within
+ * +-L/2; energies are re-summed. */
 int jmm_large_set_positions(jmm_large *h, uint32_t chain, const double *x, uint64_t n);
 int jmm_large_destroy(jmm_large *h);
+/* Host-buffer convenience: create, upload positions (NULL = the configured
+ * initial lattice; chain after chain, snapped to the grid), run n_sweeps in
+ * mode JMM_LARGE_*, copy results and positions (NULL = skip) back, destroy. */
+int jmm_large_run_host(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                       uint32_t n_chains, uint32_t domain_size, int32_t mode,
+                       const double *x_in, uint64_t n_sweeps, jmm_large_result *results,
+                       double *x_out);
 
 /* The Philox words of steps [block0, block0 + count) of one chain, computed
  * on the device (4 words per step), for RNG verification tooling. */

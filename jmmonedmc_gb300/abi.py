@@ -298,6 +298,7 @@ class LargeResult(C.Structure):
         ("pair_evals", C.c_uint64),
         ("window_overflows", C.c_uint64),
         ("max_drift", C.c_double),
+        ("grid", C.c_double),
         ("error", C.c_uint32),
         ("reserved", C.c_uint32),
     ]
@@ -306,5 +307,6 @@ class LargeResult(C.Structure):
 LARGE_RESULT_DTYPE = [
     ("e", "<f8"), ("l", "<f8"), ("sweeps", "<u8"), ("samples", "<u8"), ("sum_e", "<f8"),
     ("sum_e2", "<f8"), ("moves", "<u8"), ("accepted", "<u8"), ("pair_evals", "<u8"),
-    ("window_overflows", "<u8"), ("max_drift", "<f8"), ("error", "<u4"), ("reserved", "<u4"),
+    ("window_overflows", "<u8"), ("max_drift", "<f8"), ("grid", "<f8"), ("error", "<u4"),
+    ("reserved", "<u4"),
 ]

@@ -62,6 +62,8 @@ struct ChainParams {
   float two_max_step;
   float vol_step;
   float rc;
+  float grid;                // domain sweeps: position grid step 2^-k, displacements
+                             // snapped to it; 0 (unused) for whole chains
   double beta_d, p;
 };
 
@@ -332,6 +334,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
   g.sd = 0.0f;
   g.sd2 = 0.0f;
   g.nseg = 0;
+  const float inv_grid = HALO ? __frcp_rn(P.grid) : 0.0f;
   const uint32_t spsw = P.steps_per_sweep;
   const uint64_t step0 = rp->steps;
   uint32_t sweep_pos = (uint32_t)(step0 % spsw);
@@ -360,7 +363,9 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
           if (npt && (sweep_pos + (uint32_t)e + 1) % spsw == 0) nm_e = n;  // the sweep's volume step
         }
         ring_nm[e] = nm_e;
-        ring_md[e] = nm_e == n ? u1 : __fmul_rn(__fsub_rn(u1, 0.5f), H.two_max_step);
+        float md_e = __fmul_rn(__fsub_rn(u1, 0.5f), H.two_max_step);
+        if (HALO) md_e = __fmul_rn(rintf(__fmul_rn(md_e, inv_grid)), P.grid);  // exact: 2^k scales
+        ring_md[e] = nm_e == n ? u1 : md_e;
         ring_thr[e] = threshold_of(w.w[2]);
       }
       __syncwarp(gmask);

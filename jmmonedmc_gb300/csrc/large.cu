@@ -3,32 +3,36 @@
 // hard walls at +-L/2, ordered particles (LJ, soft sphere or Gaussian with
 // the cut-off window of the batched kernel).
 //
-// Positions live in HBM as FP64: on a chain 1.5e6 long an absolute FP32
-// coordinate has an ulp of 0.0625.  The step arithmetic is FP32 on
-// separations, as in the batched kernel.  Two ways to run the same chain:
+// Positions live in HBM as int64 multiples of a grid step 2^-k chosen per
+// chain so that a domain with its halo spans fewer than 2^22 steps (an
+// absolute FP32 coordinate on a chain 1.5e6 long would have an ulp of
+// 0.0625).  Converting them to FP32 coordinates about a domain's origin is
+// then exact, every separation within the cut-off is the same FP32 number
+// in every kernel, and trial displacements are snapped to the grid.  Two
+// ways to run the same chain:
 //
 //  * Sequential plain sweep (sequential_kernel).  One warp per chain makes
 //    the chain's N single-particle Metropolis steps in order on the HBM
-//    positions: separations are taken in FP64 and rounded to FP32, 16
-//    neighbours per side per pass.  This is the conventional sweep, latency
-//    bound (one dependent HBM round trip per step).
+//    positions, 16 neighbours per side per pass.  This is the conventional
+//    sweep, latency bound (one dependent HBM round trip per step).
 //  * Alternating-domain sweep (domain_kernel).  Per sweep the index range
 //    is cut into domains of B particles from a random offset o in [0, B):
 //    domain d = [o + (d-1)B, o + dB) clipped to [0, N).  The domains of one
 //    colour (d even, or d odd; which colour goes first is random per sweep)
 //    run at the same time, one warp each, then the other colour.  A domain
 //    copies its particles and kGhost = 16 of each neighbour's (frozen for
-//    the phase; far sentinels beyond the chain's ends) into shared memory,
-//    as FP32 coordinates about a local origin, and makes B single-particle
+//    the phase; far sentinels beyond the chain's ends) into shared memory as
+//    FP32 coordinates about a local origin, makes B single-particle
 //    Metropolis steps on its own particles with the batched kernel's step
-//    loop; it writes back, in FP64, only the particles it moved.  Two active
-//    domains are separated by a frozen interior domain of B >= 2 kGhost
-//    particles, and the kernel checks that the halo reaches beyond the
-//    cut-off (else it flags JMM_ERR_INVALID and skips the domain), so they
-//    share no pair: a phase is a product of independent Metropolis chains
-//    on the conditional distribution of each domain given the rest, which
-//    leaves the Boltzmann distribution invariant, and the random offset and
-//    colour order make every particle's position in the layout random.
+//    loop and writes its particles back.  Two active domains are separated
+//    by a frozen interior domain of B >= 2 kGhost particles, and the kernel
+//    checks that the halo reaches beyond the cut-off and that the domain
+//    fits the FP32 frame (else it flags JMM_ERR_INVALID and skips the
+//    domain), so they share no pair: a phase is a product of independent
+//    Metropolis chains on the conditional distribution of each domain given
+//    the rest, which leaves the Boltzmann distribution invariant, and the
+//    random offset and colour order make every particle's position in the
+//    layout random.
 //
 // Energies: each step-loop record accumulates its own energy changes (FP32
 // within a launch, FP64 across launches); a chain's running energy is its
@@ -54,14 +58,18 @@ constexpr int kWarpsPerBlock = 4;
 constexpr int kSeqSide = 16;   // neighbours per side per pass, sequential sweep
 constexpr uint32_t kStatWarps = 8;
 
+constexpr int64_t kFarQ = 1ll << 60;      // sentinel positions beyond the chain's ends
+constexpr int64_t kFrame = 1ll << 24;     // grid steps an FP32 frame holds exactly
+
 struct LargeChain {
-  uint64_t x_base;  // double offset of the chain's particle 0 in the padded buffer
+  uint64_t x_base;  // offset of the chain's particle 0 in the padded position buffer
   uint32_t n;
   uint32_t pot;
   uint32_t rec0;    // first domain record of the chain
   uint32_t n_dom;   // domain records: N/B rounded up, plus one for the offset
   float eps4, sigma2, inv_sigma2, rc2, beta, two_max_step, rc;
-  uint32_t pad;
+  float grid;       // position grid step 2^-k
+  int64_t wall_q;   // walls at +-wall_q grid steps: |x| <= L/2
   double l;
 };
 
@@ -75,6 +83,7 @@ struct LargeState {
 
 __device__ __forceinline__ ChainParams domain_params(const LargeChain &c, uint32_t id, uint32_t n) {
   ChainParams P;
+  P.grid = c.grid;
   P.id = id;
   P.n = n;
   P.pot = c.pot;
@@ -115,10 +124,15 @@ __device__ __forceinline__ void sweep_layout(uint64_t seed, uint32_t chain, uint
   *first = w.w[1] & 1u;
 }
 
+// Grid steps to an FP32 coordinate (exact below kFrame steps).
+__device__ __forceinline__ float q_to_f(int64_t dq, float grid) {
+  return __fmul_rn(__ll2float_rn(dq), grid);
+}
+
 template <int POT>
 __global__ void __maxnreg__(72)
     domain_kernel(const LargeChain *__restrict__ chains, const LargeState *__restrict__ states,
-                  jmm_chain_result *__restrict__ rec, double *__restrict__ x, uint32_t n_chains,
+                  jmm_chain_result *__restrict__ rec, int64_t *__restrict__ q, uint32_t n_chains,
                   uint32_t b, uint32_t phase, uint32_t doms_per_chain, KernelCfg cfg) {
   extern __shared__ float smem[];
   const uint32_t wib = threadIdx.x / 32;
@@ -136,53 +150,54 @@ __global__ void __maxnreg__(72)
   if (hi <= lo) return;
   const int n = (int)(hi - lo);
   const int cl = threadIdx.x & 31;
-  double *xc = x + ch.x_base + lo;  // xc[-kGhost .. n + kGhost - 1] are valid (padding)
+  int64_t *qc = q + ch.x_base + lo;  // qc[-kGhost .. n + kGhost - 1] are valid (padding)
   jmm_chain_result *rp = rec + ch.rec0 + d;
+  const bool left_wall = lo == 0, right_wall = hi == (int64_t)ch.n;
 
-  // the halo must reach beyond the cut-off: unloaded neighbours are farther
-  // than the last halo particle from every particle of the domain
-  const double reach = 1.0001 * (double)ch.rc;
-  const bool right_ok = hi == ch.n || __dsub_rn(xc[n + kGhost - 1], xc[n]) > reach;
-  const bool left_ok = lo == 0 || __dsub_rn(xc[-1], xc[-kGhost]) > reach;
-  if (!(right_ok && left_ok)) {
+  // local origin O and half-width H (grid steps): the walls at +-L/2 map to
+  // +-H in the step loop's symmetric wall test; an interior domain has none
+  int64_t O, H = 0;
+  if (left_wall && right_wall) {
+    O = 0;
+    H = ch.wall_q;
+  } else if (left_wall) {
+    H = (qc[n] + ch.wall_q + 1) >> 1;
+    O = H - ch.wall_q;
+  } else if (right_wall) {
+    H = (ch.wall_q - qc[-1] + 1) >> 1;
+    O = ch.wall_q - H;
+  } else {
+    O = (qc[0] + qc[n - 1]) >> 1;
+  }
+  // the halo must reach beyond the cut-off (unloaded neighbours are then
+  // farther than the last halo particle from every particle of the domain),
+  // and every real particle loaded must fit the FP32 frame
+  const double reach = 1.0001 * (double)ch.rc / (double)ch.grid;
+  const int il = lo >= kGhost ? -kGhost : -(int)lo;
+  const int ir = (int64_t)ch.n - 1 - lo >= n + kGhost - 1 ? n + kGhost - 1 : (int)((int64_t)ch.n - 1 - lo);
+  bool fits = H < kFrame && qc[ir] - O < kFrame && O - qc[il] < kFrame;
+  if (!right_wall) fits = fits && (double)(qc[n + kGhost - 1] - qc[n]) > reach;
+  if (!left_wall) fits = fits && (double)(qc[-1] - qc[-kGhost]) > reach;
+  if (!fits) {
     if (cl == 0) rp->error |= JMM_ERR_INVALID;
     return;
   }
-  // local origin O and half-width h: the walls at +-L/2 map to +-h in the
-  // step loop's symmetric wall test; an interior domain has no wall
-  const double half = __dmul_rn(0.5, ch.l);
-  double O, h;
-  if (lo == 0 && hi == ch.n) {
-    O = 0.0;
-    h = half;
-  } else if (lo == 0) {
-    O = __dmul_rn(0.5, __dsub_rn(xc[n], half));
-    h = __dmul_rn(0.5, __dadd_rn(xc[n], half));
-  } else if (hi == ch.n) {
-    O = __dmul_rn(0.5, __dadd_rn(xc[-1], half));
-    h = __dmul_rn(0.5, __dsub_rn(half, xc[-1]));
-  } else {
-    O = __dmul_rn(0.5, __dadd_rn(xc[0], xc[n - 1]));
-    h = 1e30;
-  }
   uint32_t *ring = reinterpret_cast<uint32_t *>(smem) + wib * (kRingWords + b + 2 * kGhost);
   float *xs = reinterpret_cast<float *>(ring + kRingWords) + kGhost;
-  for (int i = cl - kGhost; i < n + kGhost; i += 32) xs[i] = (float)__dsub_rn(xc[i], O);
-  if (cl == 0) rp->l = __dmul_rn(2.0, h);
+  for (int i = cl - kGhost; i < n + kGhost; i += 32) xs[i] = q_to_f(qc[i] - O, ch.grid);
+  if (cl == 0) rp->l = (left_wall || right_wall) ? __dmul_rn(2.0, (double)q_to_f(H, ch.grid)) : 2e30;
   __syncwarp();
   const ChainParams P = domain_params(ch, ch.rec0 + d, (uint32_t)n);
   run_chain<kG, kS, POT, false, false, true>(P, rec, nullptr, xs, ring, cfg, cl, 0xffffffffu);
   __syncwarp();
-  for (int i = cl; i < n; i += 32) {
-    const float xl = (float)__dsub_rn(xc[i], O);
-    if (xs[i] != xl) xc[i] = __dadd_rn(O, (double)xs[i]);
-  }
+  const float inv_grid = __frcp_rn(ch.grid);
+  for (int i = cl; i < n; i += 32) qc[i] = O + __float2ll_rn(__fmul_rn(xs[i], inv_grid));
 }
 
 template <int POT>
 __global__ void __launch_bounds__(32)
     sequential_kernel(const LargeChain *__restrict__ chains, jmm_chain_result *__restrict__ rec,
-                      double *__restrict__ x, uint32_t n_chains, uint32_t id_base, KernelCfg cfg) {
+                      int64_t *__restrict__ q, uint32_t n_chains, uint32_t id_base, KernelCfg cfg) {
   const uint32_t c = blockIdx.x;
   if (c >= n_chains) return;
   const LargeChain ch = chains[c];
@@ -193,9 +208,9 @@ __global__ void __launch_bounds__(32)
   const int n = (int)ch.n;
   const uint32_t id = id_base + c;
   jmm_chain_result *rp = rec + id;
-  double *xc = x + ch.x_base;  // xc[-kGhost .. n + kGhost - 1] are valid (padding)
+  int64_t *qc = q + ch.x_base;  // qc[-kGhost .. n + kGhost - 1] are valid (padding)
   const Hot H = hot_of(ch);
-  const double half = __dmul_rn(0.5, ch.l);
+  const float grid = ch.grid, inv_grid = __frcp_rn(ch.grid);
   const uint64_t step0 = rp->steps;
   double e_acc = 0.0;
   uint32_t n_acc = 0, chunks = 0;
@@ -206,11 +221,11 @@ __global__ void __launch_bounds__(32)
     const int nm = (int)word_to_index(w.w[0], (uint64_t)n);
     const float md = __fmul_rn(__fsub_rn(word_to_unit_f(w.w[1]), 0.5f), H.two_max_step);
     const float thr = threshold_of(w.w[2]);
-    const double xo = xc[nm];
-    const double xn = __dadd_rn(xo, (double)md);
-    const double xj = xc[nm + side * k0];  // a padding sentinel beyond either end
-    const float dn = (float)(side > 0 ? __dsub_rn(xj, xn) : __dsub_rn(xn, xj));
-    const float dd = (float)(side > 0 ? __dsub_rn(xj, xo) : __dsub_rn(xo, xj));
+    const int64_t qo = qc[nm];
+    const int64_t qn = qo + __float2ll_rn(__fmul_rn(md, inv_grid));  // snapped to the grid
+    const int64_t qj = qc[nm + side * k0];  // a padding sentinel beyond either end
+    const float dn = q_to_f(side > 0 ? qj - qn : qn - qj, grid);
+    const float dd = q_to_f(side > 0 ? qj - qo : qo - qj, grid);
     const float dn2 = __fmul_rn(dn, dn), do2 = __fmul_rn(dd, dd);
     const float t = __fsub_rn(pair_energy_h<POT, false>(dn2, H), pair_energy_h<POT, false>(do2, H));
     bool sat = k0 == kSeqSide && (dn2 <= H.rc2 || do2 <= H.rc2);
@@ -221,9 +236,9 @@ __global__ void __launch_bounds__(32)
       float t2 = 0.0f;
       sat = false;
       if (j >= 0 && j < n) {
-        const double xj2 = xc[j];
-        const float dn_2 = (float)(side > 0 ? __dsub_rn(xj2, xn) : __dsub_rn(xn, xj2));
-        const float do_2 = (float)(side > 0 ? __dsub_rn(xj2, xo) : __dsub_rn(xo, xj2));
+        const int64_t qj2 = qc[j];
+        const float dn_2 = q_to_f(side > 0 ? qj2 - qn : qn - qj2, grid);
+        const float do_2 = q_to_f(side > 0 ? qj2 - qo : qo - qj2, grid);
         const float dn22 = __fmul_rn(dn_2, dn_2), do22 = __fmul_rn(do_2, do_2);
         t2 = __fsub_rn(pair_energy_h<POT, false>(dn22, H), pair_energy_h<POT, false>(do22, H));
         sat = k0 == kSeqSide && (dn22 <= H.rc2 || do22 <= H.rc2);
@@ -231,13 +246,13 @@ __global__ void __launch_bounds__(32)
       de = __fadd_rn(de, group_sum<32>(t2, 0xffffffffu));
       chunks += 1;
     }
-    const bool ok = (xn > xc[nm - 1]) && (xn < xc[nm + 1]) && !(fabs(xn) > half);
+    const bool ok = qn > qc[nm - 1] && qn < qc[nm + 1] && qn <= ch.wall_q && qn >= -ch.wall_q;
     const bool acc = ok && ((de <= 0.0f) || (__fmul_rn(de, H.beta) < thr));
     if (acc) {
       e_acc = __dadd_rn(e_acc, (double)de);
       n_acc += 1;
-      __syncwarp();  // every lane has read x[nm] before it changes
-      if (lane == 0) xc[nm] = xn;
+      __syncwarp();  // every lane has read q[nm] before it changes
+      if (lane == 0) qc[nm] = qn;
     }
     __syncwarp();
   }
@@ -286,21 +301,21 @@ __global__ void sweep_stats_kernel(const LargeChain *__restrict__ chains,
 // Fresh energy of each chain from the FP64 positions: FP32 pair terms of the
 // FP64 separations, FP32 per-particle sums, FP64 lane and chain sums.
 __global__ void large_energy_kernel(const LargeChain *__restrict__ chains,
-                                    const double *__restrict__ x, double *__restrict__ e_out,
+                                    const int64_t *__restrict__ q, double *__restrict__ e_out,
                                     uint32_t n_chains) {
   const uint32_t c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   if (c >= n_chains) return;
   const LargeChain ch = chains[c];
   const ChainParams P = domain_params(ch, 0, ch.n);
-  const double *xc = x + ch.x_base;
+  const int64_t *qc = q + ch.x_base;
   const int lane = threadIdx.x & 31;
   const int n = (int)ch.n;
   double u = 0.0;
   for (int i = lane; i < n; i += 32) {
-    const double xi = xc[i];
+    const int64_t qi = qc[i];
     float e = 0.0f;
     for (int j = i + 1; j < n; ++j) {
-      const float d = (float)__dsub_rn(xc[j], xi);
+      const float d = q_to_f(qc[j] - qi, ch.grid);
       const float d2 = __fmul_rn(d, d);
       if (d2 > P.rc2) break;
       e = __fadd_rn(e, pair_energy<false>(d2, P));
@@ -331,14 +346,74 @@ __global__ void rebase_kernel(const LargeChain *__restrict__ chains, LargeState 
   }
 }
 
+// ---- positions: lattice, host values snapped to the grid, checks ---------
+// One block row per chain (blockIdx.y), particles along x.
+
+__global__ void lattice_kernel(const LargeChain *__restrict__ chains, int64_t *__restrict__ q,
+                               uint32_t c0, uint64_t seed, int32_t init, double jitter) {
+  const uint32_t c = c0 + blockIdx.y;
+  const LargeChain ch = chains[c];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - kGhost;
+  if (i >= (int64_t)ch.n + kGhost) return;
+  int64_t v;
+  if (i < 0) {
+    v = -kFarQ;
+  } else if (i >= (int64_t)ch.n) {
+    v = kFarQ;
+  } else {
+    // r_i = ((i + 0.5)/N - 0.5) L (jmmMCState.cpp:559-562), plus the
+    // batched chains' jitter draw
+    double r = __dmul_rn(__dsub_rn(__ddiv_rn((double)i + 0.5, (double)ch.n), 0.5), ch.l);
+    if (init == JMM_INIT_JITTER) {
+      const Words4 w = step_words(seed, (1ull << 63) | (uint64_t)i, c);
+      r = __dadd_rn(r, __dmul_rn(jitter, __dsub_rn(__dmul_rn(2.0, word_to_unit(w.w[0])), 1.0)));
+    }
+    v = __double2ll_rn(__dmul_rn(r, 1.0 / (double)ch.grid));
+    v = v > ch.wall_q ? ch.wall_q : (v < -ch.wall_q ? -ch.wall_q : v);
+  }
+  q[ch.x_base + i] = v;
+}
+
+// Host values (staged in the padded layout) to grid steps; flags values
+// outside the walls.
+__global__ void snap_kernel(const LargeChain *__restrict__ chains, const double *__restrict__ x,
+                            int64_t *__restrict__ q, uint32_t c0, uint32_t *__restrict__ bad) {
+  const LargeChain ch = chains[c0 + blockIdx.y];
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ch.n) return;
+  const double v = __dmul_rn(x[ch.x_base + i], 1.0 / (double)ch.grid);  // exact: 2^k
+  if (!(fabs(v) <= (double)ch.wall_q)) {
+    atomicOr(bad, 1u);
+    return;
+  }
+  q[ch.x_base + i] = __double2ll_rn(v);
+}
+
+// Particles strictly increasing along each chain, else a flag.
+__global__ void order_kernel(const LargeChain *__restrict__ chains, const int64_t *__restrict__ q,
+                             uint32_t c0, uint32_t *__restrict__ bad) {
+  const LargeChain ch = chains[c0 + blockIdx.y];
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (i >= ch.n) return;
+  if (!(q[ch.x_base + i] > q[ch.x_base + i - 1])) atomicOr(bad, 2u);
+}
+
+__global__ void unsnap_kernel(const LargeChain *__restrict__ chains, const int64_t *__restrict__ q,
+                              double *__restrict__ x, uint32_t c0) {
+  const LargeChain ch = chains[c0 + blockIdx.y];
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ch.n) return;
+  x[ch.x_base + i] = __dmul_rn((double)q[ch.x_base + i], (double)ch.grid);
+}
+
 template <int POT>
 void launch_phase(const LargeChain *d_chains, const LargeState *d_states, jmm_chain_result *d_rec,
-                  double *d_x, uint32_t n_chains, uint32_t b, uint32_t phase, uint32_t doms_per_chain,
+                  int64_t *d_q, uint32_t n_chains, uint32_t b, uint32_t phase, uint32_t doms_per_chain,
                   const KernelCfg &kc, cudaStream_t s) {
   const uint64_t warps = (uint64_t)n_chains * doms_per_chain;
   const uint32_t blocks = (uint32_t)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock);
   const size_t smem = (size_t)kWarpsPerBlock * (kRingWords + b + 2 * kGhost) * sizeof(float);
-  domain_kernel<POT><<<blocks, 32 * kWarpsPerBlock, smem, s>>>(d_chains, d_states, d_rec, d_x,
+  domain_kernel<POT><<<blocks, 32 * kWarpsPerBlock, smem, s>>>(d_chains, d_states, d_rec, d_q,
                                                                n_chains, b, phase, doms_per_chain, kc);
 }
 
@@ -353,8 +428,11 @@ struct jmm_large {
   LargeChain *d_chains = nullptr;
   LargeState *d_states = nullptr;
   jmm_chain_result *d_rec = nullptr;  // domain records, then one per chain for the sequential sweep
-  double *d_x = nullptr;
+  int64_t *d_q = nullptr;    // positions in grid steps, padded with sentinels
+  double *d_stage = nullptr; // host-format positions (same layout), allocated on first use
+  uint32_t *d_bad = nullptr; // flags of the position checks
   double *d_e = nullptr;
+  uint32_t max_n = 0;
   cudaStream_t stream = nullptr;
   uint64_t sweeps_since_resum = 0;
   int mode = 0;              // records holding the open changes: 0 domains, 1 sequential
@@ -365,7 +443,9 @@ static void large_free(jmm_large *h) {
   cudaFree(h->d_chains);
   cudaFree(h->d_states);
   cudaFree(h->d_rec);
-  cudaFree(h->d_x);
+  cudaFree(h->d_q);
+  cudaFree(h->d_stage);
+  cudaFree(h->d_bad);
   cudaFree(h->d_e);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -391,11 +471,62 @@ static int32_t seq_base_of(const jmm_large *h, int mode) {
 // FP64 re-summation on stream s: new base energies, open changes folded.
 static int resum(jmm_large *h, cudaStream_t s, bool note) {
   const uint32_t blocks = (h->n_chains + kStatWarps - 1) / kStatWarps;
-  large_energy_kernel<<<blocks, 32 * kStatWarps, 0, s>>>(h->d_chains, h->d_x, h->d_e, h->n_chains);
+  large_energy_kernel<<<blocks, 32 * kStatWarps, 0, s>>>(h->d_chains, h->d_q, h->d_e, h->n_chains);
   rebase_kernel<<<blocks, 32 * kStatWarps, 0, s>>>(h->d_chains, h->d_states, h->d_rec, h->d_e,
                                                    h->n_chains, seq_base_of(h, h->mode), note);
   JMM_CUDA(cudaGetLastError());
   h->sweeps_since_resum = 0;
+  return JMM_OK;
+}
+
+static dim3 chain_grid(const jmm_large *h, uint32_t c0, uint32_t c1, uint32_t extra) {
+  return dim3((h->max_n + extra + 255) / 256, c1 - c0);
+}
+
+// Orders and walls of chains [c0, c1) checked on the device: JMM_OK or
+// JMM_ERR_INVALID with the reason.
+static int check_positions(jmm_large *h, uint32_t c0, uint32_t c1, const char *what) {
+  order_kernel<<<chain_grid(h, c0, c1, 0), 256, 0, h->stream>>>(h->d_chains, h->d_q, c0, h->d_bad);
+  JMM_CUDA(cudaGetLastError());
+  uint32_t bad = 0;
+  JMM_CUDA(cudaMemcpyAsync(&bad, h->d_bad, sizeof(bad), cudaMemcpyDeviceToHost, h->stream));
+  JMM_CUDA(cudaStreamSynchronize(h->stream));
+  if (bad & 1u) return fail(JMM_ERR_INVALID, "%s: a position lies outside the walls", what);
+  if (bad & 2u)
+    return fail(JMM_ERR_INVALID, "%s: positions must increase by at least one grid step", what);
+  return JMM_OK;
+}
+
+// Host positions (compact, chain after chain) of chains [c0, c1) to the
+// device: one copy per chain into the staging buffer, then snapped.
+static int upload_positions(jmm_large *h, const double *x, uint32_t c0, uint32_t c1,
+                            const char *what) {
+  if (!h->d_stage) JMM_CUDA(cudaMalloc((void **)&h->d_stage, h->total * sizeof(double)));
+  JMM_CUDA(cudaMemsetAsync(h->d_bad, 0, sizeof(uint32_t), h->stream));
+  uint64_t src = 0;
+  for (uint32_t k = c0; k < c1; ++k) {
+    const LargeChain &lc = h->host_chains[k];
+    JMM_CUDA(cudaMemcpyAsync(h->d_stage + lc.x_base, x + src, lc.n * sizeof(double),
+                             cudaMemcpyHostToDevice, h->stream));
+    src += lc.n;
+  }
+  snap_kernel<<<chain_grid(h, c0, c1, 0), 256, 0, h->stream>>>(h->d_chains, h->d_stage, h->d_q, c0,
+                                                               h->d_bad);
+  return check_positions(h, c0, c1, what);
+}
+
+static int download_positions(jmm_large *h, double *x, uint32_t c0, uint32_t c1) {
+  if (!h->d_stage) JMM_CUDA(cudaMalloc((void **)&h->d_stage, h->total * sizeof(double)));
+  unsnap_kernel<<<chain_grid(h, c0, c1, 0), 256, 0, h->stream>>>(h->d_chains, h->d_q, h->d_stage, c0);
+  JMM_CUDA(cudaGetLastError());
+  uint64_t dst = 0;
+  for (uint32_t k = c0; k < c1; ++k) {
+    const LargeChain &lc = h->host_chains[k];
+    JMM_CUDA(cudaMemcpyAsync(x + dst, h->d_stage + lc.x_base, lc.n * sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream));
+    dst += lc.n;
+  }
+  JMM_CUDA(cudaStreamSynchronize(h->stream));
   return JMM_OK;
 }
 
@@ -411,25 +542,25 @@ static int enqueue(jmm_large *h, uint64_t n_sweeps, int mode, cudaStream_t s) {
     if (mode == 0) {
       for (uint32_t phase = 0; phase < 2; ++phase) {
         if (h->pots[0])
-          launch_phase<JMM_POT_LJCUT>(h->d_chains, h->d_states, h->d_rec, h->d_x, h->n_chains, h->b,
+          launch_phase<JMM_POT_LJCUT>(h->d_chains, h->d_states, h->d_rec, h->d_q, h->n_chains, h->b,
                                       phase, h->doms_per_chain, kc, s);
         if (h->pots[1])
-          launch_phase<JMM_POT_SOFTSPHERE>(h->d_chains, h->d_states, h->d_rec, h->d_x, h->n_chains,
+          launch_phase<JMM_POT_SOFTSPHERE>(h->d_chains, h->d_states, h->d_rec, h->d_q, h->n_chains,
                                            h->b, phase, h->doms_per_chain, kc, s);
         if (h->pots[2])
-          launch_phase<JMM_POT_GAUSS>(h->d_chains, h->d_states, h->d_rec, h->d_x, h->n_chains, h->b,
+          launch_phase<JMM_POT_GAUSS>(h->d_chains, h->d_states, h->d_rec, h->d_q, h->n_chains, h->b,
                                       phase, h->doms_per_chain, kc, s);
       }
     } else {
       const uint32_t base = h->records;
       if (h->pots[0])
-        sequential_kernel<JMM_POT_LJCUT><<<h->n_chains, 32, 0, s>>>(h->d_chains, h->d_rec, h->d_x,
+        sequential_kernel<JMM_POT_LJCUT><<<h->n_chains, 32, 0, s>>>(h->d_chains, h->d_rec, h->d_q,
                                                                    h->n_chains, base, kc);
       if (h->pots[1])
         sequential_kernel<JMM_POT_SOFTSPHERE><<<h->n_chains, 32, 0, s>>>(h->d_chains, h->d_rec,
-                                                                        h->d_x, h->n_chains, base, kc);
+                                                                        h->d_q, h->n_chains, base, kc);
       if (h->pots[2])
-        sequential_kernel<JMM_POT_GAUSS><<<h->n_chains, 32, 0, s>>>(h->d_chains, h->d_rec, h->d_x,
+        sequential_kernel<JMM_POT_GAUSS><<<h->n_chains, 32, 0, s>>>(h->d_chains, h->d_rec, h->d_q,
                                                                    h->n_chains, base, kc);
     }
     sweep_stats_kernel<<<sblocks, 32 * kStatWarps, 0, s>>>(h->d_chains, h->d_states, h->d_rec,
@@ -447,6 +578,7 @@ extern "C" int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_des
                                 uint32_t n_chains, uint32_t domain_size, jmm_large **out) {
   clear_error();
   JMM_CHECK_ARG(cfg && chains && out && n_chains > 0, "null argument or no chains");
+  JMM_CHECK_ARG(n_chains <= 65535, "at most 65535 chains");
   *out = nullptr;
   JMM_CHECK_ARG(domain_size >= 2 * kGhost && domain_size <= 8192,
                 "domain_size must be in [32, 8192]");
@@ -491,10 +623,23 @@ extern "C" int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_des
     lc.beta = (float)(1.0 / c.t);
     lc.two_max_step = (float)(2.0 * c.max_step);
     lc.l = c.l0;
+    // grid step 2^-k: a domain with both halos spans about (B + 2 kGhost) L/N,
+    // kept below 2^23 steps (half the exact FP32 frame on either side)
+    const double span = (domain_size + 2.0 * kGhost) * c.l0 / c.n;
+    const int kexp = std::min(40, (int)floor(log2(8388608.0 / span)));
+    if (kexp < 8) {
+      large_free(h);
+      return fail(JMM_ERR_INVALID,
+                  "jmm_large_create: chain %u: a domain spans %.0f sigma, more than 2^15 at a grid "
+                  "of 2^-8: lower domain_size", k, span);
+    }
+    lc.grid = ldexpf(1.0f, -kexp);
+    lc.wall_q = (int64_t)floor(0.5 * c.l0 * ldexp(1.0, kexp));
     h->host_chains.push_back(lc);
     h->pots[c.potential == JMM_POT_LJCUT ? 0 : (c.potential == JMM_POT_SOFTSPHERE ? 1 : 2)] = true;
     rec += lc.n_dom;
     max_dom = std::max(max_dom, lc.n_dom);
+    h->max_n = std::max(h->max_n, c.n);
     off += (uint64_t)c.n + 2 * kGhost;
   }
   if (rec + n_chains > 0x7fffffffull) {
@@ -510,30 +655,13 @@ extern "C" int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_des
   if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_chains, n_chains * sizeof(LargeChain));
   if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_states, n_chains * sizeof(LargeState));
   if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_rec, n_rec * sizeof(jmm_chain_result));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_x, off * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_q, off * sizeof(int64_t));
   if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_e, n_chains * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_bad, sizeof(uint32_t));
   if (e != cudaSuccess) {
     const int rc = cuda_status(e, "jmm_large_create allocation", __FILE__, __LINE__);
     large_free(h);
     return rc;
-  }
-  // lattice (plus jitter, the batched chains' draw), far sentinels in the padding
-  std::vector<double> x(off, 0.0);
-  for (uint32_t k = 0; k < n_chains; ++k) {
-    const jmm_chain_desc &c = chains[k];
-    double *xc = x.data() + h->host_chains[k].x_base;
-    for (int g = 1; g <= kGhost; ++g) {
-      xc[-g] = -(double)kFar;
-      xc[c.n - 1 + g] = (double)kFar;
-    }
-    for (uint32_t i = 0; i < c.n; ++i) {
-      double r = ((i + 0.5) / c.n - 0.5) * c.l0;
-      if (cfg->init == JMM_INIT_JITTER) {
-        const Words4 w = step_words(cfg->seed, (1ull << 63) | i, k);
-        r += cfg->jitter * (2.0 * word_to_unit(w.w[0]) - 1.0);
-      }
-      xc[i] = r;
-    }
   }
   std::vector<jmm_chain_result> recs(n_rec);
   memset(recs.data(), 0, recs.size() * sizeof(jmm_chain_result));
@@ -541,7 +669,6 @@ extern "C" int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_des
   memset(st.data(), 0, st.size() * sizeof(LargeState));
   e = cudaMemcpy(h->d_chains, h->host_chains.data(), n_chains * sizeof(LargeChain),
                  cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(h->d_x, x.data(), off * sizeof(double), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(h->d_rec, recs.data(), n_rec * sizeof(jmm_chain_result), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
@@ -562,7 +689,15 @@ extern "C" int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_des
     large_free(h);
     return rc;
   }
-  int rc = resum(h, h->stream, false);  // initial energies
+  // lattice (plus jitter, the batched chains' draw) on the grid, far
+  // sentinels in the padding
+  int rc = JMM_OK;
+  lattice_kernel<<<chain_grid(h, 0, n_chains, 2 * kGhost), 256, 0, h->stream>>>(
+      h->d_chains, h->d_q, 0, cfg->seed, cfg->init, cfg->jitter);
+  e = cudaMemsetAsync(h->d_bad, 0, sizeof(uint32_t), h->stream);
+  if (e != cudaSuccess) rc = cuda_status(e, "jmm_large_create lattice", __FILE__, __LINE__);
+  if (rc == JMM_OK) rc = check_positions(h, 0, n_chains, "jmm_large_create (initial jitter)");
+  if (rc == JMM_OK) rc = resum(h, h->stream, false);  // initial energies
   if (rc == JMM_OK) {
     e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) rc = cuda_status(e, "jmm_large_create energies", __FILE__, __LINE__);
@@ -629,6 +764,7 @@ extern "C" int jmm_large_results(jmm_large *h, jmm_large_result *out, uint32_t n
     r.sum_e = st[k].sum_e;
     r.sum_e2 = st[k].sum_e2;
     r.max_drift = st[k].max_drift;
+    r.grid = (double)lc.grid;
   }
   return JMM_OK;
 }
@@ -656,7 +792,7 @@ extern "C" int jmm_large_energies(jmm_large *h, double *e, uint32_t n_chains) {
   JMM_CHECK_ARG(n_chains == h->n_chains, "n_chains does not match");
   JMM_CUDA(cudaDeviceSynchronize());
   const uint32_t blocks = (h->n_chains + kStatWarps - 1) / kStatWarps;
-  large_energy_kernel<<<blocks, 32 * kStatWarps, 0, h->stream>>>(h->d_chains, h->d_x, h->d_e,
+  large_energy_kernel<<<blocks, 32 * kStatWarps, 0, h->stream>>>(h->d_chains, h->d_q, h->d_e,
                                                                  h->n_chains);
   JMM_CUDA(cudaGetLastError());
   JMM_CUDA(cudaStreamSynchronize(h->stream));
@@ -670,9 +806,7 @@ extern "C" int jmm_large_get_positions(jmm_large *h, uint32_t chain, double *x, 
   JMM_CHECK_ARG(chain < h->n_chains, "chain index out of range");
   JMM_CHECK_ARG(n == h->host_chains[chain].n, "N does not match the chain");
   JMM_CUDA(cudaDeviceSynchronize());
-  JMM_CUDA(cudaMemcpy(x, h->d_x + h->host_chains[chain].x_base, n * sizeof(double),
-                      cudaMemcpyDeviceToHost));
-  return JMM_OK;
+  return download_positions(h, x, chain, chain + 1);
 }
 
 extern "C" int jmm_large_set_positions(jmm_large *h, uint32_t chain, const double *x, uint64_t n) {
@@ -680,21 +814,36 @@ extern "C" int jmm_large_set_positions(jmm_large *h, uint32_t chain, const doubl
   JMM_CHECK_ARG(h && x, "null argument");
   JMM_CHECK_ARG(chain < h->n_chains, "chain index out of range");
   JMM_CHECK_ARG(n == h->host_chains[chain].n, "N does not match the chain");
-  const double half = 0.5 * h->host_chains[chain].l;
-  for (uint64_t i = 0; i < n; ++i) {
-    if (!(fabs(x[i]) <= half))
-      return fail(JMM_ERR_INVALID, "jmm_large_set_positions: x[%llu] outside the walls",
-                  (unsigned long long)i);
-    if (i > 0 && !(x[i] > x[i - 1]))
-      return fail(JMM_ERR_INVALID, "jmm_large_set_positions: positions must increase (x[%llu])",
-                  (unsigned long long)i);
-  }
   JMM_CUDA(cudaDeviceSynchronize());
-  JMM_CUDA(cudaMemcpy(h->d_x + h->host_chains[chain].x_base, x, n * sizeof(double),
-                      cudaMemcpyHostToDevice));
+  std::vector<int64_t> keep(n);  // the chain's positions, restored if the new ones are refused
+  const LargeChain &lc = h->host_chains[chain];
+  JMM_CUDA(cudaMemcpy(keep.data(), h->d_q + lc.x_base, n * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  int rc = upload_positions(h, x, chain, chain + 1, "jmm_large_set_positions");
+  if (rc) {
+    JMM_CUDA(cudaMemcpy(h->d_q + lc.x_base, keep.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice));
+    return rc;
+  }
   // fresh base energies for every chain; open changes folded
-  const int rc = resum(h, h->stream, false);
+  rc = resum(h, h->stream, false);
   if (rc) return rc;
   JMM_CUDA(cudaStreamSynchronize(h->stream));
   return JMM_OK;
+}
+
+extern "C" int jmm_large_run_host(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                                  uint32_t n_chains, uint32_t domain_size, int32_t mode,
+                                  const double *x_in, uint64_t n_sweeps, jmm_large_result *results,
+                                  double *x_out) {
+  jmm_large *h = nullptr;
+  int rc = jmm_large_create(cfg, chains, n_chains, domain_size, &h);
+  if (rc) return rc;
+  if (x_in) {
+    rc = upload_positions(h, x_in, 0, n_chains, "jmm_large_run_host");
+    if (rc == JMM_OK) rc = resum(h, h->stream, false);
+  }
+  if (rc == JMM_OK) rc = jmm_large_run(h, n_sweeps, mode);
+  if (rc == JMM_OK && results) rc = jmm_large_results(h, results, n_chains);
+  if (rc == JMM_OK && x_out) rc = download_positions(h, x_out, 0, n_chains);
+  large_free(h);
+  return rc;
 }

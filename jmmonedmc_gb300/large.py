@@ -26,6 +26,9 @@ _native.register({
     "jmm_large_get_positions": [C.c_void_p, C.c_uint32, P(C.c_double), C.c_uint64],
     "jmm_large_set_positions": [C.c_void_p, C.c_uint32, P(C.c_double), C.c_uint64],
     "jmm_large_destroy": [C.c_void_p],
+    "jmm_large_run_host": [P(abi.BatchConfig), P(abi.ChainDesc), C.c_uint32, C.c_uint32,
+                           C.c_int32, P(C.c_double), C.c_uint64, P(abi.LargeResult),
+                           P(C.c_double)],
 })
 
 MODES = {"domains": abi.JMM_LARGE_DOMAINS, "sequential": abi.JMM_LARGE_SEQUENTIAL}
@@ -94,3 +97,22 @@ class LargeChains:
         x = np.ascontiguousarray(x, dtype=np.float64)
         _native.call("jmm_large_set_positions", self._h, k, x.ctypes.data_as(P(C.c_double)),
                      x.size)
+
+
+def run_host(config, chains, n_sweeps, domain_size=256, mode="domains", x_in=None, x_out=None):
+    """jmm_large_run_host: positions (float64, chain after chain, or None for
+    the configured lattice) in, results and final positions out.  x_out may
+    be a caller-owned float64 array (pinned memory, for instance)."""
+    chains = list(chains)
+    arr = (abi.ChainDesc * len(chains))(*chains)
+    n_tot = sum(int(c.n) for c in chains)
+    if x_in is not None:
+        x_in = np.ascontiguousarray(x_in, dtype=np.float64)
+        assert x_in.size == n_tot
+    if x_out is None:
+        x_out = np.empty(n_tot, dtype=np.float64)
+    res = (abi.LargeResult * len(chains))()
+    _native.call("jmm_large_run_host", C.byref(config), arr, len(chains), int(domain_size),
+                 MODES[mode], x_in.ctypes.data_as(P(C.c_double)) if x_in is not None else None,
+                 int(n_sweeps), res, x_out.ctypes.data_as(P(C.c_double)))
+    return np.frombuffer(res, dtype=np.dtype(abi.LARGE_RESULT_DTYPE)).copy(), x_out
