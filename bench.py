@@ -437,6 +437,12 @@ def run_large(args, rank, world, local_rank):
     h2d = n_tot * 8 + args.chains * C.sizeof(chains[0]) + 64
     d2h = n_tot * 8 + args.chains * 120
 
+    traffic = None
+    prof = os.path.join(REPO, "profiles", "domain_kernel_large_chains.md")
+    if os.path.exists(prof):
+        m = re.search(r"dram_bytes_per_particle_phase:\s*([0-9.eE+-]+)", open(prof).read())
+        if m:
+            traffic = float(m.group(1)) * args.chains * args.n / 2
     launches_per_step = 3 * S
     launch_ms = total_ms / (args.steps * 2 * S)  # the two domain launches of a sweep dominate
     pairs_per_launch = pairs / (args.steps * 2 * S)
@@ -462,7 +468,7 @@ def run_large(args, rank, world, local_rank):
             "peak": fp32_peak.value,
             "unit": "TFLOP/s",
             "frac": achieved / fp32_peak.value,
-            "traffic": None,
+            "traffic": traffic,
             "peak_source": "measured live by jmm_measure_peaks (FP32 FMA kernel; "
                            "MEASURED_PEAKS.json holds no FP32 figure)",
             "pair_evals_per_launch": pairs_per_launch,

@@ -120,6 +120,8 @@ def test_fluctuation_gradient_of_energy_nvt(gpu):
     fd = (up["sum_u"] / up["samples"] - dn["sum_u"] / dn["samples"]) / (2 * delta)
     diff = est.mean() - fd.mean()
     sem = np.sqrt(est.var(ddof=1) / len(est) + fd.var(ddof=1) / len(fd))
+    print(f"d<U>/deps: fluctuation {est.mean():.4f}, finite difference {fd.mean():.4f}, "
+          f"standard error {sem:.4f}")
     assert abs(diff) < 4 * sem + 0.02 * abs(fd.mean()), (est.mean(), fd.mean(), sem)
 
 
@@ -134,4 +136,6 @@ def test_fluctuation_gradient_of_density_npt(gpu):
     fd = (up["sum_rho"] / up["samples"] - dn["sum_rho"] / dn["samples"]) / (2 * delta)
     diff = est.mean() - fd.mean()
     sem = np.sqrt(est.var(ddof=1) / len(est) + fd.var(ddof=1) / len(fd))
+    print(f"d<rho>/dsigma: fluctuation {est.mean():.5f}, finite difference {fd.mean():.5f}, "
+          f"standard error {sem:.5f}")
     assert abs(diff) < 4 * sem + 0.02 * abs(fd.mean()), (est.mean(), fd.mean(), sem)
