@@ -18,3 +18,18 @@ _COLUMN_ORDER = (4, 5, 2, 3, 6, 0, 1, 7, 8, 9, 10, 11)
 def thermo_line(sn, acc, ss):
     means = [acc[k] / ss for k in _COLUMN_ORDER]
     return f"{sn}" + "".join("\t%.8G" % m for m in means) + "\n"
+
+
+def rho_line(sn, counts, ns, rbw):
+    """One line of rho.dat.mcs (printRho, src/jmmMCState.cpp:1021-1037): the
+    step, then per bin the accumulated count / ns / rbw with %.8G; ns is the
+    steps since the last print as an unsigned 64-bit difference."""
+    ns = float(ns)
+    return f"{sn}" + "".join(" %.8G" % (float(c) / ns / rbw) for c in counts) + "\n"
+
+
+def g_line(sn, counts, ns, gsw, gbw):
+    """One line of g<k>.dat.mcs (printG, src/jmmMCState.cpp:1042-1061): per
+    separation bin of slice k, count / ns / gsw / gbw with %.8G."""
+    ns = float(ns)
+    return f"{sn}" + "".join(" %.8G" % (float(c) / ns / gsw / gbw) for c in counts) + "\n"

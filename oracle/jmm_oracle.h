@@ -28,6 +28,12 @@ int jmmo_plain_get_state(jmmo_plain *h, jmm_state *out);
 int jmmo_plain_get_positions(jmmo_plain *h, double *r, uint64_t n);
 int jmmo_plain_get_separations(jmmo_plain *h, double *rij, uint64_t n_pairs);
 void jmmo_plain_destroy(jmmo_plain *h);
+int jmmo_plain_histograms(jmmo_plain *h, uint64_t rhonb, double rbw, int32_t gns, double gsw,
+                          uint64_t gnb, double gbw);
+int jmmo_plain_take_rho(jmmo_plain *h, int32_t *out, uint64_t rhonb);
+int jmmo_plain_take_g(jmmo_plain *h, int32_t *out, uint64_t n);
+int jmmo_plain_hist_counts(jmmo_plain *h, int32_t *rho, uint64_t rhonb, int32_t *g,
+                           uint64_t ng);
 
 void jmmo_philox_raw(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 void jmmo_step_words_export(uint64_t seed, uint64_t block, uint32_t chain, uint32_t out[4]);

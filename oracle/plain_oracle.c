@@ -16,6 +16,8 @@
  *   updateThermo               src/jmmMCState.cpp:1941-1961
  *   ECheck                     src/jmmMCState.cpp:1965-2095
  *   fav                        src/jmmMCState.cpp:2161-2293
+ *   fgrho / ugrho              src/jmmMCState.cpp:1069-1149
+ *   qagrho                     src/jmmMCState.cpp:2297-2384
  *
  * Every FP64 expression keeps the reference's operand order; the file is
  * compiled with -ffp-contract=off so no multiply-add is fused.
@@ -50,6 +52,13 @@ struct jmmo_plain {
   double *q;            /* 9*N*N stored pair quantities            */
   double *rij_trial;    /* N*N                                      */
   double *q_trial;      /* 9*N*N                                    */
+  /* rho(x) and g(x) histograms: current counts (rhol, gl) and their sums
+   * since the last take (rhoA, gA), int as in the reference, g slice-major */
+  int hist_on;
+  uint64_t rhonb, gnb;
+  int32_t gns;
+  double rbw, gsw, gbw;
+  int32_t *rhol, *rhoA, *gl, *gA;
 };
 
 /* ---- pair potentials ---------------------------------------------------- */
@@ -197,6 +206,10 @@ int jmmo_plain_set_config(jmmo_plain *h, const double *r, uint64_t n, double l,
 
 void jmmo_plain_destroy(jmmo_plain *h) {
   if (!h) return;
+  free(h->rhol);
+  free(h->rhoA);
+  free(h->gl);
+  free(h->gA);
   free(h->r);
   free(h->r_trial);
   free(h->rij);
@@ -204,6 +217,125 @@ void jmmo_plain_destroy(jmmo_plain *h) {
   free(h->q);
   free(h->q_trial);
   free(h);
+}
+
+/* ---- rho(x) and g(x) histograms ------------------------------------------ */
+
+/* Counts are int in the reference; sums wrap as its int arithmetic does on
+ * the platforms it runs on. */
+static int32_t wrap_add(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
+
+static long rho_bin(const jmmo_plain *h, double x) {
+  return (long)floor(x / h->rbw + h->rhonb / 2.0);
+}
+
+static long slice_of(const jmmo_plain *h, double x) {
+  return (long)floor(x / h->gsw + h->gns / 2.0);
+}
+
+/* fgrho, src/jmmMCState.cpp:1069-1127: counts of the current positions
+ * (density) and of the stored separations (g(x), each pair in the slices of
+ * both particles).  A negative separation (particles that passed each
+ * other) gives a negative bin, which the reference writes out of bounds;
+ * here it is not counted. */
+static void fgrho(jmmo_plain *h) {
+  uint64_t n = h->n;
+  memset(h->rhol, 0, h->rhonb * sizeof(int32_t));
+  for (uint64_t i = 0; i < n; ++i) {
+    long rb = rho_bin(h, h->r[i]);
+    if (rb >= 0 && rb < (long)h->rhonb) h->rhol[rb]++;
+  }
+  memset(h->gl, 0, (uint64_t)h->gns * h->gnb * sizeof(int32_t));
+  for (uint64_t i = 0; i < n; ++i) {
+    for (uint64_t j = i + 1; j < n; ++j) {
+      long gs1 = slice_of(h, h->r[i]);
+      long gs2 = slice_of(h, h->r[j]);
+      long gb = (long)floor(h->rij[i * n + j] / h->gbw);
+      if (gb >= 0 && gb < (long)h->gnb) {
+        if (gs1 >= 0 && gs1 < h->gns) h->gl[gs1 * h->gnb + gb]++;
+        if (gs2 >= 0 && gs2 < h->gns) h->gl[gs2 * h->gnb + gb]++;
+      }
+    }
+  }
+}
+
+/* ugrho, src/jmmMCState.cpp:1131-1149 */
+static void ugrho(jmmo_plain *h) {
+  for (uint64_t b = 0; b < h->rhonb; ++b) h->rhoA[b] = wrap_add(h->rhoA[b], h->rhol[b]);
+  for (uint64_t b = 0; b < (uint64_t)h->gns * h->gnb; ++b) h->gA[b] = wrap_add(h->gA[b], h->gl[b]);
+}
+
+/* qagrho, src/jmmMCState.cpp:2297-2384: particle nm moved by md (r[nm] is
+ * the new position; the old one is formed as r[nm] - md). */
+static void qagrho(jmmo_plain *h, uint64_t nm, double md) {
+  uint64_t n = h->n;
+  long rb1 = rho_bin(h, h->r[nm] - md);
+  long rb2 = rho_bin(h, h->r[nm]);
+  if (rb1 >= 0 && rb1 < (long)h->rhonb) h->rhol[rb1]--;
+  if (rb2 >= 0 && rb2 < (long)h->rhonb) h->rhol[rb2]++;
+  long gs11 = slice_of(h, h->r[nm] - md);
+  long gs12 = slice_of(h, h->r[nm]);
+  int v11 = gs11 >= 0 && gs11 < h->gns, v12 = gs12 >= 0 && gs12 < h->gns;
+  for (uint64_t i = 0; i < n; ++i) {
+    if (i == nm) continue;
+    long gs2 = slice_of(h, h->r[i]);
+    int v2 = gs2 >= 0 && gs2 < h->gns;
+    long gb1 = (long)(unsigned long)floor(fabs(h->r[nm] - md - h->r[i]) / h->gbw);
+    long gb2 = (long)(unsigned long)floor(fabs(h->r[nm] - h->r[i]) / h->gbw);
+    int vb1 = gb1 >= 0 && gb1 < (long)h->gnb, vb2 = gb2 >= 0 && gb2 < (long)h->gnb;
+    if (v11 && vb1) h->gl[gs11 * h->gnb + gb1]--;
+    if (v12 && vb2) h->gl[gs12 * h->gnb + gb2]++;
+    if (v2 && vb1) h->gl[gs2 * h->gnb + gb1]--;
+    if (v2 && vb2) h->gl[gs2 * h->gnb + gb2]++;
+  }
+}
+
+int jmmo_plain_histograms(jmmo_plain *h, uint64_t rhonb, double rbw, int32_t gns, double gsw,
+                          uint64_t gnb, double gbw) {
+  if (!h || rhonb < 1 || gns < 1 || gnb < 1 || !(rbw > 0) || !(gsw > 0) || !(gbw > 0))
+    return JMM_ERR_INVALID;
+  free(h->rhol);
+  free(h->rhoA);
+  free(h->gl);
+  free(h->gA);
+  h->rhonb = rhonb;
+  h->rbw = rbw;
+  h->gns = gns;
+  h->gsw = gsw;
+  h->gnb = gnb;
+  h->gbw = gbw;
+  h->rhol = (int32_t *)calloc(rhonb, sizeof(int32_t));
+  h->rhoA = (int32_t *)calloc(rhonb, sizeof(int32_t));
+  h->gl = (int32_t *)calloc((uint64_t)gns * gnb, sizeof(int32_t));
+  h->gA = (int32_t *)calloc((uint64_t)gns * gnb, sizeof(int32_t));
+  if (!h->rhol || !h->rhoA || !h->gl || !h->gA) return JMM_ERR_NOMEM;
+  h->hist_on = 1;
+  fgrho(h); /* set-up: current counts, accumulated once (jmmMCState.cpp:773-776) */
+  ugrho(h);
+  return JMM_OK;
+}
+
+int jmmo_plain_take_rho(jmmo_plain *h, int32_t *out, uint64_t rhonb) {
+  if (!h->hist_on || rhonb != h->rhonb) return JMM_ERR_INVALID;
+  memcpy(out, h->rhoA, rhonb * sizeof(int32_t));
+  memset(h->rhoA, 0, rhonb * sizeof(int32_t));
+  return JMM_OK;
+}
+
+int jmmo_plain_take_g(jmmo_plain *h, int32_t *out, uint64_t n) {
+  if (!h->hist_on || n != (uint64_t)h->gns * h->gnb) return JMM_ERR_INVALID;
+  memcpy(out, h->gA, n * sizeof(int32_t));
+  memset(h->gA, 0, n * sizeof(int32_t));
+  return JMM_OK;
+}
+
+int jmmo_plain_hist_counts(jmmo_plain *h, int32_t *rho, uint64_t rhonb, int32_t *g,
+                           uint64_t ng) {
+  if (!h->hist_on || rhonb != h->rhonb || ng != (uint64_t)h->gns * h->gnb)
+    return JMM_ERR_INVALID;
+  memcpy(rho, h->rhol, rhonb * sizeof(int32_t));
+  memcpy(g, h->gl, ng * sizeof(int32_t));
+  return JMM_OK;
 }
 
 /* ---- moves -------------------------------------------------------------- */
@@ -275,9 +407,10 @@ static void set_record(jmm_step_record *rec, const jmmo_plain *h, uint64_t nm, d
   rec->outcome = outcome;
 }
 
-/* qad2, src/jmmMCState.cpp:1160-1464 */
-static int qad2(jmmo_plain *h, uint64_t nm, double rn, const jmm_draw *rp,
-                double *ran_out, double *bf_out) {
+/* qad2, src/jmmMCState.cpp:1160-1464 (the histogram updates of :1431 and
+ * :1453 in qad2 below) */
+static int qad2_move(jmmo_plain *h, uint64_t nm, double rn, const jmm_draw *rp,
+                     double *ran_out, double *bf_out) {
   uint64_t n = h->n, nn = n * n;
   double md = (rn - 0.5) * 2 * h->max_step;
   h->r_trial[nm] = h->r[nm] + md;
@@ -327,10 +460,20 @@ static int qad2(jmmo_plain *h, uint64_t nm, double rn, const jmm_draw *rp,
     h->r[nm] = h->r_trial[nm];
     for (uint64_t i = 0; i < nm; ++i) commit_pair(h, i * n + nm);
     for (uint64_t i = nm + 1; i < n; ++i) commit_pair(h, nm * n + i);
+    if (h->hist_on) qagrho(h, nm, md);
     return JMM_OUT_ACCEPT;
   }
   h->d_acc[1]++;
   return JMM_OUT_REJECT;
+}
+
+/* qad2 accumulates the histograms once whatever the outcome, the wall
+ * rejection included (ugrho at src/jmmMCState.cpp:1453). */
+static int qad2(jmmo_plain *h, uint64_t nm, double rn, const jmm_draw *rp,
+                double *ran_out, double *bf_out) {
+  int outcome = qad2_move(h, nm, rn, rp, ran_out, bf_out);
+  if (h->hist_on) ugrho(h);
+  return outcome;
 }
 
 /* fav, src/jmmMCState.cpp:2161-2293 */
@@ -425,9 +568,14 @@ static int qav_lj(jmmo_plain *h, double rn, const jmm_draw *rp, double *ran_out,
         for (int k = 0; k < 9; ++k) h->q[k * nn + ind] = phi[k];
       }
     }
+    if (h->hist_on) { /* fgrho, then ugrho (src/jmmMCState.cpp:1717, :1726) */
+      fgrho(h);
+      ugrho(h);
+    }
     return JMM_OUT_ACCEPT;
   }
   h->v_acc[1]++;
+  if (h->hist_on) ugrho(h);
   return JMM_OUT_REJECT;
 }
 

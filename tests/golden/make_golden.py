@@ -34,10 +34,13 @@ REF_STEP_DTYPE = np.dtype([
 
 # keyword -> value; every keyword is written because the reference leaves
 # omitted ones uninitialised (src/readInput.cpp:38-57)
+# histograms: 60 density bins of 2 sigma and 4 slices of 30 sigma, each with
+# 20 separation bins of 0.2 sigma (x in +-60: the N = 256 box reaches beyond,
+# so the range checks are exercised), printed every 250 / 400 steps
 BASE = dict(ENSEMBLE="NLT", N=64, P=1.0, L=106.66666666666667, T=1.0,
             NUMSTEPS=3000, POT="LJcut 3.0", NBN=-1, MAXSTEP=0.3, MAXDV=0.5,
-            CPI=1000, TPI=500, RBW=0.1, RHONB=10, RHOPI=1000000000, GSW=200.0,
-            GNS=1, GBW=0.1, GNB=10, GPI=1000000000, SEED=1, ENGCHECK=500,
+            CPI=1000, TPI=500, RBW=2.0, RHONB=60, RHOPI=250, GSW=30.0,
+            GNS=4, GBW=0.2, GNB=20, GPI=400, SEED=1, ENGCHECK=500,
             DADJ=10**18, VADJ=10**18)
 
 CASES = {
@@ -94,7 +97,9 @@ def run_case(name, overrides):
         fin = np.fromfile(os.path.join(tmp, "final.bin"), dtype="<f8")[1:]
         r_final, thermo = fin[:n], fin[n:n + 12]
         files = {}
-        for fn in ("thermo.dat.mcs", "config.dat.mcs"):
+        names = ["thermo.dat.mcs", "config.dat.mcs", "rho.dat.mcs"]
+        names += [f"g{k}.dat.mcs" for k in range(kw["GNS"])]
+        for fn in names:
             with open(os.path.join(tmp, fn)) as f:
                 files[fn] = f.read()
     outcome = np.zeros(len(steps), dtype=np.int8)
@@ -114,6 +119,8 @@ def run_case(name, overrides):
         r_final=r_final, thermo_final=thermo,
         thermo_file=np.array(files["thermo.dat.mcs"]),
         config_file=np.array(files["config.dat.mcs"]),
+        rho_file=np.array(files["rho.dat.mcs"]),
+        g_files=np.array([files[f"g{k}.dat.mcs"] for k in range(kw["GNS"])]),
         stdout_tail=np.array("\n".join(out.stdout.splitlines()[-4:])),
     )
     return dict(name=name, input=kw, steps=len(steps) - 1)

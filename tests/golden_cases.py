@@ -30,20 +30,31 @@ def load_case(name):
     return kw, inputfile.to_params(kw), data
 
 
-def run_like_driver(chain, kw):
-    """Returns (per-step log, thermo file text)."""
-    tpi = kw["TPI"]
+def run_like_driver(chain, kw, histograms=False):
+    """Returns (per-step log, thermo file text), and with histograms=True
+    also {file name: text} of rho.dat.mcs and g<k>.dat.mcs (the histograms
+    are set up from the created chain, as setupMCS does before fad)."""
+    tpi, rhopi, gpi = kw["TPI"], kw["RHOPI"], kw["GPI"]
     nsteps = kw["NUMSTEPS"]
+    files = {}
+    if histograms:
+        chain.histograms(kw["RHONB"], kw["RBW"], kw["GNS"], kw["GSW"], kw["GNB"], kw["GBW"])
     chain.fad(0, 0.5)
     chain.update_thermo()
     st = chain.state()
-    text = [thermo.HEADER, thermo.thermo_line(0, list(st.thermo), (0 - U64) % (1 << 64))]
+    first = (0 - U64) % (1 << 64)  # the reference's "last print" starts at -1
+    text = [thermo.HEADER, thermo.thermo_line(0, list(st.thermo), first)]
     chain.reset_thermo()
-    sltp = 0
+    if histograms:
+        rho = [thermo.rho_line(0, chain.take_rho(), first, kw["RBW"])]
+        gtx = [[thermo.g_line(0, row, first, kw["GSW"], kw["GBW"])] for row in chain.take_g()]
+    sltp = slrho = slg = 0
     logs = [None]
     sn = 0
     while sn < nsteps:
         nxt = min(nsteps, (sn // tpi + 1) * tpi)
+        if histograms:
+            nxt = min(nxt, (sn // rhopi + 1) * rhopi, (sn // gpi + 1) * gpi)
         logs.append(chain.steps(nxt - sn, log=True))
         sn = nxt
         if sn % tpi == 0:
@@ -51,7 +62,27 @@ def run_like_driver(chain, kw):
             text.append(thermo.thermo_line(sn, list(st.thermo), sn - sltp))
             chain.reset_thermo()
             sltp = sn
+        if histograms and sn % rhopi == 0:
+            rho.append(thermo.rho_line(sn, chain.take_rho(), sn - slrho, kw["RBW"]))
+            slrho = sn
+        if histograms and sn % gpi == 0:
+            for k, row in enumerate(chain.take_g()):
+                gtx[k].append(thermo.g_line(sn, row, sn - slg, kw["GSW"], kw["GBW"]))
+            slg = sn
+    if histograms:
+        files["rho.dat.mcs"] = "".join(rho)
+        for k, lines in enumerate(gtx):
+            files[f"g{k}.dat.mcs"] = "".join(lines)
+        return np.concatenate(logs[1:]), "".join(text), files
     return np.concatenate(logs[1:]), "".join(text)
+
+
+def reference_histogram_files(kw, ref):
+    """{file name: text} of the reference's rho.dat.mcs and g<k>.dat.mcs."""
+    out = {"rho.dat.mcs": str(ref["rho_file"])}
+    for k in range(kw["GNS"]):
+        out[f"g{k}.dat.mcs"] = str(ref["g_files"][k])
+    return out
 
 
 def bits(a):

@@ -32,6 +32,10 @@ SIGS = {
     "jmmo_plain_get_positions": ([vp, P(dbl), u64], C.c_int),
     "jmmo_plain_get_separations": ([vp, P(dbl), u64], C.c_int),
     "jmmo_plain_destroy": ([vp], None),
+    "jmmo_plain_histograms": ([vp, u64, dbl, i32, dbl, u64, dbl], C.c_int),
+    "jmmo_plain_take_rho": ([vp, P(i32), u64], C.c_int),
+    "jmmo_plain_take_g": ([vp, P(i32), u64], C.c_int),
+    "jmmo_plain_hist_counts": ([vp, P(i32), u64, P(i32), u64], C.c_int),
     "jmmo_philox_raw": ([P(u32), P(u32), P(u32)], None),
     "jmmo_step_words_export": ([u64, u64, u32, P(u32)], None),
 }
@@ -149,6 +153,30 @@ class OraclePlain:
         _ok(self.lib.jmmo_plain_get_separations(self._h, rij.ctypes.data_as(P(dbl)), m),
             "get_separations")
         return rij
+
+    def histograms(self, rhonb, rbw, gns, gsw, gnb, gbw):
+        self._hist = (int(rhonb), int(gns), int(gnb))
+        _ok(self.lib.jmmo_plain_histograms(self._h, rhonb, rbw, gns, gsw, gnb, gbw), "histograms")
+
+    def take_rho(self):
+        out = np.empty(self._hist[0], dtype=np.int32)
+        _ok(self.lib.jmmo_plain_take_rho(self._h, out.ctypes.data_as(P(i32)), out.size),
+            "take_rho")
+        return out
+
+    def take_g(self):
+        rhonb, gns, gnb = self._hist
+        out = np.empty(gns * gnb, dtype=np.int32)
+        _ok(self.lib.jmmo_plain_take_g(self._h, out.ctypes.data_as(P(i32)), out.size), "take_g")
+        return out.reshape(gns, gnb)
+
+    def hist_counts(self):
+        rhonb, gns, gnb = self._hist
+        rho = np.empty(rhonb, dtype=np.int32)
+        g = np.empty(gns * gnb, dtype=np.int32)
+        _ok(self.lib.jmmo_plain_hist_counts(self._h, rho.ctypes.data_as(P(i32)), rhonb,
+                                            g.ctypes.data_as(P(i32)), g.size), "hist_counts")
+        return rho, g.reshape(gns, gnb)
 
 
 

@@ -44,6 +44,20 @@ def test_oracle_replays_reference(name):
         assert ours == theirs
 
 
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_histogram_files_equal_reference(name):
+    """fgrho/ugrho/qagrho and printRho/printG: the rho.dat.mcs and g<k>.dat.mcs
+    text equals the reference's, byte for byte (negative g counts, which the
+    reference's stale counts after a fav volume move produce, included)."""
+    kw, params, ref = gc.load_case(name)
+    chain = oracle_lib.OraclePlain(params)
+    _, _, files = gc.run_like_driver(chain, kw, histograms=True)
+    theirs = gc.reference_histogram_files(kw, ref)
+    assert sorted(files) == sorted(theirs)
+    for fn, text in theirs.items():
+        assert files[fn] == text, fn
+
+
 def test_golden_step_zero_energy():
     """fad(0, 0.5) at set-up gives the full FP64 pair sum (src/Main.cpp:66-68)."""
     kw, params, ref = gc.load_case("nlt64_ljcut")
