@@ -165,6 +165,51 @@ int jmm_plain_get_positions(jmm_plain *h, double *r, uint64_t n);
 int jmm_plain_get_separations(jmm_plain *h, double *rij, uint64_t n_pairs);
 int jmm_plain_destroy(jmm_plain *h);
 
+/* rho(x) and g(x) histograms (fgrho / ugrho / qagrho, src/jmmMCState.cpp:
+ * 1069-1149, :2297-2384): rhonb density bins of width rbw (bin of x =
+ * floor(x/rbw + rhonb/2)); gns slices of width gsw (slice of x = floor(x/gsw
+ * + gns/2)), each with gnb separation bins of width gbw, a pair counted in
+ * the slices of both its particles.  Set-up takes the counts of the current
+ * configuration and accumulates them once, as setupMCS does (:773-776):
+ * call it after jmm_plain_set_config.  Then, as in the reference, every
+ * displacement step accumulates the counts once whatever its outcome (qad2
+ * calls ugrho), an accepted displacement updates them (qagrho), a qavLJ
+ * volume step recounts on acceptance and accumulates, and a fav volume step
+ * does neither (the reference's counts stay those of the old box).  A
+ * negative stored separation gives no g count (the reference writes out of
+ * bounds there). */
+int jmm_plain_histograms(jmm_plain *h, uint64_t rhonb, double rbw, int32_t gns, double gsw,
+                         uint64_t gnb, double gbw);
+/* Sums of the counts since the last take (the reference's int rhoA / gA,
+ * 32-bit wrapping), then zeroed, as printRho / printG do (:1021-1061);
+ * g is slice after slice (gns * gnb). */
+int jmm_plain_take_rho(jmm_plain *h, int32_t *counts, uint64_t rhonb);
+int jmm_plain_take_g(jmm_plain *h, int32_t *counts, uint64_t n);
+/* The current counts (rhol, gl). */
+int jmm_plain_hist_counts(jmm_plain *h, int32_t *rho, uint64_t rhonb, int32_t *g, uint64_t ng);
+
+/* Volume relaxation (relaxVolume, src/jmmMCState.cpp:2396-2643; the RELAX
+ * keyword): up to 20 Newton steps toward -dE/dL + N T / L = P, from central
+ * differences of E at L +- 0.1 (calculateEnergyOfTrialVolumeChange), each
+ * step clamped to 0.1 N and to the bracket of lengths tried, applied with
+ * moveVolume (positions scaled, every pair and total recomputed), until a
+ * step is shorter than 0.0025 N.  One launch for the whole relaxation. */
+typedef struct jmm_relax_step {
+  double e_up, e_down;  /* E at L + 0.1 and L - 0.1                           */
+  double dl;            /* the step taken                                     */
+  double l, e;          /* box length and E after it                          */
+} jmm_relax_step;
+/* log: room for 20 records; *n_steps records written; *converged 1 when the
+ * last step was below the criterion, 0 after 20 steps. */
+int jmm_plain_relax_volume(jmm_plain *h, jmm_relax_step *log, int32_t *n_steps,
+                           int32_t *converged);
+/* E of the positions scaled to L + dl (calculateEnergyOfTrialVolumeChange,
+ * :2756-2800); the state is not changed. */
+int jmm_plain_trial_volume_energy(jmm_plain *h, double dl, double *e);
+/* Positions scaled to box length l, every pair and total recomputed
+ * (moveVolume, :2803-2905). */
+int jmm_plain_move_volume(jmm_plain *h, double l);
+
 /* ---- batched form: many independent chains ------------------------------
  *
  * Each chain is the reference's sequential single-particle Metropolis chain

@@ -310,3 +310,12 @@ LARGE_RESULT_DTYPE = [
     ("window_overflows", "<u8"), ("max_drift", "<f8"), ("grid", "<f8"), ("error", "<u4"),
     ("reserved", "<u4"),
 ]
+
+
+class RelaxStep(C.Structure):
+    _fields_ = [("e_up", C.c_double), ("e_down", C.c_double), ("dl", C.c_double),
+                ("l", C.c_double), ("e", C.c_double)]
+
+
+RELAX_STEP_DTYPE = [("e_up", "<f8"), ("e_down", "<f8"), ("dl", "<f8"), ("l", "<f8"),
+                    ("e", "<f8")]

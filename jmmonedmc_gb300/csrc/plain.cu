@@ -13,6 +13,9 @@
 //   updateThermo                                 src/jmmMCState.cpp:1941-1961
 //   ECheck                                       src/jmmMCState.cpp:1965-2095
 //   fav                                          src/jmmMCState.cpp:2161-2293
+//   fgrho / ugrho / qagrho (rho(x), g(x))        src/jmmMCState.cpp:1069-1149, :2297-2384
+//   relaxVolume, calculateEnergyOfTrialVolumeChange, moveVolume
+//                                                src/jmmMCState.cpp:2396-2643, :2756-2905
 //
 // GB300 mapping: one persistent 1024-thread block runs many steps per launch.
 // Pair terms of a step are evaluated in parallel; the FP64 sums that decide
@@ -50,6 +53,7 @@ struct Scalars {
   double thermo[12];
   uint64_t echeck_count, echeck_resets;
   double echeck_e, echeck_e_before;
+  uint64_t hist_ticks;  // histogram accumulations (ugrho calls) since set-up
 };
 
 struct Args {
@@ -65,6 +69,17 @@ struct Args {
   int32_t pad;
   double cutoff, t, p;
   uint64_t seed, eci;
+  // rho(x) and g(x) histograms, bins [0, rhonb) density, then gns x gnb
+  // separation bins slice after slice.  The reference adds the current counts
+  // to the sums at every accumulation (ugrho); here each bin keeps its sum up
+  // to the accumulation at which its count last changed (h_acc, h_last), so
+  // that an accumulation costs O(1) instead of O(bins).
+  int32_t *h_val;               // current counts (rhol, gl)
+  long long *h_acc;             // sums up to accumulation h_last
+  unsigned long long *h_last;
+  uint64_t rhonb, gnb;
+  int32_t gns, hist_on;
+  double rbw, gsw, gbw;
 };
 
 struct Ctl {
@@ -235,6 +250,108 @@ __device__ void update_thermo(Scalars *S, uint64_t n) {
   acc[11] = __dadd_rn(acc[11], __dmul_rn(hv, hv));
 }
 
+// ---- rho(x) and g(x) histograms ---------------------------------------------
+
+// Bin indices as the reference forms them: (long) floor(x/w + nb/2.0).
+__device__ __forceinline__ long long rho_bin(const Args &a, double x) {
+  return (long long)floor(__dadd_rn(__ddiv_rn(x, a.rbw), __ddiv_rn((double)a.rhonb, 2.0)));
+}
+__device__ __forceinline__ long long slice_of(const Args &a, double x) {
+  return (long long)floor(__dadd_rn(__ddiv_rn(x, a.gsw), __ddiv_rn((double)a.gns, 2.0)));
+}
+// Separation bin of qagrho: (unsigned long) floor(|d| / gbw).
+__device__ __forceinline__ long long sep_bin(const Args &a, double d) {
+  return (long long)(unsigned long long)floor(__ddiv_rn(fabs(d), a.gbw));
+}
+
+// Brings bin b's sum up to accumulation T before its count changes; the
+// first caller of a step for a bin does it (the count is not yet changed:
+// changes are applied after a barrier).
+__device__ __forceinline__ void hist_flush(const Args &a, uint64_t b, uint64_t T) {
+  const unsigned long long old = atomicExch(&a.h_last[b], (unsigned long long)T);
+  if (old != T) a.h_acc[b] += (long long)a.h_val[b] * (long long)(T - old);
+}
+
+__device__ __forceinline__ void hist_touch(const Args &a, uint64_t b, uint64_t T, int phase,
+                                           int delta) {
+  if (phase == 0)
+    hist_flush(a, b, T);
+  else
+    atomicAdd(&a.h_val[b], delta);
+}
+
+// qagrho: particle ctl.nm moved by ctl.md, a.r[nm] already holds the new
+// position (the old one is formed as r[nm] - md, as the reference does).
+// Phase 0 flushes every bin the move touches, phase 1 changes the counts.
+__device__ void qagrho(const Args &a, const Ctl &ctl) {
+  const uint64_t n = a.n, nm = ctl.nm, nm1 = n - 1;
+  const uint64_t T = a.s->hist_ticks;
+  const double xn = a.r[nm];
+  const double xo = __dsub_rn(xn, ctl.md);
+  const long long rb1 = rho_bin(a, xo), rb2 = rho_bin(a, xn);
+  const long long gs11 = slice_of(a, xo), gs12 = slice_of(a, xn);
+  const bool v11 = gs11 >= 0 && gs11 < a.gns, v12 = gs12 >= 0 && gs12 < a.gns;
+  const long long nb = (long long)a.gnb;
+  for (int phase = 0; phase < 2; ++phase) {
+    if (threadIdx.x == 0) {
+      if (rb1 >= 0 && rb1 < (long long)a.rhonb) hist_touch(a, rb1, T, phase, -1);
+      if (rb2 >= 0 && rb2 < (long long)a.rhonb) hist_touch(a, rb2, T, phase, +1);
+    }
+    for (uint64_t p = threadIdx.x; p < nm1; p += blockDim.x) {
+      const uint64_t ii = p < nm ? p : p + 1;
+      const double xi = a.r[ii];
+      const long long gs2 = slice_of(a, xi);
+      const bool v2 = gs2 >= 0 && gs2 < a.gns;
+      const long long gb1 = sep_bin(a, __dsub_rn(xo, xi));
+      const long long gb2 = sep_bin(a, __dsub_rn(xn, xi));
+      const bool vb1 = gb1 >= 0 && gb1 < nb, vb2 = gb2 >= 0 && gb2 < nb;
+      const uint64_t g0 = a.rhonb;
+      if (v11 && vb1) hist_touch(a, g0 + gs11 * nb + gb1, T, phase, -1);
+      if (v12 && vb2) hist_touch(a, g0 + gs12 * nb + gb2, T, phase, +1);
+      if (v2 && vb1) hist_touch(a, g0 + gs2 * nb + gb1, T, phase, -1);
+      if (v2 && vb2) hist_touch(a, g0 + gs2 * nb + gb2, T, phase, +1);
+    }
+    __syncthreads();
+  }
+}
+
+// fgrho: counts of the current positions and stored separations, after every
+// bin's sum has been brought up to the current accumulation.  A negative
+// separation (particles that passed each other) gives a negative bin, which
+// the reference writes out of bounds; here it is not counted.
+__device__ void fgrho(const Args &a) {
+  const uint64_t n = a.n, T = a.s->hist_ticks;
+  const uint64_t total = a.rhonb + (uint64_t)a.gns * a.gnb;
+  for (uint64_t b = threadIdx.x; b < total; b += blockDim.x) {
+    a.h_acc[b] += (long long)a.h_val[b] * (long long)(T - a.h_last[b]);
+    a.h_last[b] = T;
+    a.h_val[b] = 0;
+  }
+  __syncthreads();
+  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const long long rb = rho_bin(a, a.r[i]);
+    if (rb >= 0 && rb < (long long)a.rhonb) atomicAdd(&a.h_val[rb], 1);
+  }
+  const long long nb = (long long)a.gnb;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (uint64_t i = warp; i < n; i += nwarps) {
+    const long long gs1 = slice_of(a, a.r[i]);
+    for (uint64_t j = i + 1 + lane; j < n; j += 32) {
+      const long long gb = (long long)floor(__ddiv_rn(a.rij[i * n + j], a.gbw));
+      if (gb < 0 || gb >= nb) continue;
+      const long long gs2 = slice_of(a, a.r[j]);
+      if (gs1 >= 0 && gs1 < a.gns) atomicAdd(&a.h_val[a.rhonb + gs1 * nb + gb], 1);
+      if (gs2 >= 0 && gs2 < a.gns) atomicAdd(&a.h_val[a.rhonb + gs2 * nb + gb], 1);
+    }
+  }
+  __syncthreads();
+}
+
+// ugrho: one accumulation.
+__device__ __forceinline__ void ugrho(const Args &a) {
+  if (threadIdx.x == 0) a.s->hist_ticks += 1;
+}
+
 // ---- the moves --------------------------------------------------------------
 
 // qad2: displacement of particle ctl.nm by (rn - 0.5) * 2 * maxStep.
@@ -320,6 +437,15 @@ __device__ void qad2(const Args &a, Ctl &ctl, double *s_new, double *s_rij, cons
     }
   }
   __syncthreads();
+  if (ctl.accept && a.hist_on) qagrho(a, ctl);  // src/jmmMCState.cpp:1431
+}
+
+// qad2 with its histogram accumulation, which the reference makes whatever
+// the outcome, the wall rejection included (src/jmmMCState.cpp:1453).
+__device__ void qad2_step(const Args &a, Ctl &ctl, double *s_new, double *s_rij,
+                          const jmm_draw *rp) {
+  qad2(a, ctl, s_new, s_rij, rp);
+  if (a.hist_on) ugrho(a);
 }
 
 // fav: full-energy volume move, linear dl uniform in +-maxdl.
@@ -440,6 +566,10 @@ __device__ void qav_lj(const Args &a, Ctl &ctl, const jmm_draw *rp) {
     }
   }
   __syncthreads();
+  if (a.hist_on) {  // fgrho on acceptance, ugrho always (src/jmmMCState.cpp:1717, :1726)
+    if (ctl.accept) fgrho(a);
+    ugrho(a);
+  }
 }
 
 // ECheck: full FP64 re-sum of E from the positions; on |dE| > 1e-4 rebuild
@@ -521,7 +651,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();
     if (ctl.nm < a.n) {
-      qad2(a, ctl, s_new, s_rij, rp);
+      qad2_step(a, ctl, s_new, s_rij, rp);
     } else if (ctl.nm == a.n) {
       if (a.use_qavlj)
         qav_lj(a, ctl, rp);
@@ -615,7 +745,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   __syncthreads();
   if (kind == JMM_KIND_DISPLACEMENT)
-    qad2(a, ctl, smem, smem + 9 * nm1, nullptr);
+    qad2_step(a, ctl, smem, smem + 9 * nm1, nullptr);
   else if (a.use_qavlj)
     qav_lj(a, ctl, nullptr);
   else
@@ -647,6 +777,165 @@ __global__ void separations_kernel(Args a) {
 
 __global__ void update_thermo_kernel(Args a) { update_thermo(a.s, a.n); }
 
+// ---- volume relaxation ----------------------------------------------------
+
+// calculateEnergyOfTrialVolumeChange: E of the positions scaled to L + dl,
+// pair terms in parallel, summed in pair order (pairs beyond NBN add zero).
+__device__ double trial_volume_energy(const Args &a, Ctl &ctl, double dl) {
+  Scalars *S = a.s;
+  if (threadIdx.x == 0) ctl.lrat1 = __ddiv_rn(__dadd_rn(S->l, dl), S->l);
+  __syncthreads();
+  const double lrat1 = ctl.lrat1;
+  for (uint64_t i = threadIdx.x; i < a.n; i += blockDim.x) a.r_trial[i] = __dmul_rn(a.r[i], lrat1);
+  __syncthreads();
+  full_terms(a, a.r_trial, false, S->l);
+  __syncthreads();
+  full_sums(a, ctl);
+  __syncthreads();
+  return ctl.sum[JMM_Q_E];
+}
+
+// moveVolume: positions scaled to box length l, every pair recomputed
+// (separations of pairs beyond NBN stay as they were), totals re-summed.
+__device__ void move_volume(const Args &a, Ctl &ctl, double l) {
+  Scalars *S = a.s;
+  const uint64_t n = a.n;
+  if (threadIdx.x == 0) ctl.lrat1 = __ddiv_rn(l, S->l);
+  __syncthreads();
+  const double lrat1 = ctl.lrat1;
+  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) a.r[i] = __dmul_rn(a.r[i], lrat1);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  for (uint64_t i = warp; i < n; i += nwarps) {
+    const uint64_t row = packed_index(i, i + 1, n);
+    for (uint64_t j = i + 1 + lane; j < n; j += 32) {
+      const uint64_t ind = i * n + j;
+      double phi[9];
+      if (pair_cut(a, i, j)) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) phi[k] = 0.0;
+      } else {
+        const double rij = __dsub_rn(a.r[j], a.r[i]);
+        a.rij[ind] = rij;
+        phi_eval(a, rij, true, l, phi);
+      }
+      double *dst = a.scratch + (row + (j - i - 1)) * 9;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        a.q[k * a.nn + ind] = phi[k];
+        dst[k] = phi[k];
+      }
+    }
+  }
+  __syncthreads();
+  full_sums(a, ctl);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    S->l = l;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) S->tot[k] = ctl.sum[k];
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads, 1) trial_volume_energy_kernel(Args a, double dl,
+                                                                          double *out) {
+  __shared__ Ctl ctl;
+  const double e = trial_volume_energy(a, ctl, dl);
+  if (threadIdx.x == 0) *out = e;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) move_volume_kernel(Args a, double l) {
+  __shared__ Ctl ctl;
+  move_volume(a, ctl, l);
+}
+
+// relaxVolume: up to 20 Newton steps, the scalar arithmetic by thread 0 in
+// the reference's operand order; out[0] = steps taken, out[1] = converged.
+__global__ void __launch_bounds__(kThreads, 1) relax_kernel(Args a, jmm_relax_step *log,
+                                                             int32_t *out) {
+  __shared__ Ctl ctl;
+  __shared__ double ltrymin, ltrymax, dle;
+  __shared__ int done;
+  Scalars *S = a.s;
+  const double hh = 0.1;
+  if (threadIdx.x == 0) {
+    ltrymin = 0.0;
+    ltrymax = 1E10;
+    done = 0;
+    out[0] = 0;
+    out[1] = 0;
+  }
+  __syncthreads();
+  for (int count = 0; count < 20; ++count) {
+    const double eup = trial_volume_energy(a, ctl, hh);
+    const double edown = trial_volume_energy(a, ctl, -hh);
+    if (threadIdx.x == 0) {
+      const double e = S->tot[JMM_Q_E], l = S->l, nd = (double)a.n;
+      const double first = __ddiv_rn(__dsub_rn(eup, edown), __dmul_rn(2.0, hh));
+      const double second =
+          __ddiv_rn(__dadd_rn(__dsub_rn(eup, __dmul_rn(2.0, e)), edown), __dmul_rn(hh, hh));
+      double d = __ddiv_rn(-__dadd_rn(__dsub_rn(a.p, __dmul_rn(__ddiv_rn(nd, l), a.t)), first),
+                           second);
+      const double relax_max = __dmul_rn(0.10, nd);
+      if (fabs(d) > relax_max) d = d < 0 ? -relax_max : relax_max;
+      if (__dadd_rn(l, d) > ltrymax)
+        d = __dmul_rn(0.5, __dsub_rn(ltrymax, l));
+      else if (__dadd_rn(l, d) < ltrymin)
+        d = __dmul_rn(0.5, __dsub_rn(ltrymin, l));
+      if (d > 0.0)
+        ltrymin = l;
+      else
+        ltrymax = l;
+      done = fabs(d) < __dmul_rn(0.0025, nd);
+      dle = d;
+      log[count].e_up = eup;
+      log[count].e_down = edown;
+      log[count].dl = d;
+    }
+    __syncthreads();
+    move_volume(a, ctl, __dadd_rn(S->l, dle));
+    if (threadIdx.x == 0) {
+      log[count].l = S->l;
+      log[count].e = S->tot[JMM_Q_E];
+      out[0] = count + 1;
+      out[1] = done;
+    }
+    __syncthreads();
+    if (done) break;
+  }
+}
+
+// Set-up of the histograms: counts of the current configuration, accumulated
+// once (setupMCS, src/jmmMCState.cpp:773-776).
+__global__ void __launch_bounds__(kThreads, 1) hist_init_kernel(Args a) {
+  const uint64_t total = a.rhonb + (uint64_t)a.gns * a.gnb;
+  for (uint64_t b = threadIdx.x; b < total; b += blockDim.x) {
+    a.h_val[b] = 0;
+    a.h_acc[b] = 0;
+    a.h_last[b] = 0;
+  }
+  if (threadIdx.x == 0) a.s->hist_ticks = 0;
+  __syncthreads();
+  fgrho(a);
+  ugrho(a);
+}
+
+// Sums of bins [b0, b0 + nb) since the last take, as the reference's int
+// accumulators hold them (wrapped to 32 bits), then zeroed (printRho /
+// printG, src/jmmMCState.cpp:1021-1061).
+__global__ void hist_take_kernel(Args a, uint64_t b0, uint64_t nb, int32_t *out) {
+  const uint64_t T = a.s->hist_ticks;
+  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < nb;
+       k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t b = b0 + k;
+    const long long total = a.h_acc[b] + (long long)a.h_val[b] * (long long)(T - a.h_last[b]);
+    out[k] = (int32_t)(uint32_t)(unsigned long long)total;
+    a.h_acc[b] = 0;
+    a.h_last[b] = T;
+  }
+}
+
 }  // namespace plain
 }  // namespace jmm
 
@@ -661,6 +950,7 @@ struct jmm_plain {
   uint64_t replay_cap;
   jmm_step_record *d_log;
   uint64_t log_cap;
+  int32_t *d_hist_out;  // staging of a histogram take
   bool initialised;  // fad has run since set-up
 };
 
@@ -672,6 +962,10 @@ static void plain_free(jmm_plain *h) {
   cudaFree(h->a.rij);
   cudaFree(h->a.q);
   cudaFree(h->a.scratch);
+  cudaFree(h->a.h_val);
+  cudaFree(h->a.h_acc);
+  cudaFree(h->a.h_last);
+  cudaFree(h->d_hist_out);
   cudaFree(h->d_replay);
   cudaFree(h->d_log);
   delete h;
@@ -999,4 +1293,132 @@ extern "C" int jmm_plain_get_separations(jmm_plain *h, double *rij, uint64_t n_p
     for (uint64_t j = i + 1; j < n; ++j) rij[k++] = dense[i * n + j];
   free(dense);
   return JMM_OK;
+}
+
+// ---- rho(x) and g(x) histograms --------------------------------------------
+
+extern "C" int jmm_plain_histograms(jmm_plain *h, uint64_t rhonb, double rbw, int32_t gns,
+                                    double gsw, uint64_t gnb, double gbw) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  JMM_CHECK_ARG(rhonb >= 1 && gns >= 1 && gnb >= 1, "bin counts must be positive");
+  JMM_CHECK_ARG(rbw > 0 && gsw > 0 && gbw > 0, "bin widths must be positive");
+  const uint64_t total = rhonb + (uint64_t)gns * gnb;
+  JMM_CHECK_ARG(total <= (1ull << 26), "at most 2^26 histogram bins");
+  Args &a = h->a;
+  cudaFree(a.h_val);
+  cudaFree(a.h_acc);
+  cudaFree(a.h_last);
+  cudaFree(h->d_hist_out);
+  a.h_val = nullptr;
+  a.h_acc = nullptr;
+  a.h_last = nullptr;
+  h->d_hist_out = nullptr;
+  a.hist_on = 0;
+  JMM_CUDA(cudaMalloc((void **)&a.h_val, total * sizeof(int32_t)));
+  JMM_CUDA(cudaMalloc((void **)&a.h_acc, total * sizeof(long long)));
+  JMM_CUDA(cudaMalloc((void **)&a.h_last, total * sizeof(unsigned long long)));
+  JMM_CUDA(cudaMalloc((void **)&h->d_hist_out, total * sizeof(int32_t)));
+  a.rhonb = rhonb;
+  a.rbw = rbw;
+  a.gns = gns;
+  a.gsw = gsw;
+  a.gnb = gnb;
+  a.gbw = gbw;
+  a.hist_on = 1;
+  hist_init_kernel<<<1, kThreads>>>(a);
+  return plain_sync("hist_init_kernel");
+}
+
+static int hist_take(jmm_plain *h, uint64_t b0, uint64_t nb, int32_t *out) {
+  hist_take_kernel<<<(unsigned)((nb + 255) / 256 < 1024 ? (nb + 255) / 256 : 1024), 256>>>(
+      h->a, b0, nb, h->d_hist_out);
+  int rc = plain_sync("hist_take_kernel");
+  if (rc) return rc;
+  JMM_CUDA(cudaMemcpy(out, h->d_hist_out, nb * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return JMM_OK;
+}
+
+extern "C" int jmm_plain_take_rho(jmm_plain *h, int32_t *counts, uint64_t rhonb) {
+  clear_error();
+  JMM_CHECK_ARG(h && counts, "null argument");
+  if (!h->a.hist_on) return fail(JMM_ERR_STATE, "jmm_plain_take_rho: histograms are not set up");
+  JMM_CHECK_ARG(rhonb == h->a.rhonb, "rhonb does not match the set-up");
+  return hist_take(h, 0, rhonb, counts);
+}
+
+extern "C" int jmm_plain_take_g(jmm_plain *h, int32_t *counts, uint64_t n) {
+  clear_error();
+  JMM_CHECK_ARG(h && counts, "null argument");
+  if (!h->a.hist_on) return fail(JMM_ERR_STATE, "jmm_plain_take_g: histograms are not set up");
+  JMM_CHECK_ARG(n == (uint64_t)h->a.gns * h->a.gnb, "n must be gns * gnb");
+  return hist_take(h, h->a.rhonb, n, counts);
+}
+
+extern "C" int jmm_plain_hist_counts(jmm_plain *h, int32_t *rho, uint64_t rhonb, int32_t *g,
+                                     uint64_t ng) {
+  clear_error();
+  JMM_CHECK_ARG(h && rho && g, "null argument");
+  if (!h->a.hist_on)
+    return fail(JMM_ERR_STATE, "jmm_plain_hist_counts: histograms are not set up");
+  JMM_CHECK_ARG(rhonb == h->a.rhonb && ng == (uint64_t)h->a.gns * h->a.gnb,
+                "sizes do not match the set-up");
+  JMM_CUDA(cudaDeviceSynchronize());
+  JMM_CUDA(cudaMemcpy(rho, h->a.h_val, rhonb * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  JMM_CUDA(cudaMemcpy(g, h->a.h_val + rhonb, ng * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return JMM_OK;
+}
+
+// ---- volume relaxation --------------------------------------------------------
+
+extern "C" int jmm_plain_relax_volume(jmm_plain *h, jmm_relax_step *log, int32_t *n_steps,
+                                      int32_t *converged) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  jmm_relax_step *d_log = nullptr;
+  int32_t *d_out = nullptr;
+  JMM_CUDA(cudaMalloc((void **)&d_log, 20 * sizeof(jmm_relax_step)));
+  cudaError_t e = cudaMalloc((void **)&d_out, 2 * sizeof(int32_t));
+  if (e != cudaSuccess) {
+    cudaFree(d_log);
+    return cuda_status(e, "cudaMalloc relax", __FILE__, __LINE__);
+  }
+  relax_kernel<<<1, kThreads>>>(h->a, d_log, d_out);
+  int rc = plain_sync("relax_kernel");
+  int32_t out[2] = {0, 0};
+  if (rc == JMM_OK) {
+    e = cudaMemcpy(out, d_out, sizeof(out), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && log)
+      e = cudaMemcpy(log, d_log, out[0] * sizeof(jmm_relax_step), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_status(e, "cudaMemcpy relax", __FILE__, __LINE__);
+  }
+  cudaFree(d_log);
+  cudaFree(d_out);
+  if (rc) return rc;
+  if (n_steps) *n_steps = out[0];
+  if (converged) *converged = out[1];
+  return JMM_OK;
+}
+
+extern "C" int jmm_plain_trial_volume_energy(jmm_plain *h, double dl, double *e_out) {
+  clear_error();
+  JMM_CHECK_ARG(h && e_out, "null argument");
+  double *d = nullptr;
+  JMM_CUDA(cudaMalloc((void **)&d, sizeof(double)));
+  trial_volume_energy_kernel<<<1, kThreads>>>(h->a, dl, d);
+  int rc = plain_sync("trial_volume_energy_kernel");
+  if (rc == JMM_OK) {
+    cudaError_t e = cudaMemcpy(e_out, d, sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_status(e, "cudaMemcpy trial energy", __FILE__, __LINE__);
+  }
+  cudaFree(d);
+  return rc;
+}
+
+extern "C" int jmm_plain_move_volume(jmm_plain *h, double l) {
+  clear_error();
+  JMM_CHECK_ARG(h, "null handle");
+  JMM_CHECK_ARG(l > 0, "box length must be positive");
+  move_volume_kernel<<<1, kThreads>>>(h->a, l);
+  return plain_sync("move_volume_kernel");
 }

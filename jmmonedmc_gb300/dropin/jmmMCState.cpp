@@ -7,8 +7,10 @@
 // loop runs on the GPU through the C ABI of include/jmm_gpu.h (the plain FP64
 // form, which reproduces the reference's trajectory step for step); this file
 // keeps the host-side parts: parameters, step counting, the print cadence and
-// the output files config.dat.mcs and thermo.dat.mcs in the reference's
-// formats (src/jmmMCState.cpp:1007-1017, :1896-1937).
+// the output files config.dat.mcs, thermo.dat.mcs, rho.dat.mcs and
+// g<k>.dat.mcs in the reference's formats (src/jmmMCState.cpp:1007-1061,
+// :1896-1937); the histogram counts themselves are kept on the GPU by the
+// move loop (jmm_plain_histograms).
 //
 // Step() only counts: the counted steps run on the GPU in one launch when
 // the driver next needs the chain's state (a print, an adjustment, the
@@ -17,9 +19,10 @@
 // team and the rest from one thread; here the former run once per team
 // (omp single, the value broadcast), the latter under a critical section.
 //
-// Not computed by this module: the rho(x) and g(x) histograms (fgrho, ugrho,
-// qagrho, printRho and printG do nothing) and the volume relaxation
-// (relaxVolume returns at once); both are stated on stderr once.
+// fgrho, ugrho and qagrho are run by the GPU move loop where the reference's
+// moves call them; called directly they do nothing.  On a restart the
+// histogram files keep their lines up to the restart step and are cut there
+// (the reference overwrites in place).
 #include "jmmMCState.h"
 
 #include <math.h>
@@ -51,18 +54,13 @@ struct MCState {
   int gns;
   char potStr[20];
   char ensembleStr[80];
-  FILE *cf, *tf;
-  bool warned_histograms, warned_relax;
+  FILE *cf, *tf, *rhof;
+  std::vector<FILE *> gf;
+  unsigned long int slrho, slg;  // steps of the last rho / g prints
+  double rbw, gsw, gbw;
 };
 
 namespace {
-
-void notice_once(bool *flag, const char *msg) {
-  if (!*flag) {
-    fprintf(stderr, "jmmMCState (GPU): %s\n", msg);
-    *flag = true;
-  }
-}
 
 void report(int rc, const char *what) {
   if (rc != JMM_OK) {
@@ -158,24 +156,34 @@ bool read_last_frame(unsigned long int n, std::vector<double> *r, unsigned long 
   return found;
 }
 
-// Keeps the header and the lines of thermo.dat.mcs up to step `sn`.
-void rewind_thermo(unsigned long int sn) {
-  FILE *f = fopen("thermo.dat.mcs", "r");
+// Keeps the lines of `name` whose step is <= `sn` (and the header line when
+// `header`), cuts the rest, and returns the last kept step.
+unsigned long int rewind_file(const char *name, unsigned long int sn, bool header) {
+  FILE *f = fopen(name, "r");
   std::vector<std::string> keep;
+  unsigned long int last = 0;
   if (f) {
-    char buf[4096];
+    std::vector<char> buf(1 << 20);
     bool first = true;
-    while (fgets(buf, sizeof(buf), f)) {
+    while (fgets(buf.data(), (int)buf.size(), f)) {
       unsigned long int s;
-      if (first || (sscanf(buf, "%lu", &s) == 1 && s <= sn)) keep.push_back(buf);
+      if (first && header) {
+        keep.push_back(buf.data());
+      } else if (sscanf(buf.data(), "%lu", &s) == 1 && s <= sn) {
+        keep.push_back(buf.data());
+        last = s;
+      }
       first = false;
     }
     fclose(f);
   }
-  f = fopen("thermo.dat.mcs", "w");
+  f = fopen(name, "w");
   for (const auto &line : keep) fputs(line.c_str(), f);
   fclose(f);
+  return last;
 }
+
+void rewind_thermo(unsigned long int sn) { rewind_file("thermo.dat.mcs", sn, true); }
 
 }  // namespace
 
@@ -257,6 +265,9 @@ struct MCState *setupMCS(struct MCInput inp) {
   mcs->seed = inp.seed;
   mcs->maxStep = inp.maxStep;
   mcs->maxdl = inp.maxdl;
+  mcs->rbw = inp.rbw;
+  mcs->gsw = inp.gsw;
+  mcs->gbw = inp.gbw;
   mcs->rn = 0.5;
   printMCP(mcs);
   if (jmm_plain_create(&p, &mcs->h) != JMM_OK) {
@@ -267,10 +278,18 @@ struct MCState *setupMCS(struct MCInput inp) {
   if (!mcs->isRestart) {
     mcs->cf = fopen("config.dat.mcs", "w");
     mcs->tf = fopen("thermo.dat.mcs", "w");
+    mcs->rhof = fopen("rho.dat.mcs", "w");
+    for (int k = 0; k < mcs->gns; ++k) {
+      char name[64];
+      snprintf(name, sizeof(name), "g%d.dat.mcs", k);
+      mcs->gf.push_back(fopen(name, "w"));
+    }
     mcs->sn = 0;
     mcs->dev_sn = 0;
     mcs->slcp = (unsigned long int)-1;
     mcs->sltp = (unsigned long int)-1;
+    mcs->slrho = (unsigned long int)-1;
+    mcs->slg = (unsigned long int)-1;
     fprintf(mcs->tf,
             "Step    Econf           Econf2          L       L2      LEconf          rho"
             "             rho2            Virial         Virial2         EconfVir        HV"
@@ -289,13 +308,40 @@ struct MCState *setupMCS(struct MCInput inp) {
     printf("Complete configuration found for step number %lu\n", sn);
     printf("Box length: %.8g\n", l);
     report(jmm_plain_set_config(mcs->h, r.data(), mcs->N, l, sn), "jmm_plain_set_config");
+    printf("Opening file %s\n", "rho.dat.mcs");
+    const unsigned long int lastrho = rewind_file("rho.dat.mcs", sn, false);
+    printf("Last rho time point <= last complete config time point: %lu\n"
+           "  Overwriting density data beyond this point.\n", lastrho);
+    unsigned long int lastgmin = sn;
+    for (int k = 0; k < mcs->gns; ++k) {
+      char name[64];
+      snprintf(name, sizeof(name), "g%d.dat.mcs", k);
+      printf("Opening file %s\n", name);
+      const unsigned long int lastg = rewind_file(name, sn, false);
+      printf("Last g[%d] time point <= last complete config time point: %lu\n", k, lastg);
+      if (lastg < lastgmin) lastgmin = lastg;
+      mcs->gf.push_back(fopen(name, "a"));
+    }
+    printf("Least compatible g time point: %lu\n"
+           "  Overwriting g(r) data beyond this point.\n", lastgmin);
     rewind_thermo(sn);
     mcs->cf = fopen("config.dat.mcs", "a");
     mcs->tf = fopen("thermo.dat.mcs", "a");
+    mcs->rhof = fopen("rho.dat.mcs", "a");
     mcs->sn = sn;
     mcs->dev_sn = sn;
     mcs->slcp = sn;
     mcs->sltp = sn;
+    mcs->slrho = sn;
+    mcs->slg = sn;
+  }
+  // the density and g(x) counts of the starting configuration, accumulated
+  // once (setupMCS, src/jmmMCState.cpp:773-776)
+  if (jmm_plain_histograms(mcs->h, mcs->rhonb, mcs->rbw, mcs->gns, mcs->gsw, mcs->gnb,
+                           mcs->gbw) != JMM_OK) {
+    printf("FATAL ERROR: %s\nABORTING SIMULATION\n\n", jmm_last_error());
+    freeMCS(mcs);
+    return nullptr;
   }
   fflush(mcs->cf);
   fflush(mcs->tf);
@@ -308,6 +354,9 @@ void freeMCS(struct MCState *mcs) {
   jmm_plain_destroy(mcs->h);
   if (mcs->cf) fclose(mcs->cf);
   if (mcs->tf) fclose(mcs->tf);
+  if (mcs->rhof) fclose(mcs->rhof);
+  for (FILE *f : mcs->gf)
+    if (f) fclose(f);
   delete mcs;
 }
 
@@ -435,17 +484,64 @@ int printCoords(struct MCState *mcs) {
   return 0;
 }
 
+// printRho (src/jmmMCState.cpp:1021-1037): the density sums since the last
+// print, divided by the steps since then and the bin width.
 int printRho(struct MCState *mcs) {
-  notice_once(&mcs->warned_histograms,
-              "the rho(x) and g(x) histograms are not computed; rho.dat.mcs and g*.dat.mcs "
-              "are not written");
+#pragma omp critical(jmm_dropin)
+  {
+    flush(mcs);
+    std::vector<int32_t> acc(mcs->rhonb);
+    report(jmm_plain_take_rho(mcs->h, acc.data(), mcs->rhonb), "jmm_plain_take_rho");
+    const unsigned long int ns = mcs->sn - mcs->slrho;
+    fprintf(mcs->rhof, "%lu", mcs->sn);
+    for (unsigned long int rb = 0; rb < mcs->rhonb; ++rb)
+      fprintf(mcs->rhof, " %.8G", (double)acc[rb] / ns / mcs->rbw);
+    fprintf(mcs->rhof, "\n");
+    fflush(mcs->rhof);
+    mcs->slrho = mcs->sn;
+  }
   return 0;
 }
 
-int printG(struct MCState *mcs) { return printRho(mcs); }
-int fgrho(struct MCState *mcs) { return printRho(mcs); }
-int ugrho(struct MCState *mcs) { return printRho(mcs); }
-int qagrho(struct MCState *mcs) { return printRho(mcs); }
+// printG (src/jmmMCState.cpp:1042-1061), which the driver calls from every
+// thread of its team: one line per slice file.
+int printG(struct MCState *mcs) {
+#pragma omp single
+  {
+#pragma omp critical(jmm_dropin)
+    {
+      flush(mcs);
+      const unsigned long int nbin = (unsigned long int)mcs->gns * mcs->gnb;
+      std::vector<int32_t> acc(nbin);
+      report(jmm_plain_take_g(mcs->h, acc.data(), nbin), "jmm_plain_take_g");
+      const unsigned long int ns = mcs->sn - mcs->slg;
+      for (int gs = 0; gs < mcs->gns; ++gs) {
+        fprintf(mcs->gf[gs], "%lu", mcs->sn);
+        for (unsigned long int gb = 0; gb < mcs->gnb; ++gb)
+          fprintf(mcs->gf[gs], " %.8G", (double)acc[gs * mcs->gnb + gb] / ns / mcs->gsw / mcs->gbw);
+        fprintf(mcs->gf[gs], "\n");
+        fflush(mcs->gf[gs]);
+      }
+      mcs->slg = mcs->sn;
+    }
+  }
+  return 0;
+}
+
+// The histogram updates run inside the GPU move loop where the reference's
+// moves call them (qad2, qavLJ) and at set-up; a direct call has nothing to do.
+int fgrho(struct MCState *mcs) {
+  (void)mcs;
+  return 0;
+}
+int ugrho(struct MCState *mcs) {
+  (void)mcs;
+  return 0;
+}
+int qagrho(struct MCState *mcs) {
+  (void)mcs;
+  return 0;
+}
 
 int ECheck(struct MCState *mcs) {
   int32_t reset = 0;
@@ -511,20 +607,51 @@ int maxDVAdjust(struct MCState *mcs) {
   return 0;
 }
 
+// relaxVolume (src/jmmMCState.cpp:2396-2643): the Newton steps run on the
+// GPU in one launch; their messages are printed from its per-step records.
 int relaxVolume(struct MCState *mcs) {
-  notice_once(&mcs->warned_relax, "relaxVolume is not part of the GPU move loop; skipped");
-  return 0;
+  int rc = 0;
+#pragma omp single copyprivate(rc)
+  {
+    flush(mcs);
+    const jmm_state st = state_of(mcs);
+    printf("Relaxing the Volume...Starting Length,Energy: %.5G,%.5G\n", st.l, st.tot[JMM_Q_E]);
+    jmm_relax_step log[20];
+    int32_t n = 0, conv = 0;
+    report(jmm_plain_relax_volume(mcs->h, log, &n, &conv), "jmm_plain_relax_volume");
+    for (int k = 0; k < n; ++k) {
+      printf("Relaxation step %d...", k);
+      if (k == n - 1 && conv)
+        printf("Relaxation converged. Length,energy: %.10G,%.10G\n", log[k].l, log[k].e);
+      else
+        printf("length,energy: %.5g,%.5G\n", log[k].l, log[k].e);
+    }
+    if (!conv)
+      printf("WARNING: Relaxation failed to converge after 20 steps. Length,energy: %.5G,%.5G\n",
+             log[n - 1].l, log[n - 1].e);
+    fflush(stdout);
+    rc = conv ? 0 : 1;
+  }
+  return rc;
 }
 
 double calculateEnergyOfTrialVolumeChange(struct MCState *mcs, double dl) {
-  (void)dl;
-  relaxVolume(mcs);
-  return NAN;
+  double e = 0;
+#pragma omp single copyprivate(e)
+  {
+    flush(mcs);
+    report(jmm_plain_trial_volume_energy(mcs->h, dl, &e), "jmm_plain_trial_volume_energy");
+  }
+  return e;
 }
 
 int moveVolume(struct MCState *mcs, double l) {
-  (void)l;
-  return relaxVolume(mcs);
+#pragma omp single
+  {
+    flush(mcs);
+    report(jmm_plain_move_volume(mcs->h, l), "jmm_plain_move_volume");
+  }
+  return (int)l;
 }
 
 unsigned long int getStepNum(struct MCState *mcs) { return mcs->sn; }

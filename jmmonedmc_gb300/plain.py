@@ -11,6 +11,18 @@ import numpy as np
 
 from . import _native, abi
 
+P = C.POINTER
+_native.register({
+    "jmm_plain_histograms": [C.c_void_p, C.c_uint64, C.c_double, C.c_int32, C.c_double,
+                             C.c_uint64, C.c_double],
+    "jmm_plain_take_rho": [C.c_void_p, P(C.c_int32), C.c_uint64],
+    "jmm_plain_take_g": [C.c_void_p, P(C.c_int32), C.c_uint64],
+    "jmm_plain_hist_counts": [C.c_void_p, P(C.c_int32), C.c_uint64, P(C.c_int32), C.c_uint64],
+    "jmm_plain_relax_volume": [C.c_void_p, C.c_void_p, P(C.c_int32), P(C.c_int32)],
+    "jmm_plain_trial_volume_energy": [C.c_void_p, C.c_double, P(C.c_double)],
+    "jmm_plain_move_volume": [C.c_void_p, C.c_double],
+})
+
 
 class PlainChain:
     def __init__(self, params: abi.Params):
@@ -108,3 +120,45 @@ class PlainChain:
         _native.call("jmm_plain_get_separations", self._h,
                      rij.ctypes.data_as(C.POINTER(C.c_double)), m)
         return rij
+
+    # --- rho(x) and g(x) histograms (fgrho/ugrho/qagrho, printRho/printG) ----
+    def histograms(self, rhonb, rbw, gns, gsw, gnb, gbw):
+        self._hist = (int(rhonb), int(gns), int(gnb))
+        _native.call("jmm_plain_histograms", self._h, rhonb, rbw, gns, gsw, gnb, gbw)
+
+    def take_rho(self):
+        out = np.empty(self._hist[0], dtype=np.int32)
+        _native.call("jmm_plain_take_rho", self._h, out.ctypes.data_as(P(C.c_int32)), out.size)
+        return out
+
+    def take_g(self):
+        rhonb, gns, gnb = self._hist
+        out = np.empty(gns * gnb, dtype=np.int32)
+        _native.call("jmm_plain_take_g", self._h, out.ctypes.data_as(P(C.c_int32)), out.size)
+        return out.reshape(gns, gnb)
+
+    def hist_counts(self):
+        rhonb, gns, gnb = self._hist
+        rho = np.empty(rhonb, dtype=np.int32)
+        g = np.empty(gns * gnb, dtype=np.int32)
+        _native.call("jmm_plain_hist_counts", self._h, rho.ctypes.data_as(P(C.c_int32)), rhonb,
+                     g.ctypes.data_as(P(C.c_int32)), g.size)
+        return rho, g.reshape(gns, gnb)
+
+    # --- volume relaxation (relaxVolume, calculateEnergyOfTrialVolumeChange, moveVolume)
+    def relax_volume(self):
+        """Returns (per-step records, converged)."""
+        log = (abi.RelaxStep * 20)()
+        n, conv = C.c_int32(), C.c_int32()
+        _native.call("jmm_plain_relax_volume", self._h, C.cast(log, C.c_void_p), C.byref(n),
+                     C.byref(conv))
+        return (np.frombuffer(log, dtype=np.dtype(abi.RELAX_STEP_DTYPE))[:n.value].copy(),
+                bool(conv.value))
+
+    def trial_volume_energy(self, dl):
+        e = C.c_double()
+        _native.call("jmm_plain_trial_volume_energy", self._h, dl, C.byref(e))
+        return e.value
+
+    def move_volume(self, l):
+        _native.call("jmm_plain_move_volume", self._h, l)

@@ -34,6 +34,9 @@ int jmmo_plain_take_rho(jmmo_plain *h, int32_t *out, uint64_t rhonb);
 int jmmo_plain_take_g(jmmo_plain *h, int32_t *out, uint64_t n);
 int jmmo_plain_hist_counts(jmmo_plain *h, int32_t *rho, uint64_t rhonb, int32_t *g,
                            uint64_t ng);
+double jmmo_plain_trial_volume_energy(jmmo_plain *h, double dl);
+int jmmo_plain_move_volume(jmmo_plain *h, double l);
+int jmmo_plain_relax_volume(jmmo_plain *h, jmm_relax_step *log, int32_t *n_steps);
 
 void jmmo_philox_raw(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 void jmmo_step_words_export(uint64_t seed, uint64_t block, uint32_t chain, uint32_t out[4]);

@@ -18,6 +18,8 @@
  *   fav                        src/jmmMCState.cpp:2161-2293
  *   fgrho / ugrho              src/jmmMCState.cpp:1069-1149
  *   qagrho                     src/jmmMCState.cpp:2297-2384
+ *   relaxVolume                src/jmmMCState.cpp:2396-2643
+ *   calculateEnergyOfTrialVolumeChange / moveVolume   :2756-2905
  *
  * Every FP64 expression keeps the reference's operand order; the file is
  * compiled with -ffp-contract=off so no multiply-add is fused.
@@ -745,4 +747,90 @@ int jmmo_plain_move(jmmo_plain *h, int32_t kind, uint64_t nm, double rn, jmm_ste
   }
   set_record(rec, h, kind == JMM_KIND_VOLUME ? h->n : nm, rn, ran, bf, kind, outcome);
   return JMM_OK;
+}
+
+/* ---- volume relaxation ----------------------------------------------------- */
+
+/* calculateEnergyOfTrialVolumeChange, src/jmmMCState.cpp:2756-2800: E of the
+ * positions scaled to L + dl, summed in pair order, pairs beyond NBN zero. */
+double jmmo_plain_trial_volume_energy(jmmo_plain *h, double dl) {
+  uint64_t n = h->n;
+  double lrat1 = (h->l + dl) / h->l;
+  for (uint64_t i = 0; i < n; ++i) h->r_trial[i] = h->r[i] * lrat1;
+  double e = 0, phi[9];
+  for (uint64_t i = 0; i < n; ++i) {
+    for (uint64_t j = i + 1; j < n; ++j) {
+      if (pair_cut(h, i, j)) continue;
+      phi_eval(h, h->r_trial[j] - h->r_trial[i], 0, h->l, phi);
+      e += phi[0];
+    }
+  }
+  return e;
+}
+
+/* moveVolume, src/jmmMCState.cpp:2803-2905: positions scaled to the box
+ * length l, every pair and total recomputed (separations of pairs beyond NBN
+ * are left as they were). */
+int jmmo_plain_move_volume(jmmo_plain *h, double l) {
+  uint64_t n = h->n, nn = n * n;
+  double lrat1 = l / h->l;
+  for (uint64_t i = 0; i < n; ++i) h->r[i] = h->r[i] * lrat1;
+  h->l = l;
+  double sum[9] = {0}, phi[9];
+  for (uint64_t i = 0; i < n; ++i) {
+    for (uint64_t j = i + 1; j < n; ++j) {
+      uint64_t ind = i * n + j;
+      if (pair_cut(h, i, j)) {
+        for (int k = 0; k < 9; ++k) h->q[k * nn + ind] = 0;
+        continue;
+      }
+      h->rij[ind] = h->r[j] - h->r[i];
+      phi_eval(h, h->rij[ind], 1, l, phi);
+      for (int k = 0; k < 9; ++k) {
+        h->q[k * nn + ind] = phi[k];
+        sum[k] += phi[k];
+      }
+    }
+  }
+  memcpy(h->tot, sum, sizeof(sum));
+  return JMM_OK;
+}
+
+/* relaxVolume, src/jmmMCState.cpp:2396-2643: up to 20 Newton steps on
+ * E(L) + P L - N T ln L from central differences at +-0.1, each clamped to
+ * 0.1 N and to the bracket of lengths seen, until a step is below 0.0025 N.
+ * One record per step; returns 1 when converged, 0 after 20 steps. */
+int jmmo_plain_relax_volume(jmmo_plain *h, jmm_relax_step *log, int32_t *n_steps) {
+  double ltrymin = 0, ltrymax = 1E10;
+  const double hh = 0.1;
+  for (int count = 0; count < 20; ++count) {
+    double eup = jmmo_plain_trial_volume_energy(h, hh);
+    double edown = jmmo_plain_trial_volume_energy(h, -hh);
+    double e = h->tot[JMM_Q_E];
+    double first = (eup - edown) / (2 * hh);
+    double second = (eup - 2.0 * e + edown) / (hh * hh);
+    double dle = -(h->prm.p - ((double)h->n / h->l) * h->prm.t + first) / second;
+    double relax_max = (double)0.10 * h->n;
+    if (fabs(dle) > relax_max) dle = dle < 0 ? -relax_max : relax_max;
+    if (h->l + dle > ltrymax)
+      dle = 0.5 * (ltrymax - h->l);
+    else if (h->l + dle < ltrymin)
+      dle = 0.5 * (ltrymin - h->l);
+    if (dle > 0.0)
+      ltrymin = h->l;
+    else
+      ltrymax = h->l;
+    int done = fabs(dle) < 0.0025 * h->n;
+    jmmo_plain_move_volume(h, h->l + dle);
+    if (log) {
+      log[count].e_up = eup;
+      log[count].e_down = edown;
+      log[count].dl = dle;
+      log[count].l = h->l;
+      log[count].e = h->tot[JMM_Q_E];
+    }
+    if (n_steps) *n_steps = count + 1;
+    if (done) return 1;
+  }
+  return 0;
 }

@@ -61,6 +61,10 @@ CASES = {
     # dense NPT start (L = N) with a wide volume step: many volume moves
     "npt32_ljcut_wide": dict(ENSEMBLE="NPT", N=32, P=2.0, T=1.5, MAXDV=2.0,
                              SEED=99, NUMSTEPS=4000, ENGCHECK=250),
+    # RELAX (as the reference's test/INPUT): relaxVolume after the step-0 fad
+    # and again at step 10000
+    "npt32_ljcut_relax": dict(ENSEMBLE="NPT", N=32, P=1.0, T=1.0, MAXDV=1.0, SEED=41,
+                              NUMSTEPS=10000, ENGCHECK=1000, TPI=1000, RELAX=1),
 }
 
 
@@ -74,6 +78,8 @@ def input_text(kw):
         if isinstance(v, float):
             v = repr(v)
         lines.append(f"{key:<10} {v}")
+    if kw.get("RELAX"):
+        lines.append("RELAX")
     return "\n".join(lines) + "\n"
 
 

@@ -3,9 +3,11 @@ parity tests (test infrastructure).
 
 ``run_like_driver`` calls a chain object (the CUDA PlainChain or the
 oracle's OraclePlain) in the order of the reference driver
-(src/Main.cpp:66-180): fad(0, 0.5), updateThermo + printThermo at step 0,
-then steps with printThermo every TPI steps, and rebuilds the text of
-thermo.dat.mcs from the accumulators.
+(src/Main.cpp:66-180): fad(0, 0.5), relaxVolume when RELAX is set (NPT),
+updateThermo + printThermo at step 0, then steps with printThermo every TPI
+steps (and the rho / g prints, and relaxVolume every 10000 steps), and
+rebuilds the text of thermo.dat.mcs (and of the histogram files) from the
+accumulators.
 """
 import json
 import os
@@ -36,10 +38,13 @@ def run_like_driver(chain, kw, histograms=False):
     are set up from the created chain, as setupMCS does before fad)."""
     tpi, rhopi, gpi = kw["TPI"], kw["RHOPI"], kw["GPI"]
     nsteps = kw["NUMSTEPS"]
+    relax = bool(kw.get("RELAX")) and kw["ENSEMBLE"] == "NPT"  # setupMCS drops it for NLT
     files = {}
     if histograms:
         chain.histograms(kw["RHONB"], kw["RBW"], kw["GNS"], kw["GSW"], kw["GNB"], kw["GBW"])
     chain.fad(0, 0.5)
+    if relax:
+        chain.relax_volume()
     chain.update_thermo()
     st = chain.state()
     first = (0 - U64) % (1 << 64)  # the reference's "last print" starts at -1
@@ -55,6 +60,8 @@ def run_like_driver(chain, kw, histograms=False):
         nxt = min(nsteps, (sn // tpi + 1) * tpi)
         if histograms:
             nxt = min(nxt, (sn // rhopi + 1) * rhopi, (sn // gpi + 1) * gpi)
+        if relax:
+            nxt = min(nxt, (sn // 10000 + 1) * 10000)
         logs.append(chain.steps(nxt - sn, log=True))
         sn = nxt
         if sn % tpi == 0:
@@ -69,6 +76,8 @@ def run_like_driver(chain, kw, histograms=False):
             for k, row in enumerate(chain.take_g()):
                 gtx[k].append(thermo.g_line(sn, row, sn - slg, kw["GSW"], kw["GBW"]))
             slg = sn
+        if relax and sn % 10000 == 0 and sn < 1000000:  # src/Main.cpp:173-176
+            chain.relax_volume()
     if histograms:
         files["rho.dat.mcs"] = "".join(rho)
         for k, lines in enumerate(gtx):
@@ -83,6 +92,15 @@ def reference_histogram_files(kw, ref):
     for k in range(kw["GNS"]):
         out[f"g{k}.dat.mcs"] = str(ref["g_files"][k])
     return out
+
+
+def unrelaxed_steps(kw, n):
+    """Mask of steps 1..n whose per-step record is not followed by a
+    relaxVolume (RELAX, NPT: every 10000 steps below 10^6)."""
+    sn = np.arange(1, n + 1)
+    if kw.get("RELAX") and kw["ENSEMBLE"] == "NPT":
+        return ~((sn % 10000 == 0) & (sn < 1000000))
+    return np.ones(n, dtype=bool)
 
 
 def bits(a):

@@ -36,6 +36,9 @@ SIGS = {
     "jmmo_plain_take_rho": ([vp, P(i32), u64], C.c_int),
     "jmmo_plain_take_g": ([vp, P(i32), u64], C.c_int),
     "jmmo_plain_hist_counts": ([vp, P(i32), u64, P(i32), u64], C.c_int),
+    "jmmo_plain_trial_volume_energy": ([vp, dbl], dbl),
+    "jmmo_plain_move_volume": ([vp, dbl], C.c_int),
+    "jmmo_plain_relax_volume": ([vp, vp, P(i32)], C.c_int),
     "jmmo_philox_raw": ([P(u32), P(u32), P(u32)], None),
     "jmmo_step_words_export": ([u64, u64, u32, P(u32)], None),
 }
@@ -169,6 +172,18 @@ class OraclePlain:
         out = np.empty(gns * gnb, dtype=np.int32)
         _ok(self.lib.jmmo_plain_take_g(self._h, out.ctypes.data_as(P(i32)), out.size), "take_g")
         return out.reshape(gns, gnb)
+
+    def relax_volume(self):
+        log = (abi.RelaxStep * 20)()
+        n = C.c_int32()
+        conv = self.lib.jmmo_plain_relax_volume(self._h, C.cast(log, C.c_void_p), C.byref(n))
+        return np.frombuffer(log, dtype=np.dtype(abi.RELAX_STEP_DTYPE))[:n.value].copy(), bool(conv)
+
+    def trial_volume_energy(self, dl):
+        return self.lib.jmmo_plain_trial_volume_energy(self._h, dl)
+
+    def move_volume(self, l):
+        _ok(self.lib.jmmo_plain_move_volume(self._h, l), "move_volume")
 
     def hist_counts(self):
         rhonb, gns, gnb = self._hist

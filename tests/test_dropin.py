@@ -56,6 +56,8 @@ def test_dropin_writes_the_reference_files(gpu, name, tmp_path):
             a, b = a.split("\t")[:-2], b.split("\t")[:-2]
         assert a == b
     assert (run / "config.dat.mcs").read_text() == str(ref["config_file"])
+    for fn, text in gc.reference_histogram_files(kw, ref).items():
+        assert (run / fn).read_text() == text, fn
     tail = str(ref["stdout_tail"]).splitlines()
     e_line = [t for t in tail if t.startswith("E = ")][0]
     assert e_line in out.stdout

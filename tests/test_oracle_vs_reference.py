@@ -26,8 +26,14 @@ def test_oracle_replays_reference(name):
     # step 0 is the driver's fad(0, 0.5)
     np.testing.assert_array_equal(log["nm"], ref["nm"][1:])
     np.testing.assert_array_equal(gc.bits(log["rn"]), gc.bits(ref["rn"][1:]))
+    # a step of relaxVolume (RELAX, every 10000 steps) follows the step's own
+    # record; the reference logs after it: compare the final state there
+    keep = gc.unrelaxed_steps(kw, len(log))
+    st_end = chain.state()
+    for q, v in (("e", st_end.tot[0]), ("vir", st_end.tot[1]), ("l", st_end.l)):
+        assert gc.bits(np.array([v]))[0] == gc.bits(ref[q][-1:])[0], q
     for q in ("e", "vir", "l") + (() if harmonic else ("hv",)):
-        diff = np.nonzero(gc.bits(log[q]) != gc.bits(ref[q][1:]))[0]
+        diff = np.nonzero((gc.bits(log[q]) != gc.bits(ref[q][1:])) & keep)[0]
         assert diff.size == 0, f"{q} differs first at step {diff[0] + 1}"
     acc = (log["outcome"] == 2).astype(np.int8)
     np.testing.assert_array_equal(acc, ref["accepted"][1:])

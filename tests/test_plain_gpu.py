@@ -24,8 +24,14 @@ def test_plain_gpu_replays_reference(gpu, name):
     log, text = gc.run_like_driver(chain, kw)
     harmonic = kw["POT"] == "HARMONIC"
     np.testing.assert_array_equal(log["nm"], ref["nm"][1:])
+    # a step of relaxVolume (RELAX, every 10000 steps) follows the step's own
+    # record; the reference logs after it: compare the final state there
+    keep = gc.unrelaxed_steps(kw, len(log))
+    st_end = chain.state()
+    for q, v in (("e", st_end.tot[0]), ("vir", st_end.tot[1]), ("l", st_end.l)):
+        assert gc.bits(np.array([v]))[0] == gc.bits(ref[q][-1:])[0], q
     for q in ("e", "vir", "l") + (() if harmonic else ("hv",)):
-        diff = np.nonzero(gc.bits(log[q]) != gc.bits(ref[q][1:]))[0]
+        diff = np.nonzero((gc.bits(log[q]) != gc.bits(ref[q][1:])) & keep)[0]
         if diff.size:
             k = diff[0]
             pytest.fail(f"{q} differs first at step {k + 1}: gpu {log[q][k]!r} ref {ref[q][k + 1]!r}"
@@ -143,3 +149,50 @@ def test_plain_gpu_direct_moves_match_oracle(gpu):
         rg, ro = g.move(kind, nm, rn), o.move(kind, nm, rn)
         assert rg.outcome == ro.outcome and rg.e == ro.e and rg.l == ro.l, k
     np.testing.assert_array_equal(gc.bits(g.positions()), gc.bits(o.positions()))
+
+
+@pytest.mark.parametrize("name", gc.case_names())
+def test_plain_gpu_histogram_files_equal_reference(gpu, name):
+    """fgrho/ugrho/qagrho on the GPU: rho.dat.mcs and g<k>.dat.mcs built from
+    the GPU's counts equal the reference's files byte for byte."""
+    kw, params, ref = gc.load_case(name)
+    chain = PlainChain(params)
+    _, _, files = gc.run_like_driver(chain, kw, histograms=True)
+    theirs = gc.reference_histogram_files(kw, ref)
+    assert sorted(files) == sorted(theirs)
+    for fn, text in theirs.items():
+        assert files[fn] == text, fn
+
+
+HIST = (50, 3.0, 5, 25.0, 40, 0.1)  # rhonb, rbw, gns, gsw, gnb, gbw
+
+
+@pytest.mark.parametrize("cfg", [
+    # qavLJ volume moves recount and accumulate (the reference aborts there)
+    dict(n=40, potential=abi.JMM_POT_LJ, nbn=-1, ensemble=abi.JMM_NPT, p=1.0, t=1.2,
+         max_step=0.4, max_dl=2.0, seed=31, eci=0),
+    # wall rejections accumulate too: a narrow box and wide steps
+    dict(n=60, l=70.0, t=2.0, cutoff=3.0, max_step=2.5, seed=6, eci=0),
+])
+def test_plain_gpu_histograms_match_oracle(gpu, cfg):
+    params = abi.make_params(**cfg)
+    g, o = PlainChain(params), oracle_lib.OraclePlain(params)
+    for c in (g, o):
+        c.histograms(*HIST)
+        c.fad()
+    for chunk in (1, 5, 700, 3000):
+        g.steps(chunk)
+        o.steps(chunk)
+        for a, b in zip(g.hist_counts(), o.hist_counts()):
+            np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(g.take_rho(), o.take_rho())
+        np.testing.assert_array_equal(g.take_g(), o.take_g())
+    rng = np.random.default_rng(9)
+    for k in range(200):  # direct moves (qad2 / qavLJ / fav outside Step)
+        kind = (abi.JMM_KIND_VOLUME if (k % 9 == 0 and cfg.get("ensemble") == abi.JMM_NPT)
+                else abi.JMM_KIND_DISPLACEMENT)
+        nm, rn = int(rng.integers(0, cfg["n"])), float(rng.random())
+        g.move(kind, nm, rn)
+        o.move(kind, nm, rn)
+    np.testing.assert_array_equal(g.take_rho(), o.take_rho())
+    np.testing.assert_array_equal(g.take_g(), o.take_g())
