@@ -305,6 +305,15 @@ int jmm_batch_device_views(jmm_batch *b, void **positions, void **results,
  * writes the chosen lanes_per_chain, steps_per_round and chains_per_block. */
 int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t *lanes_per_chain,
                        uint32_t *steps_per_round, uint32_t *chains_per_block);
+/* Step-size adjustment on the device, enqueued on the batch's stream
+ * (maxDisAdjust / maxDVAdjust, src/jmmMCState.cpp:2100-2139, per chain from
+ * its counts since creation or the last reset): what = 1 displacement,
+ * 2 volume, 3 both; the next run uses the new sizes.  A linear volume step
+ * keeps the reference's clamps in units of N, an ln L step stays in
+ * [1e-4, 1]. */
+int jmm_batch_adjust_steps(jmm_batch *b, double ideal_ratio, int32_t what);
+/* The current maximum displacement and volume step of every chain. */
+int jmm_batch_step_sizes(jmm_batch *b, double *max_step, double *vol_step, uint32_t n_chains);
 int jmm_batch_destroy(jmm_batch *b);
 
 /* ---- energy gradients (the backward of U) ------------------------------ */

@@ -30,6 +30,8 @@ _native.register({
     "jmm_batch_run_host": [P(abi.BatchConfig), P(abi.ChainDesc), C.c_uint32, P(C.c_float),
                            C.c_uint64, P(abi.ChainResult), P(C.c_float)],
     "jmm_rng_words": [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint64, P(C.c_uint32)],
+    "jmm_batch_adjust_steps": [C.c_void_p, C.c_double, C.c_int32],
+    "jmm_batch_step_sizes": [C.c_void_p, P(C.c_double), P(C.c_double), C.c_uint32],
 })
 
 
@@ -89,6 +91,19 @@ class ChainBatch:
 
     def reset_stats(self):
         _native.call("jmm_batch_reset_stats", self._h)
+
+    def adjust_steps(self, ideal_ratio=0.5, displacement=True, volume=True):
+        """maxDisAdjust / maxDVAdjust on the device from each chain's counts."""
+        what = (1 if displacement else 0) | (2 if volume else 0)
+        _native.call("jmm_batch_adjust_steps", self._h, ideal_ratio, what)
+
+    def step_sizes(self):
+        """(max displacement, volume step) per chain, float64 arrays."""
+        ms = np.empty(self.n_chains, dtype=np.float64)
+        vs = np.empty(self.n_chains, dtype=np.float64)
+        _native.call("jmm_batch_step_sizes", self._h, ms.ctypes.data_as(P(C.c_double)),
+                     vs.ctypes.data_as(P(C.c_double)), self.n_chains)
+        return ms, vs
 
     def positions(self, chain):
         n = self.chains[chain].n

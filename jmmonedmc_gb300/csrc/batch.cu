@@ -123,8 +123,28 @@ static void batch_free(jmm_batch *b) {
 }
 
 // Per-chain kernel parameters for launch shape (g, spr, cpb); uploads them.
+// Step sizes changed on the device (jmm_batch_adjust_steps) back into the
+// chain descriptions, so that a new layout keeps them.
+static int sync_step_sizes(jmm_batch *b) {
+  if (b->params.empty() || !b->d_params) return JMM_OK;
+  std::vector<ChainParams> cur(b->params.size());
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  JMM_CUDA(cudaMemcpy(cur.data(), b->d_params, cur.size() * sizeof(ChainParams),
+                      cudaMemcpyDeviceToHost));
+  for (const ChainParams &P : cur) {
+    jmm_chain_desc &c = b->chains[P.id];
+    c.max_step = 0.5 * (double)P.two_max_step;
+    c.vol_step = (double)P.vol_step;
+  }
+  return JMM_OK;
+}
+
 static int apply_layout(jmm_batch *b, uint32_t g, uint32_t spr, uint32_t cpb) {
   const bool per = b->cfg.boundary == JMM_BOUNDARY_PERIODIC;
+  {
+    const int rc = sync_step_sizes(b);
+    if (rc) return rc;
+  }
   const bool exact = b->cfg.precision == JMM_PREC_EXACT;
   if (!pick_kernel(g, spr, false, JMM_POT_LJCUT, false))
     return fail(JMM_ERR_INVALID, "unsupported launch shape: lanes_per_chain x steps_per_round "
@@ -466,6 +486,69 @@ extern "C" int jmm_batch_reset_stats(jmm_batch *b) {
   JMM_CUDA(cudaGetLastError());
   JMM_CUDA(cudaMemsetAsync(b->d_gstats, 0, b->n_chains * sizeof(jmm_grad_stats), b->stream));
   JMM_CUDA(cudaStreamSynchronize(b->stream));
+  return JMM_OK;
+}
+
+// maxDisAdjust / maxDVAdjust (src/jmmMCState.cpp:2100-2139) per chain, from
+// the chain's counts since creation or the last reset: the step is scaled by
+// ln(0.672924 ideal + 0.0644284) / ln(0.672924 (actual + 0.0644284)), the
+// displacement clamped to [0.002, 0.5]; a linear volume step (max dL) to
+// [0.002 N, 0.1 N] with values above 0.1 N set to 0.5 N as the reference
+// does; an ln L step to [1e-4, 1].
+__global__ void adjust_steps_kernel(ChainParams *prm, const jmm_chain_result *res, uint32_t n_chains,
+                                    double ideal, int32_t what, int32_t vol_move) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_chains) return;
+  ChainParams P = prm[k];
+  const jmm_chain_result &r = res[P.id];
+  const double num = log(__dadd_rn(__dmul_rn(0.672924, ideal), 0.0644284));
+  if ((what & 1) && r.disp_att > 0) {
+    const double actual = __ddiv_rn((double)r.disp_acc, (double)r.disp_att);
+    double ms = __ddiv_rn(__dmul_rn(__dmul_rn(0.5, (double)P.two_max_step), num),
+                          log(__dmul_rn(0.672924, __dadd_rn(actual, 0.0644284))));
+    ms = ms < 0.002 ? 0.002 : (ms > 0.5 ? 0.5 : ms);
+    P.two_max_step = (float)__dmul_rn(2.0, ms);
+  }
+  if ((what & 2) && P.ensemble == JMM_NPT && r.vol_att > 0) {
+    const double actual = __ddiv_rn((double)r.vol_acc, (double)r.vol_att);
+    double vs = __ddiv_rn(__dmul_rn((double)P.vol_step, num),
+                          log(__dmul_rn(0.672924, __dadd_rn(actual, 0.0644284))));
+    if (vol_move == JMM_VOLMOVE_LINEAR) {
+      const double nd = (double)P.n;
+      if (vs < __dmul_rn(0.002, nd))
+        vs = __dmul_rn(0.002, nd);
+      else if (vs > __dmul_rn(0.10, nd))
+        vs = __dmul_rn(0.50, nd);
+    } else {
+      vs = vs < 1e-4 ? 1e-4 : (vs > 1.0 ? 1.0 : vs);
+    }
+    P.vol_step = (float)vs;
+  }
+  prm[k] = P;
+}
+
+extern "C" int jmm_batch_adjust_steps(jmm_batch *b, double ideal_ratio, int32_t what) {
+  clear_error();
+  JMM_CHECK_ARG(b, "null handle");
+  JMM_CHECK_ARG(ideal_ratio > 0 && ideal_ratio < 1, "ideal_ratio must be in (0, 1)");
+  JMM_CHECK_ARG(what >= 1 && what <= 3, "what: 1 displacement, 2 volume, 3 both");
+  adjust_steps_kernel<<<(b->n_chains + 255) / 256, 256, 0, b->stream>>>(
+      b->d_params, b->d_res, b->n_chains, ideal_ratio, what, b->cfg.vol_move);
+  JMM_CUDA(cudaGetLastError());
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_step_sizes(jmm_batch *b, double *max_step, double *vol_step,
+                                    uint32_t n_chains) {
+  clear_error();
+  JMM_CHECK_ARG(b && max_step && vol_step, "null argument");
+  JMM_CHECK_ARG(n_chains == b->n_chains, "n_chains does not match the batch");
+  const int rc = sync_step_sizes(b);
+  if (rc) return rc;
+  for (uint32_t k = 0; k < n_chains; ++k) {
+    max_step[k] = b->chains[k].max_step;
+    vol_step[k] = b->chains[k].vol_step;
+  }
   return JMM_OK;
 }
 

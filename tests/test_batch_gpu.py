@@ -198,3 +198,42 @@ def test_uneven_batch_at_full_size(gpu):
         e64 = oracle_lib.energy64(chains[k], x, res["l"][k])
         assert abs(fresh[k] - e64) <= 1e-6 * max(1.0, abs(e64)), (k, fresh[k], e64)
         assert np.all(np.diff(x) > 0)
+
+
+def _swendsen(step, actual, ideal=0.5):
+    """maxDisAdjust's rescale (src/jmmMCState.cpp:2100-2116)."""
+    return step * np.log(0.672924 * ideal + 0.0644284) / np.log(0.672924 * (actual + 0.0644284))
+
+
+def test_step_adjust_on_device(gpu):
+    """jmm_batch_adjust_steps applies the reference's rescale per chain from its
+    counts (checked against the same formula on the host), keeps the
+    reference's clamps, and equilibration with it moves every chain's
+    displacement acceptance toward 1/2."""
+    chains = [abi.make_chain(128, ensemble=abi.JMM_NPT, rho=0.6, t=t, p=1.0, cutoff=3.0,
+                             max_step=ms, vol_step=0.05)
+              for t, ms in zip(np.linspace(0.6, 2.0, 64), np.tile([0.05, 0.3, 2.0, 0.001], 16))]
+    b = ChainBatch(abi.make_batch_config(seed=4), chains)
+    b.run(20)
+    r = b.results()
+    ms0, vs0 = b.step_sizes()
+    b.adjust_steps()
+    ms1, vs1 = b.step_sizes()
+    want = np.clip(_swendsen(ms0, r["disp_acc"] / r["disp_att"]), 0.002, 0.5)
+    np.testing.assert_allclose(ms1, want.astype(np.float32).astype(np.float64) * 1.0, rtol=1e-6)
+    want_v = np.clip(_swendsen(vs0, r["vol_acc"] / r["vol_att"]), 1e-4, 1.0)
+    np.testing.assert_allclose(vs1, want_v, rtol=1e-6)
+    # equilibration: adjust every 20 sweeps from the counts of the last window
+    for _ in range(15):
+        b.reset_stats()
+        b.run(20)
+        b.adjust_steps()
+    b.reset_stats()
+    b.run(50)
+    r = b.results()
+    acc = r["disp_acc"] / r["disp_att"]
+    assert np.all((acc > 0.3) & (acc < 0.75)), (acc.min(), acc.max())
+    # a new launch layout keeps the adjusted sizes
+    ms2, _ = b.step_sizes()
+    b.autotune(trial_sweeps=2)
+    np.testing.assert_array_equal(b.step_sizes()[0], ms2)
