@@ -209,7 +209,7 @@ def test_step_adjust_on_device(gpu):
     """jmm_batch_adjust_steps applies the reference's rescale per chain from its
     counts (checked against the same formula on the host), keeps the
     reference's clamps, and equilibration with it moves every chain's
-    displacement acceptance toward 1/2."""
+    displacement acceptance toward 1/2 (or its step to the 0.5 ceiling)."""
     chains = [abi.make_chain(128, ensemble=abi.JMM_NPT, rho=0.6, t=t, p=1.0, cutoff=3.0,
                              max_step=ms, vol_step=0.05)
               for t, ms in zip(np.linspace(0.6, 2.0, 64), np.tile([0.05, 0.3, 2.0, 0.001], 16))]
@@ -232,7 +232,11 @@ def test_step_adjust_on_device(gpu):
     b.run(50)
     r = b.results()
     acc = r["disp_acc"] / r["disp_att"]
-    assert np.all((acc > 0.3) & (acc < 0.75)), (acc.min(), acc.max())
+    ms_end, _ = b.step_sizes()
+    # hot chains reach the reference's 0.5 ceiling with acceptance still high
+    capped = ms_end >= np.float32(0.5)
+    assert np.all(((acc > 0.3) & (acc < 0.75)) | (capped & (acc >= 0.3))), (acc, ms_end)
+    assert np.sum(~capped) >= 8
     # a new launch layout keeps the adjusted sizes
     ms2, _ = b.step_sizes()
     b.autotune(trial_sweeps=2)
