@@ -132,14 +132,54 @@ def run_case(name, overrides):
     return dict(name=name, input=kw, steps=len(steps) - 1)
 
 
+# Restarts: a fresh run to NUMSTEPS, then the same INPUT with RESTART TRUE and
+# a larger NUMSTEPS in the same directory (the reference resumes from the
+# last complete frame of config.dat.mcs, src/jmmMCState.cpp:572-765).  The
+# fixture holds both INPUT files and every output file after the restart.
+RESTARTS = {
+    "restart_nlt64": (dict(NUMSTEPS=2000), 4000),
+    "restart_npt32": (dict(ENSEMBLE="NPT", N=32, P=1.5, T=1.2, MAXDV=1.0, SEED=23,
+                           NUMSTEPS=3000, ENGCHECK=700), 5000),
+}
+
+
+def run_restart_case(name, overrides, numsteps2):
+    kw = dict(BASE)
+    kw.update(overrides)
+    first = input_text(kw)
+    second = "RESTART    TRUE\n" + input_text(dict(kw, NUMSTEPS=numsteps2))
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    with tempfile.TemporaryDirectory() as tmp:
+        for text in (first, second):
+            with open(os.path.join(tmp, "INPUT"), "w") as f:
+                f.write(text)
+            out = subprocess.run([HARNESS, "steps.bin", "final.bin"], cwd=tmp, env=env,
+                                 check=True, capture_output=True, text=True)
+        files = {}
+        names = ["thermo.dat.mcs", "config.dat.mcs", "rho.dat.mcs"]
+        names += [f"g{k}.dat.mcs" for k in range(kw["GNS"])]
+        for fn in names:
+            with open(os.path.join(tmp, fn)) as f:
+                files[fn] = f.read()
+    np.savez_compressed(
+        os.path.join(HERE, name + ".npz"),
+        input_first=np.array(first), input_restart=np.array(second),
+        file_names=np.array(names), file_texts=np.array([files[fn] for fn in names]),
+        stdout_tail=np.array("\n".join(out.stdout.splitlines()[-4:])),
+    )
+    return dict(name=name, input=kw, restart_numsteps=numsteps2)
+
+
 def main():
     build_reference()
     index = [run_case(name, over) for name, over in CASES.items()]
+    restarts = [run_restart_case(name, over, n2) for name, (over, n2) in RESTARTS.items()]
     with open(os.path.join(HERE, "index.json"), "w") as f:
         json.dump(dict(generator="tests/golden/make_golden.py",
                        rng="Philox4x32-10, one block per step (oracle/philox.h)",
-                       cases=index), f, indent=1)
+                       cases=index, restarts=restarts), f, indent=1)
     print("\n".join(f"{c['name']}: {c['steps']} steps" for c in index))
+    print("\n".join(f"{c['name']}: restart to {c['restart_numsteps']}" for c in restarts))
 
 
 if __name__ == "__main__":

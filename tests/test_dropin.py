@@ -4,9 +4,16 @@
   and readInput.cpp, compiled against the reference's own jmmMCState.h,
   link against the drop-in and libjmmgpu.so (the interface is the same).
 * GPU: a driver with the reference driver's call sequence runs the golden
-  INPUT files through the drop-in; thermo.dat.mcs and config.dat.mcs must
-  equal the reference's own files byte for byte, and the final energy and
-  acceptance lines its stdout.
+  INPUT files through the drop-in; thermo.dat.mcs, config.dat.mcs,
+  rho.dat.mcs and g<k>.dat.mcs must equal the reference's own files byte for
+  byte, and the final energy and acceptance lines its stdout.
+* GPU, restart: a fresh run, then RESTART TRUE with more steps in the same
+  directory.  config, rho and g files equal the reference's byte for byte;
+  of thermo.dat.mcs the lines after the restart step must equal the
+  reference's (the reference's thermo restart reads an uninitialised step
+  number, src/jmmMCState.cpp:575 and :747-752, and with the value it had
+  here wrote its new lines over the start of the file; the drop-in keeps
+  the lines up to the restart step and appends).
 """
 import os
 import subprocess
@@ -63,3 +70,48 @@ def test_dropin_writes_the_reference_files(gpu, name, tmp_path):
     assert e_line in out.stdout
     acc = tail[-1].strip()
     assert acc in out.stdout
+
+
+def _restart_cases():
+    import json
+    with open(os.path.join(gc.HERE, "index.json")) as f:
+        return [c["name"] for c in json.load(f).get("restarts", [])]
+
+
+def _thermo_after(text, sn):
+    out = []
+    for line in text.splitlines():
+        head = line.split("\t", 1)[0]
+        if head.isdigit() and int(head) > sn:
+            out.append(line)
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", _restart_cases())
+def test_dropin_restart_matches_reference(gpu, name, tmp_path):
+    from jmmonedmc_gb300 import inputfile
+    exe = _build_driver(str(tmp_path))
+    z = np.load(os.path.join(gc.HERE, name + ".npz"), allow_pickle=False)
+    first = str(z["input_first"])
+    sn = inputfile.parse_text(first)["NUMSTEPS"]
+    run = tmp_path / "run"
+    run.mkdir()
+    outs = []
+    for text in (first, str(z["input_restart"])):
+        (run / "INPUT").write_text(text)
+        out = subprocess.run([exe], cwd=run, capture_output=True, text=True, timeout=300,
+                             env=dict(os.environ, OMP_NUM_THREADS="1"))
+        assert out.returncode == 0, out.stderr
+        outs.append(out.stdout)
+    for fn, text in zip(z["file_names"], z["file_texts"]):
+        ours = (run / str(fn)).read_text()
+        if str(fn) == "thermo.dat.mcs":
+            assert _thermo_after(ours, sn) == _thermo_after(str(text), sn)
+            assert len(_thermo_after(ours, sn)) > 0
+        else:
+            assert ours == str(text), fn
+    tail = str(z["stdout_tail"]).splitlines()
+    e_line = [t for t in tail if t.startswith("E = ")][0]
+    assert e_line in outs[1]
+    assert tail[-1].strip() in outs[1]
