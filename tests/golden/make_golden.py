@@ -61,6 +61,10 @@ CASES = {
     # dense NPT start (L = N) with a wide volume step: many volume moves
     "npt32_ljcut_wide": dict(ENSEMBLE="NPT", N=32, P=2.0, T=1.5, MAXDV=2.0,
                              SEED=99, NUMSTEPS=4000, ENGCHECK=250),
+    # maxDisAdjust / maxDVAdjust every 500 / 600 steps from a small step and a
+    # wide volume step
+    "npt48_ljcut_adjust": dict(ENSEMBLE="NPT", N=48, P=1.0, T=1.1, MAXSTEP=0.05, MAXDV=3.0,
+                               SEED=57, NUMSTEPS=4000, ENGCHECK=800, DADJ=500, VADJ=600),
     # RELAX (as the reference's test/INPUT): relaxVolume after the step-0 fad
     # and again at step 10000
     "npt32_ljcut_relax": dict(ENSEMBLE="NPT", N=32, P=1.0, T=1.0, MAXDV=1.0, SEED=41,

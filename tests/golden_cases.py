@@ -10,6 +10,7 @@ rebuilds the text of thermo.dat.mcs (and of the histogram files) from the
 accumulators.
 """
 import json
+import math
 import os
 
 import numpy as np
@@ -32,13 +33,52 @@ def load_case(name):
     return kw, inputfile.to_params(kw), data
 
 
+class Adjuster:
+    """maxDisAdjust / maxDVAdjust (src/jmmMCState.cpp:2100-2139): Swendsen's
+    rescale of the step toward half acceptance from the cumulative counts,
+    in the reference's operand order; the volume one only when new volume
+    trials have been made since its last change (its static counter)."""
+
+    def __init__(self, kw):
+        self.max_step = float(kw["MAXSTEP"])
+        self.max_dl = float(kw["MAXDV"])
+        self.n = int(kw["N"])
+        self.v_seen = 0
+
+    def displacement(self, chain):
+        st = chain.state()
+        actual = float(st.d_acc[0]) / (st.d_acc[0] + st.d_acc[1])
+        ms = self.max_step * math.log(0.672924 * 0.5 + 0.0644284) / math.log(
+            0.672924 * (actual + 0.0644284))
+        self.max_step = 0.002 if ms < 0.002 else (0.5 if ms > 0.5 else ms)
+        chain.set_step_sizes(self.max_step, self.max_dl)
+
+    def volume(self, chain):
+        st = chain.state()
+        tot = st.v_acc[0] + st.v_acc[1]
+        if tot - self.v_seen <= 0:
+            return
+        self.v_seen = tot
+        actual = float(st.v_acc[0]) / tot
+        md = self.max_dl * math.log(0.672924 * 0.5 + 0.0644284) / math.log(
+            0.672924 * (actual + 0.0644284))
+        if md < 0.002 * self.n:
+            md = 0.002 * self.n
+        elif md > 0.10 * self.n:
+            md = 0.50 * self.n
+        self.max_dl = md
+        chain.set_step_sizes(self.max_step, self.max_dl)
+
+
 def run_like_driver(chain, kw, histograms=False):
     """Returns (per-step log, thermo file text), and with histograms=True
     also {file name: text} of rho.dat.mcs and g<k>.dat.mcs (the histograms
     are set up from the created chain, as setupMCS does before fad)."""
     tpi, rhopi, gpi = kw["TPI"], kw["RHOPI"], kw["GPI"]
+    dadj, vadj = kw["DADJ"], kw["VADJ"]
     nsteps = kw["NUMSTEPS"]
     relax = bool(kw.get("RELAX")) and kw["ENSEMBLE"] == "NPT"  # setupMCS drops it for NLT
+    adjust = Adjuster(kw)
     files = {}
     if histograms:
         chain.histograms(kw["RHONB"], kw["RBW"], kw["GNS"], kw["GSW"], kw["GNB"], kw["GBW"])
@@ -62,6 +102,7 @@ def run_like_driver(chain, kw, histograms=False):
             nxt = min(nxt, (sn // rhopi + 1) * rhopi, (sn // gpi + 1) * gpi)
         if relax:
             nxt = min(nxt, (sn // 10000 + 1) * 10000)
+        nxt = min(nxt, (sn // dadj + 1) * dadj, (sn // vadj + 1) * vadj)
         logs.append(chain.steps(nxt - sn, log=True))
         sn = nxt
         if sn % tpi == 0:
@@ -72,6 +113,10 @@ def run_like_driver(chain, kw, histograms=False):
         if histograms and sn % rhopi == 0:
             rho.append(thermo.rho_line(sn, chain.take_rho(), sn - slrho, kw["RBW"]))
             slrho = sn
+        if sn % dadj == 0:
+            adjust.displacement(chain)
+        if sn % vadj == 0:
+            adjust.volume(chain)
         if histograms and sn % gpi == 0:
             for k, row in enumerate(chain.take_g()):
                 gtx[k].append(thermo.g_line(sn, row, sn - slg, kw["GSW"], kw["GBW"]))
