@@ -618,6 +618,8 @@ def run_ours(args, rank, world, local_rank):
     h2d = n_tot * 4 + args.chains * C.sizeof(abi.ChainDesc) + C.sizeof(abi.BatchConfig)
     d2h = n_tot * 4 + args.chains * C.sizeof(abi.ChainResult)
 
+    plain = plain_rate(chains[0], args) if args.workload == "npt" and rank == 0 else None
+
     launch_ms = total_ms / args.steps
     flop_per_launch = pairs / args.steps * FLOP_PER_PAIR
     achieved = flop_per_launch / (launch_ms * 1e-3) / 1e12
@@ -662,7 +664,32 @@ def run_ours(args, rank, world, local_rank):
     }
     if cpu is not None:
         line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if plain is not None:
+        line["plain"] = plain
     return line
+
+
+def plain_rate(chain, args, steps=20000):
+    """The plain FP64 form (the reference's algorithm on the GPU, one chain)
+    on the workload's first chain: attempted moves/s, beside the batched
+    rate.  The plain form runs the reference's move set: linear dL volume
+    moves (max dL = delta L) drawn with probability 1/(N+1) per step."""
+    from jmmonedmc_gb300 import abi
+    from jmmonedmc_gb300.plain import PlainChain
+    n = int(chain.n)
+    params = abi.make_params(n=n, ensemble=abi.JMM_NPT, potential=abi.JMM_POT_LJCUT, p=chain.p,
+                             t=chain.t, cutoff=3.0, max_step=0.3, max_dl=0.01 * n / 0.6,
+                             seed=args.seed, eci=0)
+    c = PlainChain(params)
+    c.fad()
+    c.steps(1000)
+    t0 = time.perf_counter()
+    c.steps(steps)
+    dt = time.perf_counter() - t0
+    c.close()
+    return {"value": steps / dt, "unit": UNIT, "particles": n, "steps": steps,
+            "how": "jmm_plain_steps on one chain of the workload (FP64, per-pair state, the "
+                   "reference's step for step), wall clock around the synchronous call"}
 
 
 # ---- the reference arm -----------------------------------------------------------
