@@ -26,7 +26,9 @@
 //    the per-step accumulators (sum E, E^2, L, L^2, LE, rho, rho^2).
 // Every FP32/FP64 operation is an explicit round-to-nearest intrinsic so
 // that the EXACT precision mode can be replayed bit for bit by the oracle;
-// the FAST mode differs only in using the hardware reciprocal and exp.
+// the FAST mode differs in using the hardware reciprocal, exp and log, and
+// in summing a round's per-step statistics by a scan over its slots instead
+// of step by step (the same quantities, rounded in another order).
 #pragma once
 #include <math.h>
 #include <stdint.h>
@@ -233,10 +235,12 @@ __device__ __forceinline__ float pair_energy_h(float d2, const Hot &H) {
 }
 
 // The Metropolis threshold -ln u, u the midpoint of the 23-bit cell of w
-// (exact in FP32, strictly inside (0, 1)).
+// (exact in FP32, strictly inside (0, 1)); the portable log in EXACT
+// precision, the hardware one otherwise.
+template <bool kExact>
 __device__ __forceinline__ float threshold_of(uint32_t w) {
   const float u = __fmul_rn(__fadd_rn((float)(w >> 9), 0.5f), 1.1920929e-07f);  // 2^-23
-  return -portable_logf(u);
+  return kExact ? -portable_logf(u) : -__logf(u);
 }
 
 // Neighbour index of window lane (side, k), clamped for loads, and its
@@ -366,7 +370,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
         float md_e = __fmul_rn(__fsub_rn(u1, 0.5f), H.two_max_step);
         if (HALO) md_e = __fmul_rn(rintf(__fmul_rn(md_e, inv_grid)), P.grid);  // exact: 2^k scales
         ring_md[e] = nm_e == n ? u1 : md_e;
-        ring_thr[e] = threshold_of(w.w[2]);
+        ring_thr[e] = threshold_of<kExact>(w.w[2]);
       }
       __syncwarp(gmask);
       ring_valid = true;
@@ -528,14 +532,36 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
         }
       }
       const float de_acc = acc ? de : 0.0f;
+      if (kExact || S == 1) {
+        // step by step, the order the oracle replays
 #pragma unroll
-      for (int s2 = 0; s2 < S; ++s2) {
-        const float d_s = __shfl_sync(gmask, de_acc, s2 * G, L);
-        if ((uint32_t)s2 < f) {
-          g.delta = __fadd_rn(g.delta, d_s);
-          g.sd = __fadd_rn(g.sd, g.delta);
-          g.sd2 = __fmaf_rn(g.delta, g.delta, g.sd2);
+        for (int s2 = 0; s2 < S; ++s2) {
+          const float d_s = __shfl_sync(gmask, de_acc, s2 * G, L);
+          if ((uint32_t)s2 < f) {
+            g.delta = __fadd_rn(g.delta, d_s);
+            g.sd = __fadd_rn(g.sd, g.delta);
+            g.sd2 = __fmaf_rn(g.delta, g.delta, g.sd2);
+          }
         }
+      } else {
+        // the energy change after each kept step by a scan over the slots,
+        // its sum and sum of squares by a butterfly over the slots
+        float x = de_acc;
+#pragma unroll
+        for (int o = 1; o < S; o <<= 1) {
+          const float y = __shfl_up_sync(gmask, x, o * G, L);
+          if (slot >= o) x = __fadd_rn(x, y);
+        }
+        const float v = (uint32_t)slot < f ? __fadd_rn(g.delta, x) : 0.0f;
+        float sv = v, sv2 = __fmul_rn(v, v);
+#pragma unroll
+        for (int o = 1; o < S; o <<= 1) {
+          sv = __fadd_rn(sv, __shfl_xor_sync(gmask, sv, o * G, L));
+          sv2 = __fadd_rn(sv2, __shfl_xor_sync(gmask, sv2, o * G, L));
+        }
+        g.delta = __fadd_rn(g.delta, __shfl_sync(gmask, x, (int)(f - 1) * G, L));
+        g.sd = __fadd_rn(g.sd, sv);
+        g.sd2 = __fadd_rn(g.sd2, sv2);
       }
       __syncwarp(gmask);
       const unsigned okbits = (__ballot_sync(gmask, ok) >> lane_shift & kChainBits);

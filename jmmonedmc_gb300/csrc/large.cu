@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(32)
     const Words4 w = step_words(cfg.seed, step0 + (uint64_t)s + 1, id);
     const int nm = (int)word_to_index(w.w[0], (uint64_t)n);
     const float md = __fmul_rn(__fsub_rn(word_to_unit_f(w.w[1]), 0.5f), H.two_max_step);
-    const float thr = threshold_of(w.w[2]);
+    const float thr = threshold_of<false>(w.w[2]);
     const int64_t qo = qc[nm];
     const int64_t qn = qo + __float2ll_rn(__fmul_rn(md, inv_grid));  // snapped to the grid
     const int64_t qj = qc[nm + side * k0];  // a padding sentinel beyond either end

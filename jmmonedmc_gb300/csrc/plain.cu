@@ -66,7 +66,7 @@ struct Args {
   uint64_t n, nn, npairs, num_trial_types;
   int32_t potential, nbn;
   int32_t use_qavlj;
-  int32_t pad;
+  int32_t stage_old;  // qad2 stages the stored pair terms in shared memory (N <= 1495)
   double cutoff, t, p;
   uint64_t seed, eci;
   // rho(x) and g(x) histograms, bins [0, rhonb) density, then gns x gnb
@@ -205,12 +205,14 @@ __device__ void full_terms(const Args &a, const double *x, bool virial, double l
   }
 }
 
-// Lanes 0..8 of warp 0: sequential sums of the scratch terms in pair order.
+// Lanes 0..8 of warp 0: sequential sums of the scratch terms in pair order
+// (unrolled so that many of the independent loads are in flight ahead of
+// the dependent adds).
 __device__ void full_sums(const Args &a, Ctl &ctl) {
   if (threadIdx.x < 9) {
     const int k = threadIdx.x;
     double s = 0.0;
-#pragma unroll 8
+#pragma unroll 32
     for (uint64_t p = 0; p < a.npairs; ++p) s = __dadd_rn(s, a.scratch[p * 9 + k]);
     ctl.sum[k] = s;
   }
@@ -375,6 +377,7 @@ __device__ void qad2(const Args &a, Ctl &ctl, double *s_new, double *s_rij, cons
   __syncthreads();
   if (ctl.wall) return;
   const double md = ctl.md, l = S->l;
+  double *s_old = s_rij + nm1;  // 9 * nm1 when a.stage_old
   for (uint64_t p = threadIdx.x; p < nm1; p += blockDim.x) {
     const uint64_t i = p < nm ? p : p + 1;
     const uint64_t lo = i < nm ? i : nm, hi = i < nm ? nm : i;
@@ -390,18 +393,31 @@ __device__ void qad2(const Args &a, Ctl &ctl, double *s_new, double *s_rij, cons
     s_rij[p] = rt;
 #pragma unroll
     for (int k = 0; k < 9; ++k) s_new[k * nm1 + p] = phi[k];
+    if (a.stage_old) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) s_old[k * nm1 + p] = a.q[k * a.nn + ind];
+    }
   }
   __syncthreads();
   if (threadIdx.x < 9) {
+    // the reference's order: (sum - old) + new, partners i < nm, then i > nm
     const int k = threadIdx.x;
-    const double *old = a.q + (uint64_t)k * a.nn;
     const double *nw = s_new + (uint64_t)k * nm1;
     double sa = 0.0, sb = 0.0;
-#pragma unroll 4
-    for (uint64_t p = 0; p < nm; ++p) sa = __dadd_rn(__dsub_rn(sa, old[p * n + nm]), nw[p]);
-#pragma unroll 4
-    for (uint64_t p = nm; p < nm1; ++p)
-      sb = __dadd_rn(__dsub_rn(sb, old[nm * n + p + 1]), nw[p]);
+    if (a.stage_old) {
+      const double *old = s_old + (uint64_t)k * nm1;
+#pragma unroll 8
+      for (uint64_t p = 0; p < nm; ++p) sa = __dadd_rn(__dsub_rn(sa, old[p]), nw[p]);
+#pragma unroll 8
+      for (uint64_t p = nm; p < nm1; ++p) sb = __dadd_rn(__dsub_rn(sb, old[p]), nw[p]);
+    } else {
+      const double *old = a.q + (uint64_t)k * a.nn;
+#pragma unroll 16
+      for (uint64_t p = 0; p < nm; ++p) sa = __dadd_rn(__dsub_rn(sa, old[p * n + nm]), nw[p]);
+#pragma unroll 16
+      for (uint64_t p = nm; p < nm1; ++p)
+        sb = __dadd_rn(__dsub_rn(sb, old[nm * n + p + 1]), nw[p]);
+    }
     ctl.sum[k] = __dadd_rn(sa, sb);
   }
   __syncthreads();
@@ -1016,7 +1032,11 @@ extern "C" int jmm_plain_create(const jmm_params *prm, jmm_plain **out) {
   a.p = prm->p;
   a.seed = prm->seed;
   a.eci = prm->eci;
-  h->smem_bytes = 10 * (n - 1) * sizeof(double);
+  // s_new (9 quantities) and s_rij per partner; and, where it fits, the
+  // stored old terms too, so that qad2's in-order sums read shared memory
+  // instead of one strided HBM load per term
+  a.stage_old = 19 * (n - 1) * sizeof(double) <= 227 * 1024 ? 1 : 0;
+  h->smem_bytes = (a.stage_old ? 19 : 10) * (n - 1) * sizeof(double);
 
   int rc = JMM_OK;
 #define ALLOC(ptr, bytes)                                               \
