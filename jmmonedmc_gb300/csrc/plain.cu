@@ -205,19 +205,12 @@ __device__ void full_terms(const Args &a, const double *x, bool virial, double l
   }
 }
 
-// The quantity an in-order FP64 sum belongs to: lane 0 of warps 0..8, one
-// warp each, so that the nine dependent add chains run on different
-// schedulers and their FP64 pipes; -1 for every other thread.
-__device__ __forceinline__ int sum_lane_quantity() {
-  return ((threadIdx.x & 31) == 0 && (threadIdx.x >> 5) < 9) ? (int)(threadIdx.x >> 5) : -1;
-}
-
-// Sequential sums of the scratch terms in pair order, one quantity per warp
+// Lanes 0..8 of warp 0: sequential sums of the scratch terms in pair order
 // (unrolled so that many of the independent loads are in flight ahead of
 // the dependent adds).
 __device__ void full_sums(const Args &a, Ctl &ctl) {
-  const int k = sum_lane_quantity();
-  if (k >= 0) {
+  if (threadIdx.x < 9) {
+    const int k = threadIdx.x;
     double s = 0.0;
 #pragma unroll 32
     for (uint64_t p = 0; p < a.npairs; ++p) s = __dadd_rn(s, a.scratch[p * 9 + k]);
@@ -406,25 +399,17 @@ __device__ void qad2(const Args &a, Ctl &ctl, double *s_new, double *s_rij, cons
     }
   }
   __syncthreads();
-  const int k = sum_lane_quantity();
-  if (k >= 0) {
-    // the reference's order: (sum - old) + new, partners i < nm (sa), then
-    // i > nm (sb); the two chains are independent and advance together
+  if (threadIdx.x < 9) {
+    // the reference's order: (sum - old) + new, partners i < nm, then i > nm
+    const int k = threadIdx.x;
     const double *nw = s_new + (uint64_t)k * nm1;
     double sa = 0.0, sb = 0.0;
     if (a.stage_old) {
       const double *old = s_old + (uint64_t)k * nm1;
-      const uint64_t na = nm, nb = nm1 - nm, both = na < nb ? na : nb;
-#pragma unroll 4
-      for (uint64_t p = 0; p < both; ++p) {
-        sa = __dadd_rn(__dsub_rn(sa, old[p]), nw[p]);
-        sb = __dadd_rn(__dsub_rn(sb, old[nm + p]), nw[nm + p]);
-      }
-#pragma unroll 4
-      for (uint64_t p = both; p < na; ++p) sa = __dadd_rn(__dsub_rn(sa, old[p]), nw[p]);
-#pragma unroll 4
-      for (uint64_t p = both; p < nb; ++p)
-        sb = __dadd_rn(__dsub_rn(sb, old[nm + p]), nw[nm + p]);
+#pragma unroll 8
+      for (uint64_t p = 0; p < nm; ++p) sa = __dadd_rn(__dsub_rn(sa, old[p]), nw[p]);
+#pragma unroll 8
+      for (uint64_t p = nm; p < nm1; ++p) sb = __dadd_rn(__dsub_rn(sb, old[p]), nw[p]);
     } else {
       const double *old = a.q + (uint64_t)k * a.nn;
 #pragma unroll 16
