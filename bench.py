@@ -55,19 +55,30 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=1.5,
                     help="wall seconds per host core for the CPU baseline sample")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--workload", choices=("npt", "uneven", "large"), default="npt",
+    ap.add_argument("--workload", choices=("npt", "uneven", "large", "grad"), default="npt",
                     help="npt: the batched NPT headline workload; uneven: 1024 chains of "
                          "N ~ U{32..2048}, rho ~ U(0.3, 0.9), LJ / soft sphere / Gaussian core, "
                          "T ~ U(0.5, 2), NVT; large: 64 chains of N = 2^20 LJ particles, "
-                         "rho 0.7, rc 2.5, T 1.2, alternating-domain sweep")
+                         "rho 0.7, rc 2.5, T 1.2, alternating-domain sweep; grad: 2048 chains "
+                         "of N = 512 LJ at rho 0.7, T 1 (half NVT, half NPT at P 1), energy "
+                         "gradient sampled every 10th sweep")
     ap.add_argument("--domain-size", type=int, default=1024,
                     help="large workload: particles per domain")
+    ap.add_argument("--sample-every", type=int, default=10,
+                    help="grad workload: sweeps between gradient samples")
     args = ap.parse_args()
     if args.workload == "uneven":
         if args.chains == 4096:
             args.chains = 1024
         if args.sweeps_per_step == 1000:
             args.sweeps_per_step = 500
+    if args.workload == "grad":
+        if args.chains == 4096:
+            args.chains = 2048
+        if args.n == 256:
+            args.n = 512
+        if args.sweeps_per_step == 1000:
+            args.sweeps_per_step = 200
     if args.workload == "large":
         if args.chains == 4096:
             args.chains = 64
@@ -104,6 +115,8 @@ def workload(args, rank=0):
     seed = args.seed + 1000003 * rank
     if args.workload == "uneven":
         return uneven_workload(args, seed)
+    if args.workload == "grad":
+        return grad_workload(args, seed)
     temps = [0.5 * 4.0 ** (c / max(1, n_ch - 1)) for c in range(n_ch)]
     press = [0.5 + 1.5 * u for u in uniforms(seed, n_ch, stream=0xB0)]
     chains = [abi.make_chain(args.n, potential=abi.JMM_POT_LJCUT, ensemble=abi.JMM_NPT,
@@ -116,6 +129,8 @@ def workload(args, rank=0):
 
 
 def config_dict(args, extra=None):
+    if args.workload == "grad":
+        return grad_config(args, extra)
     if args.workload == "uneven":
         d = {"workload": (f"uneven batch: {args.chains} chains, N ~ U{{32..2048}}, rho ~ "
                           "U(0.3,0.9), potential cycling LJ rc=3 / soft sphere rc=2.5 / Gaussian "
@@ -515,6 +530,178 @@ def run_reference_large(args):
     }
 
 
+# ---- the differentiation workload -------------------------------------------------
+
+GRAD_METRIC = ("attempted MC moves/s with the energy gradient sampled every 10th sweep "
+               "(batched chains, FP32 pairs / FP64 totals and gradient sums)")
+
+
+def grad_workload(args, seed):
+    """2048 chains of N = 512 LJ 12-6, rho 0.7, T 1: half NVT, half NPT (P 1)."""
+    from jmmonedmc_gb300 import abi
+    chains = [abi.make_chain(args.n, potential=abi.JMM_POT_LJCUT,
+                             ensemble=abi.JMM_NPT if k % 2 else abi.JMM_NLT, rho=0.7, t=1.0,
+                             p=1.0, cutoff=3.0, max_step=0.3, vol_step=0.02)
+              for k in range(args.chains)]
+    cfg = abi.make_batch_config(seed=seed, vol_move=abi.JMM_VOLMOVE_LNL,
+                                vol_schedule=abi.JMM_VOLSCHED_SWEEP, resum_sweeps=10,
+                                precision=abi.JMM_PREC_FAST)
+    return cfg, chains
+
+
+def grad_config(args, extra=None):
+    d = {"workload": (f"differentiation: {args.chains} chains x N={args.n}, LJ 12-6 eps=sigma=1 "
+                      "rc=3, rho=0.7 lattice start, T=1, half NVT and half NPT (P=1, ln L "
+                      "moves delta=0.02 once per sweep), max displacement 0.3; U, dU/deps, "
+                      f"dU/dsigma, dU/dL of every chain every {args.sample_every} sweeps"),
+         "chains": args.chains, "particles_per_chain": args.n,
+         "sweeps_per_step": args.sweeps_per_step, "sample_every": args.sample_every,
+         "l2": "flushed between timed steps (256 MiB device write)",
+         "precision": "FP32 pair energies and pair derivatives, FP64 totals, gradients and "
+                      "fluctuation sums"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def run_grad(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import ctypes as C
+
+    from jmmonedmc_gb300 import _native, build
+    if not os.path.exists(_native.lib_path()):
+        build.build_native()
+    from jmmonedmc_gb300.batch import ChainBatch
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    cfg, chains = grad_workload(args, args.seed + 1000003 * rank)
+    cpu = cpu_reference_sample(chains, args.cpu_seconds, args.seed) if rank == 0 and world == 1 \
+        else None
+    fp32_peak, rcp_peak = C.c_double(), C.c_double()
+    _native.call("jmm_measure_peaks", C.byref(fp32_peak), C.byref(rcp_peak))
+    b = ChainBatch(cfg, chains)
+    lanes, spr, cpb = (0, 0, 0) if args.no_autotune else b.autotune(trial_sweeps=3)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    S, every = args.sweeps_per_step, args.sample_every
+    for _ in range(args.warmup):
+        b.run_sampled_async(S, every, stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    b.reset_stats()
+    before = b.results()
+
+    def timed(run):
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        torch.cuda.synchronize(dev)
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            run()
+            ends[k].record(stream)
+        torch.cuda.synchronize(dev)
+        return sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    wall0 = time.perf_counter()
+    total_ms = timed(lambda: b.run_sampled_async(S, every, stream.cuda_stream))
+    if world > 1:
+        torch.distributed.barrier()
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    after = b.results()
+    gstats = b.grad_stats()
+    if np.any(after["error"] != 0):
+        raise RuntimeError(f"chain errors: {np.unique(after['error'])}")
+    moves = int((after["steps"] - before["steps"]).sum())
+    pairs = int((after["pair_evals"] - before["pair_evals"]).sum())
+    samples = int(gstats["samples"].sum())
+    # the same sweeps without the gradient samples, for the backward's share
+    plain_ms = timed(lambda: b.run_async(S, stream.cuda_stream))
+    moves_all = moves
+    if world > 1:
+        t = torch.tensor([total_ms, moves], dtype=torch.float64, device=dev)
+        tmax, tsum = t.clone(), t.clone()
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
+        total_ms, moves_all = float(tmax[0]), float(tsum[1])
+
+    # e2e: host buffers through the public API: a batch built from host
+    # positions, the sampled run, the gradient statistics and results read back
+    xs = [b.positions(k) for k in range(len(chains))]
+    lbox = after["l"].copy()
+    e2e_times, e2e_moves = [], 0
+    for _ in range(args.e2e_steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        b2 = ChainBatch(cfg, chains)
+        for k in range(len(chains)):
+            b2.set_positions(k, xs[k], float(lbox[k]))
+        b2.run_sampled(S, every)
+        r2, g2 = b2.results(), b2.grad_stats()
+        e2e_times.append(time.perf_counter() - t0)
+        e2e_moves += int(r2["steps"].sum())
+        b2.close()
+    n_tot = sum(int(c.n) for c in chains)
+    e2e = {"value": e2e_moves / sum(e2e_times) * world, "unit": UNIT,
+           "h2d_bytes_per_step": n_tot * 4 + len(chains) * 8,
+           "d2h_bytes_per_step": len(chains) * (C.sizeof(abi_result()) + C.sizeof(abi_gstats())),
+           "how": "ChainBatch from host positions (jmm_batch_create + set_positions), "
+                  "run_sampled, results and grad_stats read back, all inside the timed region"}
+    launch_ms = total_ms / args.steps
+    achieved = pairs / args.steps * FLOP_PER_PAIR / (launch_ms * 1e-3) / 1e12
+    line = {
+        "metric": GRAD_METRIC,
+        "value": moves_all / (total_ms * 1e-3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (lattice start, seeded Philox moves)",
+        "config": grad_config(args, {"lanes_per_chain": lanes, "steps_per_round": spr,
+                                     "chains_per_block": cpb, "parallelism": f"replicas{world}",
+                                     "wall_s_timed": wall}),
+        "gradient_samples_per_s": samples / (total_ms * 1e-3),
+        "without_gradients": {"value": moves / (plain_ms * 1e-3), "unit": UNIT,
+                              "how": "the same sweeps by run_async, no gradient samples"},
+        "roofline": {
+            "bound": "fp32", "achieved": achieved, "peak": fp32_peak.value, "unit": "TFLOP/s",
+            "frac": achieved / fp32_peak.value, "traffic": None,
+            "peak_source": "measured live by jmm_measure_peaks (FP32 FMA kernel; "
+                           "MEASURED_PEAKS.json holds no FP32 figure)",
+            "pair_evals_per_launch": pairs / args.steps, "flop_per_pair": FLOP_PER_PAIR,
+            "kernel": "jmm::batch::chains_kernel (the gradient kernel runs between)"},
+        "e2e": e2e,
+        "gpu_launches": args.steps * (1 + S // every),
+        "clocks": clocks,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    return line
+
+
+def abi_result():
+    from jmmonedmc_gb300 import abi
+    return abi.ChainResult
+
+
+def abi_gstats():
+    from jmmonedmc_gb300 import abi
+    return abi.GradStats
+
+
 # ---- our implementation ----------------------------------------------------------
 
 def run_ours(args, rank, world, local_rank):
@@ -711,7 +898,7 @@ def run_reference(args):
         steps_total += s["steps"]
     value = steps_total / t_total
     return {
-        "metric": METRIC,
+        "metric": GRAD_METRIC if args.workload == "grad" else METRIC,
         "value": value,
         "unit": UNIT,
         "n_gpus": args.gpus,
@@ -746,7 +933,8 @@ def main():
         import torch
         torch.cuda.set_device(local_rank)
         torch.distributed.init_process_group("nccl")
-    line = (run_large if args.workload == "large" else run_ours)(args, rank, world, local_rank)
+    runner = {"large": run_large, "grad": run_grad}.get(args.workload, run_ours)
+    line = runner(args, rank, world, local_rank)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -354,6 +354,10 @@ int jmm_batch_energy_grad(jmm_batch *b, double *out, uint32_t n_chains);
  * chain and its energy gradient are added to the chain's jmm_grad_stats (one
  * CUDA graph: chain kernel, gradient kernel, chain kernel, ...). */
 int jmm_batch_run_sampled(jmm_batch *b, uint64_t n_sweeps, uint32_t sample_every);
+/* Same, enqueued on a CUDA stream (cudaStream_t as void*, NULL = the batch's
+ * own), no wait. */
+int jmm_batch_run_sampled_async(jmm_batch *b, uint64_t n_sweeps, uint32_t sample_every,
+                                void *stream);
 int jmm_batch_grad_stats(jmm_batch *b, jmm_grad_stats *out, uint32_t n_chains);
 
 /* Host-buffer convenience: create, upload positions (NULL = the configured

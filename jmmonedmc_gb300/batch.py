@@ -144,6 +144,12 @@ class ChainBatch:
         from . import grad  # noqa: F401
         _native.call("jmm_batch_run_sampled", self._h, n_sweeps, sample_every)
 
+    def run_sampled_async(self, n_sweeps, sample_every=10, stream=None):
+        """Enqueue run_sampled on a CUDA stream handle (int, None = the batch's)."""
+        from . import grad  # noqa: F401
+        _native.call("jmm_batch_run_sampled_async", self._h, n_sweeps, sample_every,
+                     C.c_void_p(stream) if stream else None)
+
     def grad_stats(self):
         from . import grad  # noqa: F401
         buf = (abi.GradStats * self.n_chains)()

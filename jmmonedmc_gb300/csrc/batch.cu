@@ -831,10 +831,21 @@ extern "C" int jmm_batch_energy_grad(jmm_batch *b, double *out, uint32_t n_chain
 }
 
 extern "C" int jmm_batch_run_sampled(jmm_batch *b, uint64_t n_sweeps, uint32_t sample_every) {
+  int rc = jmm_batch_run_sampled_async(b, n_sweeps, sample_every, nullptr);
+  if (rc) return rc;
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  return check_errors(b);
+}
+
+extern "C" int jmm_batch_run_sampled_async(jmm_batch *b, uint64_t n_sweeps, uint32_t sample_every,
+                                           void *stream) {
   clear_error();
   JMM_CHECK_ARG(b, "null handle");
   JMM_CHECK_ARG(sample_every > 0, "sample_every must be positive");
   if (n_sweeps == 0) return JMM_OK;
+  for (const auto &c : b->chains)
+    if (n_sweeps * (uint64_t)(c.n + 1) >= (1ull << 31))
+      return fail(JMM_ERR_INVALID, "one run may hold at most 2^31 steps per chain: split it");
   const auto key = std::make_pair(n_sweeps, sample_every);
   auto it = b->sampled.find(key);
   cudaGraphExec_t exec;
@@ -859,9 +870,8 @@ extern "C" int jmm_batch_run_sampled(jmm_batch *b, uint64_t n_sweeps, uint32_t s
     if (e != cudaSuccess) return cuda_status(e, "cudaGraphInstantiate", __FILE__, __LINE__);
     b->sampled[key] = exec;
   }
-  JMM_CUDA(cudaGraphLaunch(exec, b->stream));
-  JMM_CUDA(cudaStreamSynchronize(b->stream));
-  return check_errors(b);
+  JMM_CUDA(cudaGraphLaunch(exec, stream ? (cudaStream_t)stream : b->stream));
+  return JMM_OK;
 }
 
 extern "C" int jmm_batch_grad_stats(jmm_batch *b, jmm_grad_stats *out, uint32_t n_chains) {

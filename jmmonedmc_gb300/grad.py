@@ -26,6 +26,7 @@ _native.register({
                         C.c_void_p],
     "jmm_batch_energy_grad": [C.c_void_p, P(C.c_double), C.c_uint32],
     "jmm_batch_run_sampled": [C.c_void_p, C.c_uint64, C.c_uint32],
+    "jmm_batch_run_sampled_async": [C.c_void_p, C.c_uint64, C.c_uint32, C.c_void_p],
     "jmm_batch_grad_stats": [C.c_void_p, P(abi.GradStats), C.c_uint32],
 })
 
