@@ -573,7 +573,9 @@ extern "C" int jmm_batch_set_positions(jmm_batch *b, uint32_t chain, const float
   for (uint32_t i = 0; i < n; ++i) {
     if (!(x[i] == x[i]) || (i > 0 && !(x[i] > x[i - 1])))
       return fail(JMM_ERR_INVALID, "positions must be finite and strictly increasing");
-    if (!periodic && !(fabs((double)x[i]) <= 0.5 * l))
+    // the kernel's own wall test, |x| <= L/2 rounded to FP32, with room for
+    // the rounding of positions that a volume move scaled in FP32
+    if (!periodic && !(fabsf(x[i]) <= (float)(0.5 * l) * (1.0f + 1e-6f)))
       return fail(JMM_ERR_INVALID, "position %u lies beyond the walls at +-L/2", i);
   }
   if (periodic && !(x[n - 1] < x[0] + l))
