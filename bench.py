@@ -636,7 +636,7 @@ def run_grad(args, rank, world, local_rank):
     # e2e: host buffers through the public API: a batch built from host
     # positions, the sampled run, the gradient statistics and results read back
     xs = [b.positions(k) for k in range(len(chains))]
-    lbox = after["l"].copy()
+    lbox = b.results()["l"].copy()  # the box lengths of these positions
     e2e_times, e2e_moves = [], 0
     for _ in range(args.e2e_steps):
         torch.cuda.synchronize(dev)
