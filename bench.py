@@ -112,7 +112,7 @@ def workload(args, rank=0):
     from jmmonedmc_gb300 import abi
     from jmmonedmc_gb300.philox_host import uniforms
     n_ch = args.chains
-    seed = args.seed + 1000003 * rank
+    seed = rank_seed(args, rank)
     if args.workload == "uneven":
         return uneven_workload(args, seed)
     if args.workload == "grad":
@@ -211,6 +211,27 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
                 "reasons": sorted(reasons), "samples": len(sm),
                 "power_w_max": max(power) if power else None}
+
+
+# ---- ranks -----------------------------------------------------------------------
+
+def reduce_over_ranks(world, device, time_ms, counts):
+    """The job's figures over the ranks of one node: the slowest rank's time
+    and the sum of each count (every rank runs its own chains, no data is
+    exchanged).  One rank: the values unchanged."""
+    if world <= 1:
+        return float(time_ms), [float(c) for c in counts]
+    import torch
+    t = torch.tensor([time_ms] + list(counts), dtype=torch.float64, device=device)
+    tmax, tsum = t.clone(), t.clone()
+    torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
+    return float(tmax[0]), [float(v) for v in tsum[1:]]
+
+
+def rank_seed(args, rank):
+    """Each rank's chains draw from their own Philox key."""
+    return args.seed + 1000003 * rank
 
 
 # ---- CPU baseline: the reference's algorithm on the host cores -------------
@@ -374,7 +395,7 @@ def run_large(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    cfg, chains = large_workload(args, args.seed + 1000003 * rank)
+    cfg, chains = large_workload(args, rank_seed(args, rank))
     cpu = cpu_large_sample(args, args.cpu_seconds) if rank == 0 and world == 1 else None
     fp32_peak, rcp_peak = C.c_double(), C.c_double()
     _native.call("jmm_measure_peaks", C.byref(fp32_peak), C.byref(rcp_peak))
@@ -412,14 +433,7 @@ def run_large(args, rank, world, local_rank):
     moves = int((after["moves"] - before["moves"]).sum())
     pairs = int((after["pair_evals"] - before["pair_evals"]).sum())
     total_ms = float(sum(step_ms))
-    if world > 1:
-        t = torch.tensor([total_ms, moves], dtype=torch.float64, device=dev)
-        tmax, tsum = t.clone(), t.clone()
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
-        total_ms, moves_all = float(tmax[0]), float(tsum[1])
-    else:
-        moves_all = moves
+    total_ms, (moves_all,) = reduce_over_ranks(world, dev, total_ms, [moves])
 
     # the sequential plain sweep of the same chains, one sweep, beside
     seq_start, seq_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -576,7 +590,7 @@ def run_grad(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    cfg, chains = grad_workload(args, args.seed + 1000003 * rank)
+    cfg, chains = grad_workload(args, rank_seed(args, rank))
     cpu = cpu_reference_sample(chains, args.cpu_seconds, args.seed) if rank == 0 and world == 1 \
         else None
     fp32_peak, rcp_peak = C.c_double(), C.c_double()
@@ -625,13 +639,7 @@ def run_grad(args, rank, world, local_rank):
     samples = int(gstats["samples"].sum())
     # the same sweeps without the gradient samples, for the backward's share
     plain_ms = timed(lambda: b.run_async(S, stream.cuda_stream))
-    moves_all = moves
-    if world > 1:
-        t = torch.tensor([total_ms, moves], dtype=torch.float64, device=dev)
-        tmax, tsum = t.clone(), t.clone()
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
-        total_ms, moves_all = float(tmax[0]), float(tsum[1])
+    total_ms, (moves_all,) = reduce_over_ranks(world, dev, total_ms, [moves])
 
     # e2e: host buffers through the public API: a batch built from host
     # positions, the sampled run, the gradient statistics and results read back
@@ -767,15 +775,7 @@ def run_ours(args, rank, world, local_rank):
     moves = int((after["steps"] - before["steps"]).sum())
     pairs = int((after["pair_evals"] - before["pair_evals"]).sum())
     total_ms = float(sum(step_ms))
-    if world > 1:
-        t = torch.tensor([total_ms, moves, pairs], dtype=torch.float64, device=dev)
-        tmax = t.clone()
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-        tsum = t.clone()
-        torch.distributed.all_reduce(tsum, op=torch.distributed.ReduceOp.SUM)
-        total_ms, moves_all, pairs_all = float(tmax[0]), float(tsum[1]), float(tsum[2])
-    else:
-        moves_all, pairs_all = moves, pairs
+    total_ms, (moves_all, pairs_all) = reduce_over_ranks(world, dev, total_ms, [moves, pairs])
 
     # e2e: host buffers through the C ABI (jmm_batch_run_host), H2D and D2H inside
     n_tot = sum(int(c.n) for c in chains)
@@ -840,6 +840,8 @@ def run_ours(args, rank, world, local_rank):
             "pair_evals_per_launch": pairs / args.steps,
             "flop_per_pair": FLOP_PER_PAIR,
             "mufu_rcp_frac": (pairs / args.steps) / (launch_ms * 1e-3) / (rcp_peak.value * 1e12),
+            "pair_evals_per_s": (pairs / args.steps) / (launch_ms * 1e-3),
+            "smem": smem_roofline(pairs / args.steps, launch_ms),
             "kernel": "jmm::batch::chains_kernel",
         },
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -854,6 +856,22 @@ def run_ours(args, rank, world, local_rank):
     if plain is not None:
         line["plain"] = plain
     return line
+
+
+SMEM_BYTES_PER_CLOCK_SM = 128
+SM_COUNT = 152
+SM_MAX_MHZ = 2070
+
+
+def smem_roofline(pair_evals_per_launch, launch_ms):
+    """Shared-memory side of the roofline: one 4-byte neighbour position read
+    serves the old and the trial pair energy, so 2 B per pair evaluation,
+    against the nominal 128 B/clock/SM x 152 SMs x 2.07 GHz."""
+    achieved = pair_evals_per_launch * 2.0 / (launch_ms * 1e-3) / 1e9
+    peak = SMEM_BYTES_PER_CLOCK_SM * SM_COUNT * SM_MAX_MHZ * 1e6 / 1e9
+    return {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "basis": "4 B per neighbour position read (old and trial pair energy), nominal "
+                     "peak 128 B/clock/SM x 152 SMs x 2.07 GHz"}
 
 
 def plain_rate(chain, args, steps=20000):
