@@ -739,6 +739,9 @@ def run_ours(args, rank, world, local_rank):
         lanes, spr, cpb = 0, 0, 0
     else:
         lanes, spr, cpb = b.autotune(trial_sweeps=5)
+    class_names = {abi.JMM_POT_LJCUT: "ljcut", abi.JMM_POT_SOFTSPHERE: "softsphere",
+                   abi.JMM_POT_GAUSS: "gauss"}
+    class_shapes = {class_names[p]: "%dx%d, %d per block" % v for p, v in b.shapes().items()}
     # a stream of our own: torch's default stream is the legacy stream, whose
     # handle (0) would not name it to the library
     stream = torch.cuda.Stream(dev)
@@ -825,7 +828,7 @@ def run_ours(args, rank, world, local_rank):
         "dtype": "f32",
         "data": "synthetic (seeded Philox: T log-spaced, P uniform, lattice start)",
         "config": config_dict(args, {"lanes_per_chain": lanes, "steps_per_round": spr,
-                                     "chains_per_block": cpb,
+                                     "chains_per_block": cpb, "class_shapes": class_shapes,
                                      "parallelism": f"replicas{world}",
                                      "wall_s_timed": wall}),
         "roofline": {

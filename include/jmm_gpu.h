@@ -301,10 +301,16 @@ int jmm_batch_energies(jmm_batch *b, double *e, uint32_t n_chains);
  * jmm_chain_result array, for zero-copy tooling (torch, benchmarks). */
 int jmm_batch_device_views(jmm_batch *b, void **positions, void **results,
                            uint64_t *offsets, uint32_t n_chains);
-/* Time candidate launch shapes on a copy of the state and keep the fastest;
- * writes the chosen lanes_per_chain, steps_per_round and chains_per_block. */
+/* Time candidate launch shapes on a copy of the state and keep the fastest:
+ * in FAST precision one per potential class (each class timed alone), in
+ * EXACT one for the whole batch; writes the lanes_per_chain,
+ * steps_per_round and chains_per_block of the largest class. */
 int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t *lanes_per_chain,
                        uint32_t *steps_per_round, uint32_t *chains_per_block);
+/* The launch shape of each potential class (LJcut, soft sphere, Gaussian
+ * core): shapes[3k .. 3k+2] = lanes, steps per round, chains per block; 0 for
+ * a class without chains. */
+int jmm_batch_shapes(jmm_batch *b, uint32_t *shapes, uint32_t n);
 /* Step-size adjustment on the device, enqueued on the batch's stream
  * (maxDisAdjust / maxDVAdjust, src/jmmMCState.cpp:2100-2139, per chain from
  * its counts since creation or the last reset): what = 1 displacement,

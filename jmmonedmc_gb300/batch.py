@@ -31,6 +31,7 @@ _native.register({
                            C.c_uint64, P(abi.ChainResult), P(C.c_float)],
     "jmm_rng_words": [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint64, P(C.c_uint32)],
     "jmm_batch_adjust_steps": [C.c_void_p, C.c_double, C.c_int32],
+    "jmm_batch_shapes": [C.c_void_p, P(C.c_uint32), C.c_uint32],
     "jmm_batch_step_sizes": [C.c_void_p, P(C.c_double), P(C.c_double), C.c_uint32],
 })
 
@@ -162,6 +163,14 @@ class ChainBatch:
         _native.call("jmm_batch_autotune", self._h, trial_sweeps, C.byref(g), C.byref(s),
                      C.byref(c))
         return g.value, s.value, c.value
+
+    def shapes(self):
+        """{potential: (lanes, steps per round, chains per block)} of the classes
+        present (LJcut, soft sphere, Gaussian core)."""
+        out = (C.c_uint32 * 9)()
+        _native.call("jmm_batch_shapes", self._h, out, 9)
+        pots = (abi.JMM_POT_LJCUT, abi.JMM_POT_SOFTSPHERE, abi.JMM_POT_GAUSS)
+        return {p: tuple(out[3 * k:3 * k + 3]) for k, p in enumerate(pots) if out[3 * k]}
 
 
 def run_host(config, chains, n_sweeps, x_in=None):

@@ -57,8 +57,14 @@ constexpr int kPots[3] = {JMM_POT_LJCUT, JMM_POT_SOFTSPHERE, JMM_POT_GAUSS};
 
 // The chains of one potential: a contiguous range of launch slots with its
 // own blocks and shared-memory size.
+// A launch shape: G window lanes x S steps per round, chains per block.
+struct Shape {
+  uint32_t g, spr, cpb;
+};
+
 struct PotClass {
   int pot;
+  Shape shape;
   uint32_t first, count;
   uint32_t n_blocks;
   size_t smem;
@@ -80,7 +86,8 @@ struct jmm_batch {
   jmm_chain_result *d_res = nullptr;
   float *d_x = nullptr;
   double *d_e = nullptr;
-  uint32_t g = 8, spr = 4, cpb = 4, n_blocks = 0;
+  uint32_t g = 8, spr = 4, cpb = 4, n_blocks = 0;  // the shape of the largest class
+  Shape shapes[3] = {{8, 4, 4}, {8, 4, 4}, {8, 4, 4}};  // per potential class (kPots order)
   size_t smem = 0;
   cudaStream_t stream = nullptr;
   std::map<uint64_t, cudaGraphExec_t> graphs;  // n_sweeps -> instantiated run
@@ -122,7 +129,6 @@ static void batch_free(jmm_batch *b) {
   delete b;
 }
 
-// Per-chain kernel parameters for launch shape (g, spr, cpb); uploads them.
 // Step sizes changed on the device (jmm_batch_adjust_steps) back into the
 // chain descriptions, so that a new layout keeps them.
 static int sync_step_sizes(jmm_batch *b) {
@@ -139,36 +145,40 @@ static int sync_step_sizes(jmm_batch *b) {
   return JMM_OK;
 }
 
-static int apply_layout(jmm_batch *b, uint32_t g, uint32_t spr, uint32_t cpb) {
+// Per-chain kernel parameters for one launch shape per potential class
+// (kPots order); uploads them.
+static int apply_layout(jmm_batch *b, const Shape shapes[3]) {
   const bool per = b->cfg.boundary == JMM_BOUNDARY_PERIODIC;
   {
     const int rc = sync_step_sizes(b);
     if (rc) return rc;
   }
   const bool exact = b->cfg.precision == JMM_PREC_EXACT;
-  if (!pick_kernel(g, spr, false, JMM_POT_LJCUT, false))
-    return fail(JMM_ERR_INVALID, "unsupported launch shape: lanes_per_chain x steps_per_round "
-                "must be 4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or 32x1");
-  const uint32_t lanes = g * spr;
-  if (cpb == 0 || cpb * lanes > 256)
-    return fail(JMM_ERR_INVALID, "chains_per_block * lanes per chain must be <= 256");
-  const uint32_t w = (uint32_t)window_of((int)g);
-  if (per) {
-    for (const auto &c : b->chains)
-      if (c.n < 2 * w + 1)
-        return fail(JMM_ERR_INVALID, "periodic chains need N > twice the neighbour window");
-  }
   std::vector<ChainParams> prm(b->n_chains);
   std::vector<PotClass> classes;
-  const uint64_t ring_floats = (uint64_t)cpb * kRingWords;
   uint32_t slot0 = 0;
-  for (int pot : kPots) {
+  for (int pi = 0; pi < 3; ++pi) {
+    const int pot = kPots[pi];
+    const uint32_t g = shapes[pi].g, spr = shapes[pi].spr, cpb = shapes[pi].cpb;
+    if (!pick_kernel(g, spr, false, JMM_POT_LJCUT, false))
+      return fail(JMM_ERR_INVALID, "unsupported launch shape: lanes_per_chain x steps_per_round "
+                  "must be 4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or 32x1");
+    if (cpb == 0 || cpb * g * spr > 256)
+      return fail(JMM_ERR_INVALID, "chains_per_block * lanes per chain must be <= 256");
+    const uint64_t ring_floats = (uint64_t)cpb * kRingWords;
     PotClass pc;
     pc.pot = pot;
+    pc.shape = shapes[pi];
     pc.first = slot0;
     pc.count = 0;
     while (slot0 + pc.count < b->n_chains && b->chains[b->order[slot0 + pc.count]].potential == pot)
       pc.count++;
+    if (per) {
+      const uint32_t w = (uint32_t)window_of((int)g);
+      for (uint32_t k = 0; k < pc.count; ++k)
+        if (b->chains[b->order[pc.first + k]].n < 2 * w + 1)
+          return fail(JMM_ERR_INVALID, "periodic chains need N > twice the neighbour window");
+    }
     pc.n_blocks = (pc.count + cpb - 1) / cpb;
     pc.smem = 0;
     for (uint32_t blk = 0; blk < pc.n_blocks; ++blk) {
@@ -215,16 +225,31 @@ static int apply_layout(jmm_batch *b, uint32_t g, uint32_t spr, uint32_t cpb) {
                       cudaMemcpyHostToDevice));
   b->params.swap(prm);
   b->classes.swap(classes);
-  b->g = g;
-  b->spr = spr;
-  b->cpb = cpb;
+  uint32_t most = 0;
+  for (int pi = 0; pi < 3; ++pi) b->shapes[pi] = shapes[pi];
+  for (const PotClass &pc : b->classes) {
+    if (pc.count > most) {
+      most = pc.count;
+      b->g = pc.shape.g;
+      b->spr = pc.shape.spr;
+      b->cpb = pc.shape.cpb;
+    }
+  }
   drop_graphs(b);
   return JMM_OK;
 }
 
+// The same launch shape for every class.
+static int apply_layout(jmm_batch *b, uint32_t g, uint32_t spr, uint32_t cpb) {
+  const Shape sh[3] = {{g, spr, cpb}, {g, spr, cpb}, {g, spr, cpb}};
+  return apply_layout(b, sh);
+}
+
 // One launch per potential class; with several classes they run on forked
 // streams that rejoin `s`, so that a graph holds them as parallel nodes.
-static int launch(jmm_batch *b, uint64_t n_sweeps, cudaStream_t s) {
+// Class k's kernel on stream st.
+static int launch_class(jmm_batch *b, size_t k, uint64_t n_sweeps, cudaStream_t st) {
+  const PotClass &pc = b->classes[k];
   KernelCfg kc;
   kc.seed = b->cfg.seed;
   kc.n_sweeps = n_sweeps;
@@ -232,20 +257,25 @@ static int launch(jmm_batch *b, uint64_t n_sweeps, cudaStream_t s) {
   kc.vol_move = b->cfg.vol_move;
   kc.vol_schedule = b->cfg.vol_schedule;
   kc.resum_sweeps = (int32_t)b->cfg.resum_sweeps;
-  kc.chains_per_block = b->cpb;
+  kc.chains_per_block = pc.shape.cpb;
+  kc.n_chains = pc.count;
   const bool per = b->cfg.boundary == JMM_BOUNDARY_PERIODIC;
   const bool exact = b->cfg.precision == JMM_PREC_EXACT;
-  const uint32_t threads = b->g * b->spr * b->cpb;
+  const uint32_t threads = pc.shape.g * pc.shape.spr * pc.shape.cpb;
+  ChainsKernel kf = pick_kernel(pc.shape.g, pc.shape.spr, exact, pc.pot, per);
+  kf<<<pc.n_blocks, threads, pc.smem, st>>>(b->d_params + pc.first, b->d_res, b->d_x, kc);
+  JMM_CUDA(cudaGetLastError());
+  return JMM_OK;
+}
+
+static int launch(jmm_batch *b, uint64_t n_sweeps, cudaStream_t s) {
   const bool fork = b->classes.size() > 1;
   if (fork) JMM_CUDA(cudaEventRecord(b->fork, s));
   for (size_t k = 0; k < b->classes.size(); ++k) {
-    const PotClass &pc = b->classes[k];
     cudaStream_t st = fork ? b->side[k] : s;
     if (fork) JMM_CUDA(cudaStreamWaitEvent(st, b->fork, 0));
-    kc.n_chains = pc.count;
-    ChainsKernel kf = pick_kernel(b->g, b->spr, exact, pc.pot, per);
-    kf<<<pc.n_blocks, threads, pc.smem, st>>>(b->d_params + pc.first, b->d_res, b->d_x, kc);
-    JMM_CUDA(cudaGetLastError());
+    const int rc = launch_class(b, k, n_sweeps, st);
+    if (rc) return rc;
     if (fork) {
       JMM_CUDA(cudaEventRecord(b->join[k], st));
       JMM_CUDA(cudaStreamWaitEvent(s, b->join[k], 0));
@@ -620,6 +650,11 @@ extern "C" int jmm_batch_device_views(jmm_batch *b, void **positions, void **res
   return JMM_OK;
 }
 
+// Launch shapes tried by the autotuner: G x S, and threads per block.
+static const uint32_t kTuneShapes[][2] = {{4, 8}, {4, 4}, {4, 2}, {8, 4},
+                                          {8, 2}, {16, 2}, {16, 1}, {32, 1}};
+static const uint32_t kTuneThreads[] = {32u, 64u, 128u, 256u};
+
 extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t *lanes_out,
                                   uint32_t *spr_out, uint32_t *cpb_out) {
   clear_error();
@@ -639,42 +674,69 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
   cudaEvent_t t0, t1;
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
-  const uint32_t g0 = b->g, s0 = b->spr, c0 = b->cpb;
-  float best = 1e30f;
-  uint32_t best_g = g0, best_s = s0, best_c = c0;
-  int rc = JMM_OK;
-  const uint32_t shapes[][2] = {{4, 8}, {4, 4}, {4, 2}, {8, 4}, {8, 2}, {16, 2}, {16, 1}, {32, 1}};
-  for (const auto &shape : shapes) {
-    const uint32_t g = shape[0], spr = shape[1];
-    for (uint32_t threads : {32u, 64u, 128u, 256u}) {
-      const uint32_t cpb = threads / (g * spr);
-      if (cpb == 0) continue;
-      if (apply_layout(b, g, spr, cpb) != JMM_OK) {
-        clear_error();
-        continue;
-      }
-      float ms = 0.0f;
-      for (int rep = 0; rep < 2; ++rep) {  // first run warms the code path
-        cudaMemcpyAsync(b->d_x, x_save, b->total_floats * sizeof(float), cudaMemcpyDeviceToDevice,
-                        b->stream);
-        cudaMemcpyAsync(b->d_res, r_save, b->n_chains * sizeof(jmm_chain_result),
-                        cudaMemcpyDeviceToDevice, b->stream);
-        cudaEventRecord(t0, b->stream);
+  // Time of a trial: the whole batch (cls < 0), or class cls alone; the
+  // state is restored before each run, the first run warms the code path.
+  auto trial = [&](int cls, float *ms_out) -> int {
+    float ms = 0.0f;
+    for (int rep = 0; rep < 2; ++rep) {
+      cudaMemcpyAsync(b->d_x, x_save, b->total_floats * sizeof(float), cudaMemcpyDeviceToDevice,
+                      b->stream);
+      cudaMemcpyAsync(b->d_res, r_save, b->n_chains * sizeof(jmm_chain_result),
+                      cudaMemcpyDeviceToDevice, b->stream);
+      cudaEventRecord(t0, b->stream);
+      int rc = JMM_OK;
+      if (cls < 0) {
         rc = launch(b, trial_sweeps, b->stream);
-        cudaEventRecord(t1, b->stream);
+      } else {
+        for (size_t k = 0; k < b->classes.size(); ++k)
+          if (b->classes[k].pot == kPots[cls]) rc = launch_class(b, k, trial_sweeps, b->stream);
+      }
+      cudaEventRecord(t1, b->stream);
+      if (rc) return rc;
+      cudaEventSynchronize(t1);
+      cudaEventElapsedTime(&ms, t0, t1);
+    }
+    *ms_out = ms;
+    return JMM_OK;
+  };
+  Shape best[3];
+  for (int pi = 0; pi < 3; ++pi) best[pi] = b->shapes[pi];
+  int rc = JMM_OK;
+  // EXACT runs keep one shape for the whole batch (the oracle replays one G);
+  // FAST runs tune every potential class on its own
+  const bool per_class = b->cfg.precision != JMM_PREC_EXACT;
+  const int rounds = per_class ? 3 : 1;
+  for (int pi = 0; pi < rounds && rc == JMM_OK; ++pi) {
+    if (per_class) {
+      bool present = false;
+      for (const PotClass &pc : b->classes) present = present || pc.pot == kPots[pi];
+      if (!present) continue;
+    }
+    float best_ms = 1e30f;
+    for (const auto &shape : kTuneShapes) {
+      for (uint32_t threads : kTuneThreads) {
+        const uint32_t cpb = threads / (shape[0] * shape[1]);
+        if (cpb == 0) continue;
+        Shape sh[3];
+        for (int q = 0; q < 3; ++q) sh[q] = per_class ? best[q] : Shape{shape[0], shape[1], cpb};
+        if (per_class) sh[pi] = Shape{shape[0], shape[1], cpb};
+        if (apply_layout(b, sh) != JMM_OK) {
+          clear_error();
+          continue;
+        }
+        float ms = 0.0f;
+        rc = trial(per_class ? pi : -1, &ms);
         if (rc) break;
-        cudaEventSynchronize(t1);
-        cudaEventElapsedTime(&ms, t0, t1);
+        if (ms < best_ms) {
+          best_ms = ms;
+          if (per_class)
+            best[pi] = sh[pi];
+          else
+            for (int q = 0; q < 3; ++q) best[q] = sh[q];
+        }
       }
       if (rc) break;
-      if (ms < best) {
-        best = ms;
-        best_g = g;
-        best_s = spr;
-        best_c = cpb;
-      }
     }
-    if (rc) break;
   }
   cudaMemcpy(b->d_x, x_save, b->total_floats * sizeof(float), cudaMemcpyDeviceToDevice);
   cudaMemcpy(b->d_res, r_save, b->n_chains * sizeof(jmm_chain_result), cudaMemcpyDeviceToDevice);
@@ -683,15 +745,29 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
   cudaFree(x_save);
   cudaFree(r_save);
   if (rc) return rc;
-  rc = apply_layout(b, best_g, best_s, best_c);
+  rc = apply_layout(b, best);
   if (rc) return rc;
-  b->cfg.lanes_per_chain = best_g;
-  b->cfg.steps_per_round = best_s;
-  b->cfg.chains_per_block = best_c;
-  if (lanes_out) *lanes_out = best_g;
-  if (spr_out) *spr_out = best_s;
-  if (cpb_out) *cpb_out = best_c;
+  b->cfg.lanes_per_chain = b->g;
+  b->cfg.steps_per_round = b->spr;
+  b->cfg.chains_per_block = b->cpb;
+  if (lanes_out) *lanes_out = b->g;
+  if (spr_out) *spr_out = b->spr;
+  if (cpb_out) *cpb_out = b->cpb;
   JMM_CUDA(cudaDeviceSynchronize());
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_shapes(jmm_batch *b, uint32_t *shapes, uint32_t n) {
+  clear_error();
+  JMM_CHECK_ARG(b && shapes, "null argument");
+  JMM_CHECK_ARG(n == 9, "shapes holds 3 x (lanes, steps per round, chains per block)");
+  for (int pi = 0; pi < 3; ++pi) {
+    bool present = false;
+    for (const PotClass &pc : b->classes) present = present || pc.pot == kPots[pi];
+    shapes[3 * pi + 0] = present ? b->shapes[pi].g : 0;
+    shapes[3 * pi + 1] = present ? b->shapes[pi].spr : 0;
+    shapes[3 * pi + 2] = present ? b->shapes[pi].cpb : 0;
+  }
   return JMM_OK;
 }
 

@@ -298,3 +298,36 @@ def test_fast_ensemble_averages_match_fp64_oracle(gpu):
         print(f"{q}: gpu {np.round(mg, 4)} cpu {np.round(mc, 4)} z {np.round(z, 2)}")
         worst = max(worst, np.abs(z).max())
     assert worst < 4.0, worst
+
+
+def test_autotune_per_potential_class(gpu):
+    """FAST precision: every potential class gets its own launch shape (dense
+    Gaussian-core chains need a wider neighbour window than LJ chains); the
+    tuned batch stays within the FP64 energy tolerance and keeps its state."""
+    chains = []
+    for k in range(96):
+        if k % 2:
+            chains.append(abi.make_chain(512, potential=abi.JMM_POT_GAUSS, cutoff=4.0, rho=0.9,
+                                         t=1.0, max_step=0.3))
+        else:
+            chains.append(abi.make_chain(512, potential=abi.JMM_POT_LJCUT, cutoff=3.0, rho=0.6,
+                                         t=1.0, max_step=0.3))
+    b = ChainBatch(abi.make_batch_config(seed=3, precision=abi.JMM_PREC_FAST, resum_sweeps=5),
+                   chains)
+    b.run(3)
+    before = b.results()
+    b.autotune(trial_sweeps=2)
+    after = b.results()
+    assert np.array_equal(before["e"], after["e"]) and np.array_equal(before["steps"], after["steps"])
+    shapes = b.shapes()
+    print("per-class shapes", shapes)
+    assert set(shapes) == {abi.JMM_POT_LJCUT, abi.JMM_POT_GAUSS}
+    assert shapes[abi.JMM_POT_GAUSS][0] >= 16  # a window of at least 8 per side
+    b.run(10)
+    res = b.results()
+    assert np.all(res["error"] == 0)
+    fresh = b.energies()
+    for k in (0, 1, 94, 95):
+        x = b.positions(k).astype(np.float64)
+        e64 = oracle_lib.energy64(chains[k], x, res["l"][k])
+        assert abs(fresh[k] - e64) <= 1e-6 * max(1.0, abs(e64))
