@@ -790,10 +790,15 @@ def run_ours(args, rank, world, local_rank):
     lbox = after["l"].copy()
     for k, c in enumerate(chains):
         c.l0 = float(lbox[k])
+    # one class: the tuned shape; several: the library's per-class defaults
+    # (a host-buffer call carries one shape only)
+    one_class = len(class_shapes) == 1
     e2e_cfg = abi.make_batch_config(seed=cfg.seed + 7, vol_move=cfg.vol_move,
                                     vol_schedule=cfg.vol_schedule, precision=cfg.precision,
-                                    lanes_per_chain=lanes, steps_per_round=spr,
-                                    chains_per_block=cpb)
+                                    resum_sweeps=cfg.resum_sweeps,
+                                    lanes_per_chain=lanes if one_class else 0,
+                                    steps_per_round=spr if one_class else 0,
+                                    chains_per_block=cpb if one_class else 0)
     e2e_times, e2e_moves = [], 0
     for _ in range(args.e2e_steps):
         torch.cuda.synchronize(dev)

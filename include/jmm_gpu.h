@@ -258,7 +258,10 @@ typedef struct jmm_batch_config {
                                 many sweeps (0 = only at the end of a run)      */
   uint32_t lanes_per_chain;  /* lanes G of one trial move: 4, 8, 16 or 32; they
                                 look at W = max(4, G/2) neighbours per side;
-                                0 = 4                                           */
+                                0 = 4 in EXACT precision, and in FAST a default
+                                per potential class from its densest chain
+                                (4, or 16 / 32 where more neighbours fall
+                                within the cut-off)                             */
   uint32_t steps_per_round;  /* S steps evaluated at once per chain: G x S is
                                 4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or 32x1;
                                 0 = 32/G                                        */

@@ -416,7 +416,28 @@ extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_des
   const uint32_t g = cfg->lanes_per_chain ? cfg->lanes_per_chain : 4;
   const uint32_t spr = cfg->steps_per_round ? cfg->steps_per_round : (g <= 32 ? 32 / g : 1);
   const uint32_t cpb = cfg->chains_per_block ? cfg->chains_per_block : 128 / (g * spr ? g * spr : 1);
-  rc = apply_layout(b, g, spr, cpb);
+  if (cfg->lanes_per_chain == 0 && cfg->precision != JMM_PREC_EXACT) {
+    // no shape given, FAST precision: a default per class from the densest
+    // chain's neighbours within the cut-off.  A 12-power core keeps LJ and
+    // soft-sphere neighbours at least ~0.85 sigma apart, a Gaussian core
+    // lets them overlap (about 1.5 rho rc per side at the densest).
+    Shape sh[3];
+    for (int pi = 0; pi < 3; ++pi) {
+      double need = 0.0;
+      for (const auto &c : b->chains) {
+        if (c.potential != kPots[pi]) continue;
+        const double side = c.potential == JMM_POT_GAUSS ? 1.5 * c.n / c.l0 * c.cutoff
+                                                         : c.cutoff / (0.85 * c.sigma);
+        need = std::max(need, side);
+      }
+      const uint32_t gg = need <= 4.0 ? 4u : (need <= 8.0 ? 16u : 32u);
+      const uint32_t ss = 32 / gg;
+      sh[pi] = Shape{gg, ss, 128 / (gg * ss)};
+    }
+    rc = apply_layout(b, sh);
+  } else {
+    rc = apply_layout(b, g, spr, cpb);
+  }
   if (rc == JMM_OK) rc = energies(b, b->stream);
   if (rc == JMM_OK) {
     set_energies_kernel<<<(n_chains + 255) / 256, 256, 0, b->stream>>>(b->d_res, b->d_e, n_chains);
