@@ -15,8 +15,9 @@
 //    steps of the chain at once, all from the current positions.  Step s of
 //    the round is kept if no earlier kept step of the round was accepted
 //    within W index positions of it (its window would have seen the moved
-//    particle); the first step that fails is re-evaluated at the start of
-//    the next round.  Kept steps are committed in order, so every step's
+//    particle) — with walls, only if the two particles are neighbours or
+//    their old-to-trial spans come within the cut-off; the first step that
+//    fails is re-evaluated at the start of the next round.  Kept steps are committed in order, so every step's
 //    outcome, the running energy and the statistics are those of the
 //    sequential chain, operation for operation.
 //  * Philox words of 32 steps ahead are drawn by the chain's lanes into a
@@ -506,16 +507,30 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       const unsigned accbits = (__ballot_sync(gmask, acc) >> lane_shift & kChainBits);
       if (S > 1 && f > 1) {
         // lane w of slot s2 checks earlier slots s1 = w, w + G, ... for an
-        // accepted move within W index positions of its own particle
+        // accepted move within W index positions of its own particle.  With
+        // walls, a neighbour two or more places away matters only if the
+        // spans [old, trial] of the two particles come within the cut-off:
+        // otherwise every pair term between them is 0 before and after
+        // (FP32 rounding is monotone, so fl(gap)^2 > rc^2 bounds all four),
+        // and beyond W nothing changes since no particle passes another.
         bool conflict = false;
 #pragma unroll
         for (int r = 0; r < (S + G - 1) / G; ++r) {
           const int s1 = wl + r * G;
-          const int nm1 = __shfl_sync(gmask, nmc, (s1 < S ? s1 : 0) * G, L);
+          const int src = (s1 < S ? s1 : 0) * G;
+          const int nm1 = __shfl_sync(gmask, nmc, src, L);
           int dist = nm1 - nmc;
           dist = dist < 0 ? -dist : dist;
           if (PER) dist = min(dist, n - dist);
-          conflict = conflict || (s1 < slot && ((accbits >> (s1 * G)) & 1u) && dist <= W);
+          bool hit = dist <= W;
+          if (!PER) {
+            const float a0 = __shfl_sync(gmask, xo, src, L);
+            const float a1 = __shfl_sync(gmask, xn, src, L);
+            const float gap = fmaxf(__fsub_rn(fminf(a0, a1), fmaxf(xo, xn)),
+                                    __fsub_rn(fminf(xo, xn), fmaxf(a0, a1)));
+            hit = hit && (dist <= 1 || !(gap > 0.0f && __fmul_rn(gap, gap) > H.rc2));
+          }
+          conflict = conflict || (s1 < slot && ((accbits >> (s1 * G)) & 1u) && hit);
         }
         const unsigned cbits = ((__ballot_sync(gmask, conflict) >> lane_shift & kChainBits)) | satbits;
         const unsigned late = cbits & ~kSlotBits;  // slots 1 .. S-1
