@@ -513,25 +513,37 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
         // otherwise every pair term between them is 0 before and after
         // (FP32 rounding is monotone, so fl(gap)^2 > rc^2 bounds all four),
         // and beyond W nothing changes since no particle passes another.
-        bool conflict = false;
+        constexpr int R = (S + G - 1) / G;
+        bool cand[R];
+        int far[R];  // candidates two or more places away: index of the source lane
+        bool any_far = false;
 #pragma unroll
-        for (int r = 0; r < (S + G - 1) / G; ++r) {
+        for (int r = 0; r < R; ++r) {
           const int s1 = wl + r * G;
           const int src = (s1 < S ? s1 : 0) * G;
           const int nm1 = __shfl_sync(gmask, nmc, src, L);
           int dist = nm1 - nmc;
           dist = dist < 0 ? -dist : dist;
           if (PER) dist = min(dist, n - dist);
-          bool hit = dist <= W;
-          if (!PER) {
+          cand[r] = s1 < slot && ((accbits >> (s1 * G)) & 1u) && dist <= W;
+          far[r] = (!PER && cand[r] && dist >= 2) ? src : -1;
+          any_far = any_far || far[r] >= 0;
+        }
+        // the spans are compared only in the rounds that have such a candidate
+        if (!PER && __any_sync(gmask, any_far)) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const int src = far[r] >= 0 ? far[r] : 0;
             const float a0 = __shfl_sync(gmask, xo, src, L);
             const float a1 = __shfl_sync(gmask, xn, src, L);
             const float gap = fmaxf(__fsub_rn(fminf(a0, a1), fmaxf(xo, xn)),
                                     __fsub_rn(fminf(xo, xn), fmaxf(a0, a1)));
-            hit = hit && (dist <= 1 || !(gap > 0.0f && __fmul_rn(gap, gap) > H.rc2));
+            if (far[r] >= 0 && gap > 0.0f && __fmul_rn(gap, gap) > H.rc2) cand[r] = false;
           }
-          conflict = conflict || (s1 < slot && ((accbits >> (s1 * G)) & 1u) && hit);
         }
+        bool conflict = false;
+#pragma unroll
+        for (int r = 0; r < R; ++r) conflict = conflict || cand[r];
         const unsigned cbits = ((__ballot_sync(gmask, conflict) >> lane_shift & kChainBits)) | satbits;
         const unsigned late = cbits & ~kSlotBits;  // slots 1 .. S-1
         if (late) f = min(f, (uint32_t)(__ffs(late) - 1) / G);
