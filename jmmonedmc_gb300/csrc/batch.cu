@@ -45,6 +45,7 @@ ChainsKernel pick_kernel(uint32_t g, uint32_t s, bool exact, int pot, bool per) 
   if (g == 4 && s == 4) return exact ? pick_pot<4, 4, true>(pot, per) : pick_pot<4, 4, false>(pot, per);
   if (g == 4 && s == 2) return exact ? pick_pot<4, 2, true>(pot, per) : pick_pot<4, 2, false>(pot, per);
   if (g == 4 && s == 8) return exact ? pick_pot<4, 8, true>(pot, per) : pick_pot<4, 8, false>(pot, per);
+  if (g == 2 && s == 16) return exact ? pick_pot<2, 16, true>(pot, per) : pick_pot<2, 16, false>(pot, per);
   if (g == 8 && s == 4) return exact ? pick_pot<8, 4, true>(pot, per) : pick_pot<8, 4, false>(pot, per);
   if (g == 8 && s == 2) return exact ? pick_pot<8, 2, true>(pot, per) : pick_pot<8, 2, false>(pot, per);
   if (g == 16 && s == 2) return exact ? pick_pot<16, 2, true>(pot, per) : pick_pot<16, 2, false>(pot, per);
@@ -162,7 +163,7 @@ static int apply_layout(jmm_batch *b, const Shape shapes[3]) {
     const uint32_t g = shapes[pi].g, spr = shapes[pi].spr, cpb = shapes[pi].cpb;
     if (!pick_kernel(g, spr, false, JMM_POT_LJCUT, false))
       return fail(JMM_ERR_INVALID, "unsupported launch shape: lanes_per_chain x steps_per_round "
-                  "must be 4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or 32x1");
+                  "must be 2x16, 4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or 32x1");
     if (cpb == 0 || cpb * g * spr > 256)
       return fail(JMM_ERR_INVALID, "chains_per_block * lanes per chain must be <= 256");
     const uint64_t ring_floats = (uint64_t)cpb * kRingWords;
@@ -672,7 +673,7 @@ extern "C" int jmm_batch_device_views(jmm_batch *b, void **positions, void **res
 }
 
 // Launch shapes tried by the autotuner: G x S, and threads per block.
-static const uint32_t kTuneShapes[][2] = {{4, 8}, {4, 4}, {4, 2}, {8, 4},
+static const uint32_t kTuneShapes[][2] = {{4, 8}, {2, 16}, {4, 4}, {4, 2}, {8, 4},
                                           {8, 2}, {16, 2}, {16, 1}, {32, 1}};
 static const uint32_t kTuneThreads[] = {32u, 64u, 128u, 256u};
 

@@ -17,9 +17,9 @@
 //    within W index positions of it (its window would have seen the moved
 //    particle) — with walls, only if the two particles are neighbours or
 //    their old-to-trial spans come within the cut-off; the first step that
-//    fails is re-evaluated at the start of the next round.  Kept steps are committed in order, so every step's
-//    outcome, the running energy and the statistics are those of the
-//    sequential chain, operation for operation.
+//    fails is re-evaluated at the start of the next round.  Kept steps are
+//    committed in order, so every step's outcome, the running energy and the
+//    statistics are those of the sequential chain, operation for operation.
 //  * Philox words of 32 steps ahead are drawn by the chain's lanes into a
 //    small shared buffer.
 //  * The running energy is an FP64 base plus an FP32 offset, folded into
@@ -27,9 +27,11 @@
 //    the per-step accumulators (sum E, E^2, L, L^2, LE, rho, rho^2).
 // Every FP32/FP64 operation is an explicit round-to-nearest intrinsic so
 // that the EXACT precision mode can be replayed bit for bit by the oracle;
-// the FAST mode differs in using the hardware reciprocal, exp and log, and
-// in summing a round's per-step statistics by a scan over its slots instead
-// of step by step (the same quantities, rounded in another order).
+// the FAST mode differs in using the hardware reciprocal, exp and log, in
+// scaling a window's summed pair shapes by the potential's strength once, and
+// in summing a round's per-step statistics by a scan over its slots into
+// per-lane shares instead of step by step (the same quantities, rounded in
+// another order).
 #pragma once
 #include <math.h>
 #include <stdint.h>
@@ -216,6 +218,17 @@ __device__ __forceinline__ void note_drift(jmm_chain_result *__restrict__ rp, bo
   if (writer && drift > rp->max_drift) rp->max_drift = drift;
 }
 
+// In FAST precision each slot leader keeps its steps' share of the segment
+// sums (sum of delta, of delta^2) in its own registers; the shares join the
+// chain's sums before every fold.
+template <int L>
+__device__ __forceinline__ void gather_shares(Seg &g, float &sd_loc, float &sd2_loc, unsigned gmask) {
+  g.sd = __fadd_rn(g.sd, group_sum<L>(sd_loc, gmask));
+  g.sd2 = __fadd_rn(g.sd2, group_sum<L>(sd2_loc, gmask));
+  sd_loc = 0.0f;
+  sd2_loc = 0.0f;
+}
+
 // The per-chain constants of the step loop, kept in registers.
 struct Hot {
   float eps4, sigma2, inv_sigma2, rc2, beta, two_max_step;
@@ -233,6 +246,30 @@ __device__ __forceinline__ float pair_energy_h(float d2, const Hot &H) {
                                     : __fmul_rn(H.eps4, __fmul_rn(inv6, __fsub_rn(inv6, 1.0f)));
   }
   return d2 <= H.rc2 ? e : 0.0f;
+}
+
+// The pair energy over its strength (eps4): the FAST step loop sums these
+// and scales the chain's energy change once.
+template <int POT>
+__device__ __forceinline__ float pair_shape_fast(float d2, const Hot &H) {
+  float e;
+  if (POT == JMM_POT_GAUSS) {
+    e = __expf(-__fmul_rn(d2, H.inv_sigma2));
+  } else {
+    const float inv2 = __fmul_rn(H.sigma2, rcp32<false>(d2));
+    const float inv6 = __fmul_rn(__fmul_rn(inv2, inv2), inv2);
+    e = (POT == JMM_POT_SOFTSPHERE) ? __fmul_rn(inv6, inv6) : __fmul_rn(inv6, __fsub_rn(inv6, 1.0f));
+  }
+  return d2 <= H.rc2 ? e : 0.0f;
+}
+
+// Energy change of one window pair, old separation^2 do2 to trial dn2: in
+// EXACT precision the difference of the two pair energies; in FAST the
+// difference of their shapes, scaled by eps4 after the window sum.
+template <int POT, bool kExact>
+__device__ __forceinline__ float pair_change(float dn2, float do2, const Hot &H) {
+  if (kExact) return __fsub_rn(pair_energy_h<POT, true>(dn2, H), pair_energy_h<POT, true>(do2, H));
+  return __fsub_rn(pair_shape_fast<POT>(dn2, H), pair_shape_fast<POT>(do2, H));
 }
 
 // The Metropolis threshold -ln u, u the midpoint of the 23-bit cell of w
@@ -316,6 +353,27 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
   const int kb = wl % H2 + 1;  // this lane's offsets: kb, kb + H2, ...
   const int lane_shift = (int)(threadIdx.x & 31) - cl;  // first lane of the chain in the warp
   constexpr unsigned kChainBits = (L == 32) ? 0xffffffffu : ((1u << L) - 1u);
+  // The conflict test gives each lane R pairs (s1 < s2) of the round's
+  // slots: pair number cl + r*L in the order of s2 and then s1, so that the
+  // lowest lane of the first set r with a conflict names the first slot to
+  // drop.  Packed as src1 | src2 << 8 | s2 << 16 (lanes of slots s1, s2);
+  // s2 = S marks an idle entry.
+  constexpr int kPairs = S * (S - 1) / 2;
+  constexpr int R = kPairs > L ? (kPairs + L - 1) / L : 1;
+  uint32_t ptab[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    int c = cl + r * L, p1 = 0, p2 = S;
+    for (int s2 = 1; s2 < S; ++s2) {
+      if (c < s2) {
+        p1 = c;
+        p2 = s2;
+        break;
+      }
+      c -= s2;
+    }
+    ptab[r] = (uint32_t)(p1 * G) | ((uint32_t)((p2 < S ? p2 : 0) * G) << 8) | ((uint32_t)p2 << 16);
+  }
   const bool writer = cl == 0;
   int32_t *ring_nm = reinterpret_cast<int32_t *>(ring);
   float *ring_md = reinterpret_cast<float *>(ring + kRingSteps);  // md, or u1 of a volume step
@@ -339,6 +397,8 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
   g.sd = 0.0f;
   g.sd2 = 0.0f;
   g.nseg = 0;
+  constexpr bool kShares = !kExact && S > 1;
+  float sd_loc = 0.0f, sd2_loc = 0.0f;  // this lane's shares (kShares)
   const float inv_grid = HALO ? __frcp_rn(P.grid) : 0.0f;
   const uint32_t spsw = P.steps_per_sweep;
   const uint64_t step0 = rp->steps;
@@ -413,6 +473,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       group_energies<L, kExact, true>(xs, P, cl, gmask, PER, lf, s, lnf, uo, un, pairs, err);
       const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
       note_drift(rp, writer, drift);
+      if (kShares) gather_shares<L>(g, sd_loc, sd2_loc, gmask);
       const double du = __dsub_rn(un, uo);
       const double arg = __dsub_rn(
           __dmul_rn(P.beta_d, __dadd_rn(du, __dmul_rn(P.p, __dsub_rn(lnew, L_box)))), logw);
@@ -458,11 +519,10 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       for (int q = 0; q < KPL; ++q) {
         const int k = kb + q * H2;
         const float xj = xs[nmc + side * k];  // a ghost beyond either end
-        const float dnw = side > 0 ? __fsub_rn(xj, xn) : __fsub_rn(xn, xj);
-        const float dol = side > 0 ? __fsub_rn(xj, xo) : __fsub_rn(xo, xj);
+        // xj - x and x - xj round to the same magnitude: the side needs no sign
+        const float dnw = __fsub_rn(xj, xn), dol = __fsub_rn(xj, xo);
         const float dn2 = __fmul_rn(dnw, dnw), do2 = __fmul_rn(dol, dol);
-        const float tq =
-            __fsub_rn(pair_energy_h<POT, kExact>(dn2, H), pair_energy_h<POT, kExact>(do2, H));
+        const float tq = pair_change<POT, kExact>(dn2, do2, H);
         t_lane = q == 0 ? tq : __fadd_rn(t_lane, tq);
         if (q == KPL - 1) sat = ok && k == W && (dn2 <= H.rc2 || do2 <= H.rc2);
       }
@@ -482,12 +542,9 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
             float shift2;
             const int j2 = window_index<PER, HALO>(nmc, side, k, n, lf, inr2, shift2);
             const float xj2 = __fadd_rn(xs[j2], shift2);
-            const float dn_2 = side > 0 ? __fsub_rn(xj2, xn) : __fsub_rn(xn, xj2);
-            const float do_2 = side > 0 ? __fsub_rn(xj2, xo) : __fsub_rn(xo, xj2);
+            const float dn_2 = __fsub_rn(xj2, xn), do_2 = __fsub_rn(xj2, xo);
             const float dn22 = __fmul_rn(dn_2, dn_2), do22 = __fmul_rn(do_2, do_2);
-            const float tq = inr2 ? __fsub_rn(pair_energy_h<POT, kExact>(dn22, H),
-                                              pair_energy_h<POT, kExact>(do22, H))
-                                  : 0.0f;
+            const float tq = inr2 ? pair_change<POT, kExact>(dn22, do22, H) : 0.0f;
             t2 = q == 0 ? tq : __fadd_rn(t2, tq);
             if (q == KPL - 1)
               sat2 = inr2 && k == (chunk + 1) * W && (dn22 <= H.rc2 || do22 <= H.rc2);
@@ -503,49 +560,46 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
         f = 1;
         overflows += 1;
       }
+      if (!kExact) de = __fmul_rn(de, H.eps4);  // the window sum of pair shapes
       const bool acc = ok && ((de <= 0.0f) || (__fmul_rn(de, H.beta) < thr));
       const unsigned accbits = (__ballot_sync(gmask, acc) >> lane_shift & kChainBits);
       if (S > 1 && f > 1) {
-        // lane w of slot s2 checks earlier slots s1 = w, w + G, ... for an
-        // accepted move within W index positions of its own particle.  With
-        // walls, a neighbour two or more places away matters only if the
-        // spans [old, trial] of the two particles come within the cut-off:
-        // otherwise every pair term between them is 0 before and after
-        // (FP32 rounding is monotone, so fl(gap)^2 > rc^2 bounds all four),
-        // and beyond W nothing changes since no particle passes another.
-        constexpr int R = (S + G - 1) / G;
-        bool cand[R];
-        int far[R];  // candidates two or more places away: index of the source lane
-        bool any_far = false;
+        // Step s2 is dropped, with every later one, if an earlier step s1 of
+        // the round was accepted within W index positions of its particle.
+        // With walls, a neighbour two or more places away matters only if
+        // the spans [old, trial] of the two particles come within the
+        // cut-off: otherwise every pair term between them is 0 before and
+        // after (FP32 rounding is monotone, so fl(gap)^2 > rc^2 bounds all
+        // four), and beyond W nothing changes since no particle passes
+        // another.  Each lane tests its pairs, set by set.
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-          const int s1 = wl + r * G;
-          const int src = (s1 < S ? s1 : 0) * G;
-          const int nm1 = __shfl_sync(gmask, nmc, src, L);
-          int dist = nm1 - nmc;
+          const int src1 = (int)(ptab[r] & 0xffu), src2 = (int)((ptab[r] >> 8) & 0xffu);
+          const int s2 = (int)(ptab[r] >> 16);
+          const int nm1 = __shfl_sync(gmask, nmc, src1, L);
+          const int nm2 = __shfl_sync(gmask, nmc, src2, L);
+          int dist = nm1 - nm2;
           dist = dist < 0 ? -dist : dist;
           if (PER) dist = min(dist, n - dist);
-          cand[r] = s1 < slot && ((accbits >> (s1 * G)) & 1u) && dist <= W;
-          far[r] = (!PER && cand[r] && dist >= 2) ? src : -1;
-          any_far = any_far || far[r] >= 0;
-        }
-        // the spans are compared only in the rounds that have such a candidate
-        if (!PER && __any_sync(gmask, any_far)) {
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            const int src = far[r] >= 0 ? far[r] : 0;
-            const float a0 = __shfl_sync(gmask, xo, src, L);
-            const float a1 = __shfl_sync(gmask, xn, src, L);
-            const float gap = fmaxf(__fsub_rn(fminf(a0, a1), fmaxf(xo, xn)),
-                                    __fsub_rn(fminf(xo, xn), fmaxf(a0, a1)));
-            if (far[r] >= 0 && gap > 0.0f && __fmul_rn(gap, gap) > H.rc2) cand[r] = false;
+          bool cand = s2 < S && ((accbits >> src1) & 1u) && dist <= W;
+          const bool far = !PER && cand && dist >= 2;
+          // the spans are compared only when some pair is such a candidate
+          if (!PER && __any_sync(gmask, far)) {
+            const float a0 = __shfl_sync(gmask, xo, src1, L);
+            const float a1 = __shfl_sync(gmask, xn, src1, L);
+            const float b0 = __shfl_sync(gmask, xo, src2, L);
+            const float b1 = __shfl_sync(gmask, xn, src2, L);
+            const float gap = fmaxf(__fsub_rn(fminf(a0, a1), fmaxf(b0, b1)),
+                                    __fsub_rn(fminf(b0, b1), fmaxf(a0, a1)));
+            if (far && gap > 0.0f && __fmul_rn(gap, gap) > H.rc2) cand = false;
+          }
+          const unsigned pbits = (__ballot_sync(gmask, cand) >> lane_shift & kChainBits);
+          if (pbits) {  // later sets hold later pairs
+            f = min(f, (uint32_t)__shfl_sync(gmask, s2, __ffs(pbits) - 1, L));
+            break;
           }
         }
-        bool conflict = false;
-#pragma unroll
-        for (int r = 0; r < R; ++r) conflict = conflict || cand[r];
-        const unsigned cbits = ((__ballot_sync(gmask, conflict) >> lane_shift & kChainBits)) | satbits;
-        const unsigned late = cbits & ~kSlotBits;  // slots 1 .. S-1
+        const unsigned late = satbits & ~kSlotBits;  // windows of slots 1 .. S-1 beyond W
         if (late) f = min(f, (uint32_t)(__ffs(late) - 1) / G);
       }
       // commit steps 0 .. f-1 in order: positions by every slot leader at
@@ -571,24 +625,18 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
           }
         }
       } else {
-        // the energy change after each kept step by a scan over the slots,
-        // its sum and sum of squares by a butterfly over the slots
+        // the energy change after each kept step by a scan over the slots
         float x = de_acc;
 #pragma unroll
         for (int o = 1; o < S; o <<= 1) {
           const float y = __shfl_up_sync(gmask, x, o * G, L);
           if (slot >= o) x = __fadd_rn(x, y);
         }
-        const float v = (uint32_t)slot < f ? __fadd_rn(g.delta, x) : 0.0f;
-        float sv = v, sv2 = __fmul_rn(v, v);
-#pragma unroll
-        for (int o = 1; o < S; o <<= 1) {
-          sv = __fadd_rn(sv, __shfl_xor_sync(gmask, sv, o * G, L));
-          sv2 = __fadd_rn(sv2, __shfl_xor_sync(gmask, sv2, o * G, L));
-        }
+        // the slot leaders of kept steps add their step's share
+        const float v = ((uint32_t)slot < f && wl == 0) ? __fadd_rn(g.delta, x) : 0.0f;
+        sd_loc = __fadd_rn(sd_loc, v);
+        sd2_loc = __fmaf_rn(v, v, sd2_loc);
         g.delta = __fadd_rn(g.delta, __shfl_sync(gmask, x, (int)(f - 1) * G, L));
-        g.sd = __fadd_rn(g.sd, sv);
-        g.sd2 = __fadd_rn(g.sd2, sv2);
       }
       __syncwarp(gmask);
       const unsigned okbits = (__ballot_sync(gmask, ok) >> lane_shift & kChainBits);
@@ -608,11 +656,13 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
                                          err);
         const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
         note_drift(rp, writer, drift);
+        if (kShares) gather_shares<L>(g, sd_loc, sd2_loc, gmask);
         fold(g, rp, writer, L_box, (uint32_t)n);
         g.e0 = uo;
       }
     }
   }
+  if (kShares) gather_shares<L>(g, sd_loc, sd2_loc, gmask);
   fold(g, rp, writer, L_box, (uint32_t)n);
   if (!isfinite(g.e0)) err = JMM_ERR_NUMERIC;
   if (writer) {

@@ -69,7 +69,7 @@ EXACT_CASES = {
 }
 
 
-SHAPES = [(4, 8), (4, 4), (4, 2), (8, 4), (8, 2), (16, 2), (16, 1), (32, 1)]
+SHAPES = [(4, 8), (2, 16), (4, 4), (4, 2), (8, 4), (8, 2), (16, 2), (16, 1), (32, 1)]
 
 
 @pytest.mark.parametrize("shape", SHAPES, ids=[f"{g}x{s}" for g, s in SHAPES])
