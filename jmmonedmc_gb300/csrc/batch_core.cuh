@@ -44,7 +44,9 @@ namespace jmm {
 namespace batch {
 
 constexpr int kRingSteps = 32;  // Philox words drawn ahead per chain
-constexpr int kRingWords = 3 * kRingSteps;
+// One 16-byte record per step (particle index, displacement or volume
+// uniform, Metropolis threshold, unused), read with one shared-memory load.
+constexpr int kRingWords = 4 * kRingSteps;
 // Ghost slots on each side of a chain's positions in shared memory: far
 // sentinels between hard walls, periodic images on a ring, so that the
 // neighbour window is read without bounds tests.
@@ -185,10 +187,11 @@ struct Seg {
   uint32_t nseg;   // steps sampled in the segment
 };
 
-// Folds the segment into the chain's FP64 sums; the record lives in HBM and
-// only the chain's first lane (`writer`) updates it.
+// Folds the segment into the chain's FP64 sums at box length l and density
+// rho = n / l; the record lives in HBM and only the chain's first lane
+// (`writer`) updates it.
 __device__ __forceinline__ void fold(Seg &g, jmm_chain_result *__restrict__ rp, bool writer,
-                                     double l, uint32_t n) {
+                                     double l, double rho) {
   if (writer) {
     const double nd = (double)g.nseg;
     const double sdd = (double)g.sd, sd2d = (double)g.sd2;
@@ -201,7 +204,6 @@ __device__ __forceinline__ void fold(Seg &g, jmm_chain_result *__restrict__ rp, 
     rp->sum_l = __dadd_rn(rp->sum_l, __dmul_rn(nd, l));
     rp->sum_l2 = __dadd_rn(rp->sum_l2, __dmul_rn(__dmul_rn(nd, l), l));
     rp->sum_le = __dadd_rn(rp->sum_le, __dmul_rn(l, lin));
-    const double rho = __ddiv_rn((double)n, l);
     rp->sum_rho = __dadd_rn(rp->sum_rho, __dmul_rn(nd, rho));
     rp->sum_rho2 = __dadd_rn(rp->sum_rho2, __dmul_rn(__dmul_rn(nd, rho), rho));
     rp->samples += g.nseg;
@@ -279,6 +281,72 @@ template <bool kExact>
 __device__ __forceinline__ float threshold_of(uint32_t w) {
   const float u = __fmul_rn(__fadd_rn((float)(w >> 9), 0.5f), 1.1920929e-07f);  // 2^-23
   return kExact ? -portable_logf(u) : -__logf(u);
+}
+
+// group_energies for the step loop: potential and boundary fixed at compile
+// time.  EXACT precision sums in the same order (per-particle FP32, lane and
+// chain FP64); FAST sums each lane's pair shapes in FP32, scales them by eps4
+// in FP64 and sums the lanes in FP64.
+template <int L, int POT, bool PER, bool kExact, bool kScaled>
+__device__ __noinline__ void chain_energies(const float *xs, const Hot &H, int n, int gl,
+                                               unsigned gmask, float lf, float s, float lnf,
+                                               double &u_old, double &u_new, uint64_t &pairs,
+                                               uint32_t &err) {
+  double uo = 0.0, un = 0.0;
+  float fo = 0.0f, fn = 0.0f;  // FAST: the lane's shape sums
+  uint32_t cnt = 0;
+  for (int i = gl; i < n; i += L) {
+    const float xi = xs[i];
+    const float xin = kScaled ? __fmul_rn(xi, s) : xi;
+    float eo = 0.0f, en = 0.0f;
+    for (int k = 1;; ++k) {
+      int j = i + k;
+      float shift = 0.0f, shiftn = 0.0f;
+      if (!PER) {
+        if (j >= n) break;
+      } else {
+        if (2 * k > n - 1) {  // the window reached half the ring: images would overlap
+          err = JMM_ERR_INVALID;
+          break;
+        }
+        if (j >= n) {
+          j -= n;
+          shift = lf;
+          shiftn = lnf;
+        }
+      }
+      const float xj = xs[j];
+      // with walls the shifts are 0 and adding them changes no bit
+      const float d = __fsub_rn(PER ? __fadd_rn(xj, shift) : xj, xi);
+      const float d2 = __fmul_rn(d, d);
+      float dn2 = d2;
+      if (kScaled) {
+        const float xjs = __fmul_rn(xj, s);
+        const float dn = __fsub_rn(PER ? __fadd_rn(xjs, shiftn) : xjs, xin);
+        dn2 = __fmul_rn(dn, dn);
+      }
+      if (d2 > H.rc2 && dn2 > H.rc2) break;
+      if (kExact) {
+        eo = __fadd_rn(eo, pair_energy_h<POT, true>(d2, H));
+        if (kScaled) en = __fadd_rn(en, pair_energy_h<POT, true>(dn2, H));
+      } else {
+        fo = __fadd_rn(fo, pair_shape_fast<POT>(d2, H));
+        if (kScaled) fn = __fadd_rn(fn, pair_shape_fast<POT>(dn2, H));
+      }
+      cnt += kScaled ? 2 : 1;
+    }
+    if (kExact) {
+      uo = __dadd_rn(uo, (double)eo);
+      if (kScaled) un = __dadd_rn(un, (double)en);
+    }
+  }
+  if (!kExact) {
+    uo = __dmul_rn((double)H.eps4, (double)fo);
+    un = __dmul_rn((double)H.eps4, (double)fn);
+  }
+  u_old = group_sum_d<L>(uo, gmask);
+  u_new = kScaled ? group_sum_d<L>(un, gmask) : u_old;
+  pairs += __reduce_add_sync(gmask, cnt);
 }
 
 // Neighbour index of window lane (side, k), clamped for loads, and its
@@ -375,9 +443,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
     ptab[r] = (uint32_t)(p1 * G) | ((uint32_t)((p2 < S ? p2 : 0) * G) << 8) | ((uint32_t)p2 << 16);
   }
   const bool writer = cl == 0;
-  int32_t *ring_nm = reinterpret_cast<int32_t *>(ring);
-  float *ring_md = reinterpret_cast<float *>(ring + kRingSteps);  // md, or u1 of a volume step
-  float *ring_thr = reinterpret_cast<float *>(ring + 2 * kRingSteps);
+  uint4 *ring_rec = reinterpret_cast<uint4 *>(ring);  // 16-byte aligned: see kRingWords
   Hot H;
   H.eps4 = P.eps4;
   H.sigma2 = P.sigma2;
@@ -391,6 +457,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
   const bool per_sweep = cfg.vol_schedule == JMM_VOLSCHED_SWEEP;
   double L_box = rp->l;
   float lf = (float)L_box, half_l = (float)__dmul_rn(L_box, 0.5);
+  double rho_box = __ddiv_rn((double)n, L_box);  // n / L, renewed when L changes
   Seg g;
   g.e0 = rp->e;
   g.delta = 0.0f;
@@ -406,7 +473,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
   uint32_t sweeps_since_resum = 0;
   uint32_t err = rp->error;
   uint64_t pairs = rp->pair_evals;
-  uint32_t pairs32 = 0;  // displacement pair energies of this launch
+  uint32_t ok_loc = 0;  // window chunks of this lane's kept steps (4 W pair energies each)
   uint32_t d_acc = 0, d_att = 0, v_acc = 0, v_att = 0, overflows = 0;
   const uint32_t total = (uint32_t)(cfg.n_sweeps * (uint64_t)spsw);
   __syncwarp(gmask);  // every lane has read the record before lane 0 updates it
@@ -417,6 +484,9 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
     if (!ring_valid || base + S > pbase + kRingSteps) {
       pbase = base;
       __syncwarp(gmask);
+      // ring offset of the next sweep-closing volume step; later ones follow
+      // every spsw steps
+      const uint32_t e_vol = spsw - 1u - sweep_pos;
       for (int e = cl; e < kRingSteps; e += L) {
         const Words4 w = step_words(cfg.seed, step0 + pbase + e + 1, P.id);
         const float u1 = word_to_unit_f(w.w[1]);
@@ -425,13 +495,14 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
           nm_e = (int)word_to_index(w.w[0], (uint64_t)n + 1);
         } else {
           nm_e = (int)word_to_index(w.w[0], (uint64_t)n);
-          if (npt && (sweep_pos + (uint32_t)e + 1) % spsw == 0) nm_e = n;  // the sweep's volume step
+          if (npt && (uint32_t)e >= e_vol &&
+              (spsw >= (uint32_t)kRingSteps ? (uint32_t)e == e_vol : ((uint32_t)e - e_vol) % spsw == 0))
+            nm_e = n;  // the sweep's volume step
         }
-        ring_nm[e] = nm_e;
         float md_e = __fmul_rn(__fsub_rn(u1, 0.5f), H.two_max_step);
         if (HALO) md_e = __fmul_rn(rintf(__fmul_rn(md_e, inv_grid)), P.grid);  // exact: 2^k scales
-        ring_md[e] = nm_e == n ? u1 : md_e;
-        ring_thr[e] = threshold_of<kExact>(w.w[2]);
+        ring_rec[e] = make_uint4((uint32_t)nm_e, __float_as_uint(nm_e == n ? u1 : md_e),
+                                 __float_as_uint(threshold_of<kExact>(w.w[2])), 0u);
       }
       __syncwarp(gmask);
       ring_valid = true;
@@ -439,10 +510,10 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
     uint32_t rem = total - base;
     if (rem > (uint32_t)S) rem = S;
     if (rem > spsw - sweep_pos) rem = spsw - sweep_pos;
-    const uint32_t ri = base + slot - pbase;  // < 32
-    const int nm = ring_nm[ri];
-    const float u1 = ring_md[ri];  // md of a displacement, u1 of a volume step
-    const float thr = ring_thr[ri];
+    const uint4 rec = ring_rec[base + slot - pbase];  // offset < 32
+    const int nm = (int)rec.x;
+    const float u1 = __uint_as_float(rec.y);  // md of a displacement, u1 of a volume step
+    const float thr = __uint_as_float(rec.z);
     const bool isvol = nm == n;
     const unsigned volbits =
         (__ballot_sync(gmask, isvol && wl == 0 && (uint32_t)slot < rem) >> lane_shift & kChainBits);
@@ -470,7 +541,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       }
       double uo, un;
       const float lnf = (float)lnew;
-      group_energies<L, kExact, true>(xs, P, cl, gmask, PER, lf, s, lnf, uo, un, pairs, err);
+      chain_energies<L, POT, PER, kExact, true>(xs, H, n, cl, gmask, lf, s, lnf, uo, un, pairs, err);
       const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
       note_drift(rp, writer, drift);
       if (kShares) gather_shares<L>(g, sd_loc, sd2_loc, gmask);
@@ -480,11 +551,12 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       bool acc = arg < (double)thr_0;
       if (!(lnew > 0.0)) acc = false;
       if (PER && !(lnew > 2.0 * (double)P.rc)) acc = false;
-      fold(g, rp, writer, L_box, (uint32_t)n);
+      fold(g, rp, writer, L_box, rho_box);
       v_att += 1;
       if (acc) {
         for (int i = cl; i < n; i += L) xs[i] = __fmul_rn(xs[i], s);
         L_box = lnew;
+        rho_box = __ddiv_rn((double)n, L_box);
         lf = (float)L_box;
         half_l = (float)__dmul_rn(L_box, 0.5);
         if (PER) {
@@ -639,9 +711,9 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
         g.delta = __fadd_rn(g.delta, __shfl_sync(gmask, x, (int)(f - 1) * G, L));
       }
       __syncwarp(gmask);
-      const unsigned okbits = (__ballot_sync(gmask, ok) >> lane_shift & kChainBits);
+      // this slot leader's kept step with its window chunks (pair energies)
+      if (wl == 0 && (uint32_t)slot < f && ok) ok_loc += 1u + (slot == 0 ? extra_chunks : 0u);
       d_acc += __popc(accbits & committed);
-      pairs32 += (uint32_t)(4 * W) * (__popc(okbits & committed) + ((okbits & 1u) ? extra_chunks : 0u));
       d_att += f;
       g.nseg += f;
       base += f;
@@ -652,24 +724,25 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       if (!npt && cfg.resum_sweeps > 0 && ++sweeps_since_resum >= (uint32_t)cfg.resum_sweeps) {
         sweeps_since_resum = 0;
         double uo, un;
-        group_energies<L, kExact, false>(xs, P, cl, gmask, PER, lf, 1.0f, lf, uo, un, pairs,
-                                         err);
+        chain_energies<L, POT, PER, kExact, false>(xs, H, n, cl, gmask, lf, 1.0f, lf, uo, un, pairs,
+                                                   err);
         const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
         note_drift(rp, writer, drift);
         if (kShares) gather_shares<L>(g, sd_loc, sd2_loc, gmask);
-        fold(g, rp, writer, L_box, (uint32_t)n);
+        fold(g, rp, writer, L_box, rho_box);
         g.e0 = uo;
       }
     }
   }
   if (kShares) gather_shares<L>(g, sd_loc, sd2_loc, gmask);
-  fold(g, rp, writer, L_box, (uint32_t)n);
+  fold(g, rp, writer, L_box, rho_box);
   if (!isfinite(g.e0)) err = JMM_ERR_NUMERIC;
+  const uint32_t ok_sum = __reduce_add_sync(gmask, ok_loc);
   if (writer) {
     rp->e = g.e0;
     rp->l = L_box;
     rp->steps = step0 + total;
-    rp->pair_evals = pairs + pairs32;
+    rp->pair_evals = pairs + (uint64_t)(4 * W) * ok_sum;
     rp->disp_acc += d_acc;
     rp->disp_att += d_att;
     rp->vol_acc += v_acc;
@@ -692,7 +765,7 @@ __global__ void __maxnreg__(G * S == 32 ? 72 : 128) chains_kernel(const ChainPar
                                                      jmm_chain_result *__restrict__ res,
                                                      float *__restrict__ xg, KernelCfg cfg) {
   constexpr int L = G * S;
-  extern __shared__ float smem[];
+  extern __shared__ __align__(16) float smem[];
   const int cl = threadIdx.x % L;
   const int cw = (threadIdx.x & 31) / L;
   const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << (cw * L));

@@ -55,6 +55,12 @@ namespace {
 
 constexpr int kG = 4, kS = 8;  // the batched kernel's default launch shape
 constexpr int kWarpsPerBlock = 4;
+// Shared words of one domain warp: its step ring, then its particles with
+// their halo, padded to 16 bytes so that the next warp's ring records stay
+// aligned.
+__host__ __device__ constexpr uint32_t warp_words(uint32_t b) {
+  return (uint32_t)kRingWords + ((b + 2u * kGhost + 3u) & ~3u);
+}
 constexpr int kSeqSide = 16;   // neighbours per side per pass, sequential sweep
 constexpr uint32_t kStatWarps = 8;
 
@@ -134,7 +140,7 @@ __global__ void __maxnreg__(72)
     domain_kernel(const LargeChain *__restrict__ chains, const LargeState *__restrict__ states,
                   jmm_chain_result *__restrict__ rec, int64_t *__restrict__ q, uint32_t n_chains,
                   uint32_t b, uint32_t phase, uint32_t doms_per_chain, KernelCfg cfg) {
-  extern __shared__ float smem[];
+  extern __shared__ __align__(16) float smem[];
   const uint32_t wib = threadIdx.x / 32;
   const uint64_t warp = (uint64_t)blockIdx.x * kWarpsPerBlock + wib;
   const uint32_t c = (uint32_t)(warp / doms_per_chain);
@@ -182,7 +188,7 @@ __global__ void __maxnreg__(72)
     if (cl == 0) rp->error |= JMM_ERR_INVALID;
     return;
   }
-  uint32_t *ring = reinterpret_cast<uint32_t *>(smem) + wib * (kRingWords + b + 2 * kGhost);
+  uint32_t *ring = reinterpret_cast<uint32_t *>(smem) + wib * warp_words(b);
   float *xs = reinterpret_cast<float *>(ring + kRingWords) + kGhost;
   for (int i = cl - kGhost; i < n + kGhost; i += 32) xs[i] = q_to_f(qc[i] - O, ch.grid);
   if (cl == 0) rp->l = (left_wall || right_wall) ? __dmul_rn(2.0, (double)q_to_f(H, ch.grid)) : 2e30;
@@ -412,7 +418,7 @@ void launch_phase(const LargeChain *d_chains, const LargeState *d_states, jmm_ch
                   const KernelCfg &kc, cudaStream_t s) {
   const uint64_t warps = (uint64_t)n_chains * doms_per_chain;
   const uint32_t blocks = (uint32_t)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock);
-  const size_t smem = (size_t)kWarpsPerBlock * (kRingWords + b + 2 * kGhost) * sizeof(float);
+  const size_t smem = (size_t)kWarpsPerBlock * warp_words(b) * sizeof(float);
   domain_kernel<POT><<<blocks, 32 * kWarpsPerBlock, smem, s>>>(d_chains, d_states, d_rec, d_q,
                                                                n_chains, b, phase, doms_per_chain, kc);
 }
@@ -673,7 +679,7 @@ extern "C" int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_des
     e = cudaMemcpy(h->d_rec, recs.data(), n_rec * sizeof(jmm_chain_result), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(h->d_states, st.data(), n_chains * sizeof(LargeState), cudaMemcpyHostToDevice);
-  const size_t smem = (size_t)kWarpsPerBlock * (kRingWords + domain_size + 2 * kGhost) * sizeof(float);
+  const size_t smem = (size_t)kWarpsPerBlock * warp_words(domain_size) * sizeof(float);
   if (e == cudaSuccess && smem > 48 * 1024) {
     e = cudaFuncSetAttribute(domain_kernel<JMM_POT_LJCUT>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -64,7 +64,11 @@ __host__ __device__ __forceinline__ Words4 step_words(uint64_t seed, uint64_t bl
 
 __host__ __device__ __forceinline__ uint64_t word_to_index(uint32_t w, uint64_t n) {
   // n < 2^32 always holds here (particle counts), so the product fits 64 bits.
+#if defined(__CUDA_ARCH__)
+  return __umulhi(w, (uint32_t)n);
+#else
   return ((uint64_t)w * n) >> 32;
+#endif
 }
 
 __host__ __device__ __forceinline__ double word_to_unit(uint32_t w) {
