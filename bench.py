@@ -741,7 +741,8 @@ def run_ours(args, rank, world, local_rank):
         lanes, spr, cpb = b.autotune(trial_sweeps=5)
     class_names = {abi.JMM_POT_LJCUT: "ljcut", abi.JMM_POT_SOFTSPHERE: "softsphere",
                    abi.JMM_POT_GAUSS: "gauss"}
-    class_shapes = {class_names[p]: "%dx%d, %d per block" % v for p, v in b.shapes().items()}
+    class_shapes = {class_names[p]: "%dx%d, %d per block, window %d" % v
+                    for p, v in b.shapes().items()}
     # a stream of our own: torch's default stream is the legacy stream, whose
     # handle (0) would not name it to the library
     stream = torch.cuda.Stream(dev)
@@ -798,7 +799,8 @@ def run_ours(args, rank, world, local_rank):
                                     resum_sweeps=cfg.resum_sweeps,
                                     lanes_per_chain=lanes if one_class else 0,
                                     steps_per_round=spr if one_class else 0,
-                                    chains_per_block=cpb if one_class else 0)
+                                    chains_per_block=cpb if one_class else 0,
+                                    window=next(iter(b.shapes().values()))[3] if one_class else 0)
     e2e_times, e2e_moves = [], 0
     for _ in range(args.e2e_steps):
         torch.cuda.synchronize(dev)

@@ -256,18 +256,23 @@ typedef struct jmm_batch_config {
   int32_t precision;         /* JMM_PREC_*                                      */
   uint32_t resum_sweeps;     /* constant-L chains: FP64 re-sum of E every this
                                 many sweeps (0 = only at the end of a run)      */
-  uint32_t lanes_per_chain;  /* lanes G of one trial move: 4, 8, 16 or 32; they
-                                look at W = max(4, G/2) neighbours per side;
+  uint32_t lanes_per_chain;  /* lanes G of one trial move: 2, 4, 8, 16 or 32;
                                 0 = 4 in EXACT precision, and in FAST a default
-                                per potential class from its densest chain
-                                (4, or 16 / 32 where more neighbours fall
-                                within the cut-off)                             */
+                                shape per potential class from its densest and
+                                its longest chain (4x8, or 2x16 with a chain
+                                of 1024 or more; window 8 where more than 4
+                                neighbours per side fall within the cut-off;
+                                32x1 beyond 8)                                  */
   uint32_t steps_per_round;  /* S steps evaluated at once per chain: G x S is
-                                4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or 32x1;
-                                0 = 32/G                                        */
+                                2x16, 4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or
+                                32x1; 0 = 32/G                                  */
   uint32_t chains_per_block; /* 0 = 128 / (G*S)                                 */
   int32_t init;              /* JMM_INIT_*                                      */
   double jitter;             /* half-width of the initial jitter               */
+  uint32_t window;           /* neighbours W per side a trial move looks at
+                                before it extends its window: 0 = max(4, G/2);
+                                8 with the shapes 2x16, 4x8 and 8x4            */
+  uint32_t reserved;         /* 0                                               */
 } jmm_batch_config;
 
 /* Per-chain state and statistics, FP64 (also the device-side record). */
@@ -311,8 +316,8 @@ int jmm_batch_device_views(jmm_batch *b, void **positions, void **results,
 int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t *lanes_per_chain,
                        uint32_t *steps_per_round, uint32_t *chains_per_block);
 /* The launch shape of each potential class (LJcut, soft sphere, Gaussian
- * core): shapes[3k .. 3k+2] = lanes, steps per round, chains per block; 0 for
- * a class without chains. */
+ * core): shapes[4k .. 4k+3] = lanes, steps per round, chains per block,
+ * neighbours per side; 0 for a class without chains (n = 12). */
 int jmm_batch_shapes(jmm_batch *b, uint32_t *shapes, uint32_t n);
 /* Step-size adjustment on the device, enqueued on the batch's stream
  * (maxDisAdjust / maxDVAdjust, src/jmmMCState.cpp:2100-2139, per chain from

@@ -165,12 +165,12 @@ class ChainBatch:
         return g.value, s.value, c.value
 
     def shapes(self):
-        """{potential: (lanes, steps per round, chains per block)} of the classes
-        present (LJcut, soft sphere, Gaussian core)."""
-        out = (C.c_uint32 * 9)()
-        _native.call("jmm_batch_shapes", self._h, out, 9)
+        """{potential: (lanes, steps per round, chains per block, neighbours
+        per side)} of the classes present (LJcut, soft sphere, Gaussian core)."""
+        out = (C.c_uint32 * 12)()
+        _native.call("jmm_batch_shapes", self._h, out, 12)
         pots = (abi.JMM_POT_LJCUT, abi.JMM_POT_SOFTSPHERE, abi.JMM_POT_GAUSS)
-        return {p: tuple(out[3 * k:3 * k + 3]) for k, p in enumerate(pots) if out[3 * k]}
+        return {p: tuple(out[4 * k:4 * k + 4]) for k, p in enumerate(pots) if out[4 * k]}
 
 
 def run_host(config, chains, n_sweeps, x_in=None):

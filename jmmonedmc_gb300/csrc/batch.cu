@@ -27,30 +27,39 @@ constexpr size_t kMaxSmem = 227 * 1024;
 
 typedef void (*ChainsKernel)(const ChainParams *, jmm_chain_result *, float *, KernelCfg);
 
-template <int G, int S, bool E>
+template <int G, int S, bool E, int WIN = window_of(G)>
 ChainsKernel pick_pot(int pot, bool per) {
   switch (pot * 2 + (per ? 1 : 0)) {
-    case JMM_POT_LJCUT * 2: return chains_kernel<G, S, JMM_POT_LJCUT, false, E>;
-    case JMM_POT_LJCUT * 2 + 1: return chains_kernel<G, S, JMM_POT_LJCUT, true, E>;
-    case JMM_POT_SOFTSPHERE * 2: return chains_kernel<G, S, JMM_POT_SOFTSPHERE, false, E>;
-    case JMM_POT_SOFTSPHERE * 2 + 1: return chains_kernel<G, S, JMM_POT_SOFTSPHERE, true, E>;
-    case JMM_POT_GAUSS * 2: return chains_kernel<G, S, JMM_POT_GAUSS, false, E>;
-    case JMM_POT_GAUSS * 2 + 1: return chains_kernel<G, S, JMM_POT_GAUSS, true, E>;
+    case JMM_POT_LJCUT * 2: return chains_kernel<G, S, JMM_POT_LJCUT, false, E, WIN>;
+    case JMM_POT_LJCUT * 2 + 1: return chains_kernel<G, S, JMM_POT_LJCUT, true, E, WIN>;
+    case JMM_POT_SOFTSPHERE * 2: return chains_kernel<G, S, JMM_POT_SOFTSPHERE, false, E, WIN>;
+    case JMM_POT_SOFTSPHERE * 2 + 1: return chains_kernel<G, S, JMM_POT_SOFTSPHERE, true, E, WIN>;
+    case JMM_POT_GAUSS * 2: return chains_kernel<G, S, JMM_POT_GAUSS, false, E, WIN>;
+    case JMM_POT_GAUSS * 2 + 1: return chains_kernel<G, S, JMM_POT_GAUSS, true, E, WIN>;
     default: return nullptr;
   }
 }
 
-// Launch shapes: G window lanes x S steps per round, G*S = 16 or 32 lanes.
-ChainsKernel pick_kernel(uint32_t g, uint32_t s, bool exact, int pot, bool per) {
-  if (g == 4 && s == 4) return exact ? pick_pot<4, 4, true>(pot, per) : pick_pot<4, 4, false>(pot, per);
-  if (g == 4 && s == 2) return exact ? pick_pot<4, 2, true>(pot, per) : pick_pot<4, 2, false>(pot, per);
-  if (g == 4 && s == 8) return exact ? pick_pot<4, 8, true>(pot, per) : pick_pot<4, 8, false>(pot, per);
-  if (g == 2 && s == 16) return exact ? pick_pot<2, 16, true>(pot, per) : pick_pot<2, 16, false>(pot, per);
-  if (g == 8 && s == 4) return exact ? pick_pot<8, 4, true>(pot, per) : pick_pot<8, 4, false>(pot, per);
-  if (g == 8 && s == 2) return exact ? pick_pot<8, 2, true>(pot, per) : pick_pot<8, 2, false>(pot, per);
-  if (g == 16 && s == 2) return exact ? pick_pot<16, 2, true>(pot, per) : pick_pot<16, 2, false>(pot, per);
-  if (g == 16 && s == 1) return exact ? pick_pot<16, 1, true>(pot, per) : pick_pot<16, 1, false>(pot, per);
-  if (g == 32 && s == 1) return exact ? pick_pot<32, 1, true>(pot, per) : pick_pot<32, 1, false>(pot, per);
+// Launch shapes: G window lanes x S steps per round (G*S = 16 or 32 lanes),
+// W neighbours per side (0 = the default of G).
+ChainsKernel pick_kernel(uint32_t g, uint32_t s, uint32_t w, bool exact, int pot, bool per) {
+  if (w == 0) w = (uint32_t)window_of((int)g);
+#define JMM_SHAPE(G_, S_, W_)                                                        \
+  if (g == G_ && s == S_ && w == W_)                                                \
+    return exact ? pick_pot<G_, S_, true, W_>(pot, per) : pick_pot<G_, S_, false, W_>(pot, per);
+  JMM_SHAPE(4, 8, 4)
+  JMM_SHAPE(2, 16, 4)
+  JMM_SHAPE(4, 4, 4)
+  JMM_SHAPE(4, 2, 4)
+  JMM_SHAPE(8, 4, 4)
+  JMM_SHAPE(8, 2, 4)
+  JMM_SHAPE(16, 2, 8)
+  JMM_SHAPE(16, 1, 8)
+  JMM_SHAPE(32, 1, 16)
+  JMM_SHAPE(4, 8, 8)
+  JMM_SHAPE(2, 16, 8)
+  JMM_SHAPE(8, 4, 8)
+#undef JMM_SHAPE
   return nullptr;
 }
 
@@ -58,9 +67,10 @@ constexpr int kPots[3] = {JMM_POT_LJCUT, JMM_POT_SOFTSPHERE, JMM_POT_GAUSS};
 
 // The chains of one potential: a contiguous range of launch slots with its
 // own blocks and shared-memory size.
-// A launch shape: G window lanes x S steps per round, chains per block.
+// A launch shape: G window lanes x S steps per round, chains per block, W
+// neighbours per side.
 struct Shape {
-  uint32_t g, spr, cpb;
+  uint32_t g, spr, cpb, w;
 };
 
 struct PotClass {
@@ -87,8 +97,8 @@ struct jmm_batch {
   jmm_chain_result *d_res = nullptr;
   float *d_x = nullptr;
   double *d_e = nullptr;
-  uint32_t g = 8, spr = 4, cpb = 4, n_blocks = 0;  // the shape of the largest class
-  Shape shapes[3] = {{8, 4, 4}, {8, 4, 4}, {8, 4, 4}};  // per potential class (kPots order)
+  uint32_t g = 8, spr = 4, cpb = 4, win = 4, n_blocks = 0;  // the shape of the largest class
+  Shape shapes[3] = {{8, 4, 4, 4}, {8, 4, 4, 4}, {8, 4, 4, 4}};  // per potential class (kPots order)
   size_t smem = 0;
   cudaStream_t stream = nullptr;
   std::map<uint64_t, cudaGraphExec_t> graphs;  // n_sweeps -> instantiated run
@@ -161,23 +171,25 @@ static int apply_layout(jmm_batch *b, const Shape shapes[3]) {
   for (int pi = 0; pi < 3; ++pi) {
     const int pot = kPots[pi];
     const uint32_t g = shapes[pi].g, spr = shapes[pi].spr, cpb = shapes[pi].cpb;
-    if (!pick_kernel(g, spr, false, JMM_POT_LJCUT, false))
+    const uint32_t win = shapes[pi].w ? shapes[pi].w : (uint32_t)window_of((int)g);
+    if (!pick_kernel(g, spr, win, false, JMM_POT_LJCUT, false))
       return fail(JMM_ERR_INVALID, "unsupported launch shape: lanes_per_chain x steps_per_round "
-                  "must be 2x16, 4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or 32x1");
+                  "must be 2x16, 4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or 32x1, with a window "
+                  "of 0 (the default) or 8 for 2x16, 4x8 and 8x4");
     if (cpb == 0 || cpb * g * spr > 256)
       return fail(JMM_ERR_INVALID, "chains_per_block * lanes per chain must be <= 256");
     const uint64_t ring_floats = (uint64_t)cpb * kRingWords;
     PotClass pc;
     pc.pot = pot;
     pc.shape = shapes[pi];
+    pc.shape.w = win;
     pc.first = slot0;
     pc.count = 0;
     while (slot0 + pc.count < b->n_chains && b->chains[b->order[slot0 + pc.count]].potential == pot)
       pc.count++;
     if (per) {
-      const uint32_t w = (uint32_t)window_of((int)g);
       for (uint32_t k = 0; k < pc.count; ++k)
-        if (b->chains[b->order[pc.first + k]].n < 2 * w + 1)
+        if (b->chains[b->order[pc.first + k]].n < 2 * win + 1)
           return fail(JMM_ERR_INVALID, "periodic chains need N > twice the neighbour window");
     }
     pc.n_blocks = (pc.count + cpb - 1) / cpb;
@@ -216,7 +228,7 @@ static int apply_layout(jmm_batch *b, const Shape shapes[3]) {
       return fail(JMM_ERR_INVALID, "a block's chains need %zu bytes of shared memory (max %zu): "
                   "lower chains_per_block", pc.smem, kMaxSmem);
     if (pc.count) {
-      ChainsKernel kf = pick_kernel(g, spr, exact, pot, per);
+      ChainsKernel kf = pick_kernel(g, spr, win, exact, pot, per);
       JMM_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
       classes.push_back(pc);
     }
@@ -227,22 +239,51 @@ static int apply_layout(jmm_batch *b, const Shape shapes[3]) {
   b->params.swap(prm);
   b->classes.swap(classes);
   uint32_t most = 0;
-  for (int pi = 0; pi < 3; ++pi) b->shapes[pi] = shapes[pi];
+  for (int pi = 0; pi < 3; ++pi) {
+    b->shapes[pi] = shapes[pi];
+    if (!b->shapes[pi].w) b->shapes[pi].w = (uint32_t)window_of((int)shapes[pi].g);
+  }
   for (const PotClass &pc : b->classes) {
     if (pc.count > most) {
       most = pc.count;
       b->g = pc.shape.g;
       b->spr = pc.shape.spr;
       b->cpb = pc.shape.cpb;
+      b->win = pc.shape.w;
     }
   }
   drop_graphs(b);
   return JMM_OK;
 }
 
+// The FAST default launch shape of each potential class (kPots order).
+static void default_shapes(const jmm_batch *b, Shape sh[3]) {
+  // From the densest chain's neighbours within the cut-off and the longest
+  // chain.  A 12-power core keeps LJ and soft-sphere neighbours at least
+  // ~0.85 sigma apart, a Gaussian core lets them overlap (about 1.5 rho rc
+  // per side at the densest).  Windows of 4 or 8 per side take 8 steps per
+  // round, or 16 where the class holds a chain of 1024 or more particles (a
+  // class lasts as long as its longest chain, whose rounds rarely conflict).
+  for (int pi = 0; pi < 3; ++pi) {
+    double need = 0.0;
+    uint32_t n_max = 0;
+    for (const auto &c : b->chains) {
+      if (c.potential != kPots[pi]) continue;
+      const double side = c.potential == JMM_POT_GAUSS ? 1.5 * c.n / c.l0 * c.cutoff
+                                                       : c.cutoff / (0.85 * c.sigma);
+      need = std::max(need, side);
+      n_max = std::max(n_max, c.n);
+    }
+    const uint32_t gg = need > 8.0 ? 32u : (n_max >= 1024 ? 2u : 4u);
+    const uint32_t ss = 32 / gg;
+    const uint32_t ww = need > 8.0 ? 16u : (need > 4.0 ? 8u : 4u);
+    sh[pi] = Shape{gg, ss, 128 / (gg * ss), ww};
+  }
+}
+
 // The same launch shape for every class.
-static int apply_layout(jmm_batch *b, uint32_t g, uint32_t spr, uint32_t cpb) {
-  const Shape sh[3] = {{g, spr, cpb}, {g, spr, cpb}, {g, spr, cpb}};
+static int apply_layout(jmm_batch *b, uint32_t g, uint32_t spr, uint32_t cpb, uint32_t w) {
+  const Shape sh[3] = {{g, spr, cpb, w}, {g, spr, cpb, w}, {g, spr, cpb, w}};
   return apply_layout(b, sh);
 }
 
@@ -263,7 +304,7 @@ static int launch_class(jmm_batch *b, size_t k, uint64_t n_sweeps, cudaStream_t 
   const bool per = b->cfg.boundary == JMM_BOUNDARY_PERIODIC;
   const bool exact = b->cfg.precision == JMM_PREC_EXACT;
   const uint32_t threads = pc.shape.g * pc.shape.spr * pc.shape.cpb;
-  ChainsKernel kf = pick_kernel(pc.shape.g, pc.shape.spr, exact, pc.pot, per);
+  ChainsKernel kf = pick_kernel(pc.shape.g, pc.shape.spr, pc.shape.w, exact, pc.pot, per);
   kf<<<pc.n_blocks, threads, pc.smem, st>>>(b->d_params + pc.first, b->d_res, b->d_x, kc);
   JMM_CUDA(cudaGetLastError());
   return JMM_OK;
@@ -418,26 +459,12 @@ extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_des
   const uint32_t spr = cfg->steps_per_round ? cfg->steps_per_round : (g <= 32 ? 32 / g : 1);
   const uint32_t cpb = cfg->chains_per_block ? cfg->chains_per_block : 128 / (g * spr ? g * spr : 1);
   if (cfg->lanes_per_chain == 0 && cfg->precision != JMM_PREC_EXACT) {
-    // no shape given, FAST precision: a default per class from the densest
-    // chain's neighbours within the cut-off.  A 12-power core keeps LJ and
-    // soft-sphere neighbours at least ~0.85 sigma apart, a Gaussian core
-    // lets them overlap (about 1.5 rho rc per side at the densest).
+    // no shape given, FAST precision: a default per potential class
     Shape sh[3];
-    for (int pi = 0; pi < 3; ++pi) {
-      double need = 0.0;
-      for (const auto &c : b->chains) {
-        if (c.potential != kPots[pi]) continue;
-        const double side = c.potential == JMM_POT_GAUSS ? 1.5 * c.n / c.l0 * c.cutoff
-                                                         : c.cutoff / (0.85 * c.sigma);
-        need = std::max(need, side);
-      }
-      const uint32_t gg = need <= 4.0 ? 4u : (need <= 8.0 ? 16u : 32u);
-      const uint32_t ss = 32 / gg;
-      sh[pi] = Shape{gg, ss, 128 / (gg * ss)};
-    }
+    default_shapes(b, sh);
     rc = apply_layout(b, sh);
   } else {
-    rc = apply_layout(b, g, spr, cpb);
+    rc = apply_layout(b, g, spr, cpb, cfg->window);
   }
   if (rc == JMM_OK) rc = energies(b, b->stream);
   if (rc == JMM_OK) {
@@ -673,8 +700,9 @@ extern "C" int jmm_batch_device_views(jmm_batch *b, void **positions, void **res
 }
 
 // Launch shapes tried by the autotuner: G x S, and threads per block.
-static const uint32_t kTuneShapes[][2] = {{4, 8}, {2, 16}, {4, 4}, {4, 2}, {8, 4},
-                                          {8, 2}, {16, 2}, {16, 1}, {32, 1}};
+static const uint32_t kTuneShapes[][3] = {{4, 8, 4}, {2, 16, 4}, {4, 4, 4}, {4, 2, 4},
+                                          {8, 4, 4}, {8, 2, 4}, {16, 2, 8}, {16, 1, 8},
+                                          {32, 1, 16}, {4, 8, 8}, {2, 16, 8}, {8, 4, 8}};
 static const uint32_t kTuneThreads[] = {32u, 64u, 128u, 256u};
 
 extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t *lanes_out,
@@ -740,8 +768,9 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
         const uint32_t cpb = threads / (shape[0] * shape[1]);
         if (cpb == 0) continue;
         Shape sh[3];
-        for (int q = 0; q < 3; ++q) sh[q] = per_class ? best[q] : Shape{shape[0], shape[1], cpb};
-        if (per_class) sh[pi] = Shape{shape[0], shape[1], cpb};
+        for (int q = 0; q < 3; ++q)
+          sh[q] = per_class ? best[q] : Shape{shape[0], shape[1], cpb, shape[2]};
+        if (per_class) sh[pi] = Shape{shape[0], shape[1], cpb, shape[2]};
         if (apply_layout(b, sh) != JMM_OK) {
           clear_error();
           continue;
@@ -760,6 +789,18 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
       if (rc) break;
     }
   }
+  if (per_class && rc == JMM_OK && b->classes.size() > 1) {
+    // the classes were timed alone but run side by side: keep the per-class
+    // defaults where they run the whole batch faster than the tuned shapes
+    Shape dflt[3];
+    default_shapes(b, dflt);
+    float t_best = 1e30f, t_dflt = 1e30f;
+    if (apply_layout(b, best) == JMM_OK) rc = trial(-1, &t_best);
+    if (rc == JMM_OK && apply_layout(b, dflt) == JMM_OK) rc = trial(-1, &t_dflt);
+    clear_error();
+    if (rc == JMM_OK && t_dflt < t_best)
+      for (int q = 0; q < 3; ++q) best[q] = dflt[q];
+  }
   cudaMemcpy(b->d_x, x_save, b->total_floats * sizeof(float), cudaMemcpyDeviceToDevice);
   cudaMemcpy(b->d_res, r_save, b->n_chains * sizeof(jmm_chain_result), cudaMemcpyDeviceToDevice);
   cudaEventDestroy(t0);
@@ -772,6 +813,7 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
   b->cfg.lanes_per_chain = b->g;
   b->cfg.steps_per_round = b->spr;
   b->cfg.chains_per_block = b->cpb;
+  b->cfg.window = b->win;
   if (lanes_out) *lanes_out = b->g;
   if (spr_out) *spr_out = b->spr;
   if (cpb_out) *cpb_out = b->cpb;
@@ -782,13 +824,14 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
 extern "C" int jmm_batch_shapes(jmm_batch *b, uint32_t *shapes, uint32_t n) {
   clear_error();
   JMM_CHECK_ARG(b && shapes, "null argument");
-  JMM_CHECK_ARG(n == 9, "shapes holds 3 x (lanes, steps per round, chains per block)");
+  JMM_CHECK_ARG(n == 12, "shapes holds 3 x (lanes, steps per round, chains per block, window)");
   for (int pi = 0; pi < 3; ++pi) {
     bool present = false;
     for (const PotClass &pc : b->classes) present = present || pc.pot == kPots[pi];
-    shapes[3 * pi + 0] = present ? b->shapes[pi].g : 0;
-    shapes[3 * pi + 1] = present ? b->shapes[pi].spr : 0;
-    shapes[3 * pi + 2] = present ? b->shapes[pi].cpb : 0;
+    shapes[4 * pi + 0] = present ? b->shapes[pi].g : 0;
+    shapes[4 * pi + 1] = present ? b->shapes[pi].spr : 0;
+    shapes[4 * pi + 2] = present ? b->shapes[pi].cpb : 0;
+    shapes[4 * pi + 3] = present ? b->shapes[pi].w : 0;
   }
   return JMM_OK;
 }

@@ -6,11 +6,12 @@
 //
 //  * Window.  Particles stay ordered along the line, so the partners within
 //    the cut-off of the moved particle are index neighbours.  G lanes
-//    evaluate one trial move: lane w looks at neighbour side(w)*k(w),
-//    side = -1 for w < W = G/2, k = w % W + 1, at the old and the trial
-//    position; the energy change is the butterfly sum (xor 1, 2, 4, ...) of
-//    the G lanes.  When the W-th neighbour on a side is still within the
-//    cut-off the window is extended in chunks of W (a rare slow path).
+//    evaluate one trial move against W neighbours per side: lane w takes
+//    side -1 for w < G/2, +1 otherwise, and the offsets k = w % (G/2) + 1,
+//    k + G/2, ... up to W, at the old and the trial position; the energy
+//    change is the butterfly sum (xor 1, 2, 4, ...) of the G lanes.  When
+//    the W-th neighbour on a side is still within the cut-off the window is
+//    extended in chunks of W (a rare slow path).
 //  * Speculative rounds.  The S lane segments of a chain evaluate the next S
 //    steps of the chain at once, all from the current positions.  Step s of
 //    the round is kept if no earlier kept step of the round was accepted
@@ -392,9 +393,10 @@ __device__ __forceinline__ void set_ghosts(float *xs, int n, float lf, int cl, i
   }
 }
 
-// Neighbours looked at on each side of a moved particle for G lanes per step:
-// 4 for G <= 8 (two lanes per side each take two offsets when G = 4), G/2
-// beyond.
+// The default number of neighbours looked at on each side of a moved
+// particle for G lanes per step: 4 for G <= 8 (two lanes per side each take
+// two offsets when G = 4), G/2 beyond.  A shape may widen it to any multiple
+// of G/2 up to kGhost.
 __host__ __device__ constexpr int window_of(int g) { return g <= 8 ? 4 : g / 2; }
 
 __host__ __device__ constexpr unsigned leader_bits(int g, int s) {
@@ -404,11 +406,12 @@ __host__ __device__ constexpr unsigned leader_bits(int g, int s) {
 }
 
 // One chain for one launch: n_sweeps sweeps in speculative rounds of S steps.
-template <int G, int S, int POT, bool PER, bool kExact, bool HALO = false>
+template <int G, int S, int POT, bool PER, bool kExact, bool HALO = false, int WIN = window_of(G)>
 __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result *__restrict__ res,
                                           float *__restrict__ xg, float *xs, uint32_t *ring,
                                           const KernelCfg &cfg, int cl, unsigned gmask) {
-  constexpr int W = window_of(G);   // neighbours looked at on each side
+  constexpr int W = WIN;            // neighbours looked at on each side
+  static_assert(W >= G / 2 && W % (G / 2) == 0 && W <= kGhost, "window: multiple of G/2, <= kGhost");
   constexpr int H2 = G / 2;         // lanes per side
   constexpr int KPL = W / H2;       // neighbours per lane
   constexpr int L = G * S;
@@ -760,7 +763,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
 // A single-warp chain is held to 72 registers so that 27 of them stay
 // resident per SM (4096 chains on 152 SMs in one wave); chains that share a
 // warp (G*S < 32) may use 128.
-template <int G, int S, int POT, bool PER, bool kExact>
+template <int G, int S, int POT, bool PER, bool kExact, int WIN>
 __global__ void __maxnreg__(G * S == 32 ? 72 : 128) chains_kernel(const ChainParams *__restrict__ prm,
                                                      jmm_chain_result *__restrict__ res,
                                                      float *__restrict__ xg, KernelCfg cfg) {
@@ -779,7 +782,7 @@ __global__ void __maxnreg__(G * S == 32 ? 72 : 128) chains_kernel(const ChainPar
   __syncwarp(gmask);
   set_ghosts<PER>(xs, (int)P.n, (float)res[P.id].l, cl, L);
   __syncwarp(gmask);
-  run_chain<G, S, POT, PER, kExact>(P, res, xg, xs, ring, cfg, cl, gmask);
+  run_chain<G, S, POT, PER, kExact, false, WIN>(P, res, xg, xs, ring, cfg, cl, gmask);
 }
 
 // Fresh FP64 energies of every chain (32 lanes per chain).

@@ -53,7 +53,7 @@ using namespace jmm::batch;
 
 namespace {
 
-constexpr int kG = 4, kS = 8;  // the batched kernel's default launch shape
+constexpr int kG = 2, kS = 16;  // a domain's step loop: 2 window lanes x 16 steps per round
 constexpr int kWarpsPerBlock = 4;
 // Shared words of one domain warp: its step ring, then its particles with
 // their halo, padded to 16 bytes so that the next warp's ring records stay

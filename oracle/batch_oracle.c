@@ -236,7 +236,7 @@ static void run_chain(jmmo_batch *b, uint32_t c, uint64_t n_sweeps) {
   const chain_prm Pv = make_prm(&b->chains[c], c);
   const chain_prm *P = &Pv;
   const int fp64 = b->fp64;
-  const uint32_t G = b->g, W = G <= 8 ? 4 : G / 2;
+  const uint32_t G = b->g, W = b->cfg.window ? b->cfg.window : (G <= 8 ? 4 : G / 2);
   const int n = (int)P->n;
   float *xs = fp64 ? NULL : b->xf[c];
   double *xd = fp64 ? b->xd[c] : NULL;

@@ -69,19 +69,21 @@ EXACT_CASES = {
 }
 
 
-SHAPES = [(4, 8), (2, 16), (4, 4), (4, 2), (8, 4), (8, 2), (16, 2), (16, 1), (32, 1)]
+# (lanes, steps per round, neighbours per side; 0 = the default of the lanes)
+SHAPES = [(4, 8, 0), (2, 16, 0), (4, 4, 0), (4, 2, 0), (8, 4, 0), (8, 2, 0), (16, 2, 0),
+          (16, 1, 0), (32, 1, 0), (4, 8, 8), (2, 16, 8), (8, 4, 8)]
 
 
-@pytest.mark.parametrize("shape", SHAPES, ids=[f"{g}x{s}" for g, s in SHAPES])
+@pytest.mark.parametrize("shape", SHAPES, ids=[f"{g}x{s}w{w}" for g, s, w in SHAPES])
 @pytest.mark.parametrize("case", sorted(EXACT_CASES))
 def test_batch_exact_matches_oracle(gpu, case, shape):
-    lanes, spr = shape
+    lanes, spr, window = shape
     spec = EXACT_CASES[case]
     rng = np.random.default_rng(abs(hash(case)) % (2 ** 32))
     chains = _mixed_chains(rng, 24, *spec["n"], ensemble=spec["ens"],
                            pots=spec.get("pots", (abi.JMM_POT_LJCUT,)))
     cfg = abi.make_batch_config(seed=11, precision=abi.JMM_PREC_EXACT, lanes_per_chain=lanes,
-                                steps_per_round=spr, init=abi.JMM_INIT_JITTER, jitter=0.05,
+                                steps_per_round=spr, window=window, init=abi.JMM_INIT_JITTER, jitter=0.05,
                                 **spec["cfg"])
     gpu = ChainBatch(cfg, chains)
     ora = oracle_lib.OracleBatch(cfg, chains)
@@ -156,12 +158,13 @@ def test_batch_autotune_keeps_state(gpu):
     gpu = ChainBatch(cfg, chains)
     before = gpu.results()
     g, spr, c = gpu.autotune(trial_sweeps=2)
-    assert (g, spr) in SHAPES and c * g * spr in (32, 64, 128, 256)
+    (w,) = {v[3] for v in gpu.shapes().values()}
+    assert (g, spr) in {(a, b) for a, b, _ in SHAPES} and c * g * spr in (32, 64, 128, 256)
     after = gpu.results()
     assert np.array_equal(before["e"], after["e"]) and np.array_equal(before["steps"], after["steps"])
     # the EXACT result does not depend on the block shape, only on the lanes
     cfg2 = abi.make_batch_config(seed=6, precision=abi.JMM_PREC_EXACT, lanes_per_chain=g,
-                                 steps_per_round=spr)
+                                 steps_per_round=spr, window=w)
     ora = oracle_lib.OracleBatch(cfg2, chains)
     gpu.run(5)
     ora.run(5)
@@ -322,7 +325,7 @@ def test_autotune_per_potential_class(gpu):
     shapes = b.shapes()
     print("per-class shapes", shapes)
     assert set(shapes) == {abi.JMM_POT_LJCUT, abi.JMM_POT_GAUSS}
-    assert shapes[abi.JMM_POT_GAUSS][0] >= 16  # a window of at least 8 per side
+    assert shapes[abi.JMM_POT_GAUSS][3] >= 8  # a window of at least 8 per side
     b.run(10)
     res = b.results()
     assert np.all(res["error"] == 0)
