@@ -720,7 +720,7 @@ def run_ours(args, rank, world, local_rank):
     from jmmonedmc_gb300 import _native, abi, build
     if not os.path.exists(_native.lib_path()):
         build.build_native()
-    from jmmonedmc_gb300.batch import ChainBatch, run_host
+    from jmmonedmc_gb300.batch import ChainBatch, chain_array, chain_view, run_host
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
@@ -801,16 +801,18 @@ def run_ours(args, rank, world, local_rank):
                                     steps_per_round=spr if one_class else 0,
                                     chains_per_block=cpb if one_class else 0,
                                     window=next(iter(b.shapes().values()))[3] if one_class else 0)
+    # the chain descriptions as the C call takes them, built once like the
+    # pinned positions; each step continues from the last one's box lengths
+    desc = chain_array(chains)
     e2e_times, e2e_moves = [], 0
     for _ in range(args.e2e_steps):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        res_h, x_out = run_host(e2e_cfg, chains, S, x_in=x_host)
+        res_h, x_out = run_host(e2e_cfg, desc, S, x_in=x_host)
         e2e_times.append(time.perf_counter() - t0)
         e2e_moves += int(res_h["steps"].sum())
         x_host[:] = x_out
-        for k, c in enumerate(chains):
-            c.l0 = float(res_h["l"][k])
+        chain_view(desc)["l0"] = res_h["l"]
     e2e_value = e2e_moves / sum(e2e_times) * world
     h2d = n_tot * 4 + args.chains * C.sizeof(abi.ChainDesc) + C.sizeof(abi.BatchConfig)
     d2h = n_tot * 4 + args.chains * C.sizeof(abi.ChainResult)

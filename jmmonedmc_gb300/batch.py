@@ -37,10 +37,18 @@ _native.register({
 
 
 def chain_array(chains):
+    """A ctypes array of jmm_chain_desc: chains itself if it already is one."""
+    if isinstance(chains, C.Array) and chains._type_ is abi.ChainDesc:
+        return chains
     arr = (abi.ChainDesc * len(chains))()
     for k, c in enumerate(chains):
         arr[k] = c
     return arr
+
+
+def chain_view(arr):
+    """A numpy structured view of a ctypes jmm_chain_desc array (shares memory)."""
+    return np.frombuffer(arr, dtype=np.dtype(abi.ChainDesc))
 
 
 def results_to_numpy(buf):
@@ -174,9 +182,10 @@ class ChainBatch:
 
 
 def run_host(config, chains, n_sweeps, x_in=None):
-    """Create, run and read back in one call through host buffers."""
+    """Create, run and read back in one call through host buffers.  chains is
+    a sequence of ChainDesc or a ctypes array of them (passed as it is)."""
     arr = chain_array(chains)
-    n_tot = sum(int(c.n) for c in chains)
+    n_tot = int(chain_view(arr)["n"].sum())
     res = (abi.ChainResult * len(chains))()
     x_out = np.empty(n_tot, dtype=np.float32)
     xin_ptr = None

@@ -93,6 +93,7 @@ struct jmm_batch {
   std::vector<uint32_t> order;  // launch order -> user index
   uint64_t total_floats = 0;
   std::vector<ChainParams> params;  // launch order
+  char *d_block = nullptr;  // the one device allocation behind the arrays below
   ChainParams *d_params = nullptr;
   jmm_chain_result *d_res = nullptr;
   float *d_x = nullptr;
@@ -123,14 +124,7 @@ static void drop_graphs(jmm_batch *b) {
 static void batch_free(jmm_batch *b) {
   if (!b) return;
   drop_graphs(b);
-  cudaFree(b->d_params);
-  cudaFree(b->d_res);
-  cudaFree(b->d_x);
-  cudaFree(b->d_e);
-  cudaFree(b->d_desc);
-  cudaFree(b->d_xoff);
-  cudaFree(b->d_gout);
-  cudaFree(b->d_gstats);
+  cudaFree(b->d_block);  // every device array of the batch
   for (int k = 0; k < 3; ++k) {
     if (b->side[k]) cudaStreamDestroy(b->side[k]);
     if (b->join[k]) cudaEventDestroy(b->join[k]);
@@ -388,8 +382,10 @@ static void initial_positions(const jmm_batch_config *cfg, const jmm_chain_desc 
   }
 }
 
-extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
-                                uint32_t n_chains, jmm_batch **out) {
+// Creates a batch; with x_packed (the chains' positions back to back, host
+// memory) the positions start there instead of the configured lattice.
+static int batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                        uint32_t n_chains, jmm_batch **out, const float *x_packed) {
   clear_error();
   JMM_CHECK_ARG(out, "null output");
   *out = nullptr;
@@ -421,14 +417,27 @@ extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_des
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming);
   }
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_params, n_chains * sizeof(ChainParams));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_res, n_chains * sizeof(jmm_chain_result));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_x, b->total_floats * sizeof(float));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_e, n_chains * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_desc, n_chains * sizeof(jmm_chain_desc));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_xoff, n_chains * sizeof(uint64_t));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_gout, 4 * n_chains * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_gstats, n_chains * sizeof(jmm_grad_stats));
+  // one allocation, carved into the batch's arrays at 256-byte boundaries
+  const size_t sizes[8] = {n_chains * sizeof(ChainParams), n_chains * sizeof(jmm_chain_result),
+                           b->total_floats * sizeof(float), n_chains * sizeof(double),
+                           n_chains * sizeof(jmm_chain_desc), n_chains * sizeof(uint64_t),
+                           4 * n_chains * sizeof(double), n_chains * sizeof(jmm_grad_stats)};
+  size_t offs[8], bytes = 0;
+  for (int k = 0; k < 8; ++k) {
+    offs[k] = bytes;
+    bytes += (sizes[k] + 255) & ~(size_t)255;
+  }
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_block, bytes);
+  if (e == cudaSuccess) {
+    b->d_params = reinterpret_cast<ChainParams *>(b->d_block + offs[0]);
+    b->d_res = reinterpret_cast<jmm_chain_result *>(b->d_block + offs[1]);
+    b->d_x = reinterpret_cast<float *>(b->d_block + offs[2]);
+    b->d_e = reinterpret_cast<double *>(b->d_block + offs[3]);
+    b->d_desc = reinterpret_cast<jmm_chain_desc *>(b->d_block + offs[4]);
+    b->d_xoff = reinterpret_cast<uint64_t *>(b->d_block + offs[5]);
+    b->d_gout = reinterpret_cast<double *>(b->d_block + offs[6]);
+    b->d_gstats = reinterpret_cast<jmm_grad_stats *>(b->d_block + offs[7]);
+  }
   if (e == cudaSuccess)
     e = cudaMemcpy(b->d_desc, chains, n_chains * sizeof(jmm_chain_desc), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
@@ -441,8 +450,13 @@ extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_des
   }
   std::vector<float> x(b->total_floats, 0.0f);
   std::vector<jmm_chain_result> res(n_chains);
+  uint64_t src = 0;
   for (uint32_t k = 0; k < n_chains; ++k) {
-    initial_positions(cfg, chains[k], k, x.data() + b->x_off[k]);
+    if (x_packed)
+      memcpy(x.data() + b->x_off[k], x_packed + src, chains[k].n * sizeof(float));
+    else
+      initial_positions(cfg, chains[k], k, x.data() + b->x_off[k]);
+    src += chains[k].n;
     memset(&res[k], 0, sizeof(jmm_chain_result));
     res[k].l = chains[k].l0;
   }
@@ -478,6 +492,11 @@ extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_des
   }
   *out = b;
   return JMM_OK;
+}
+
+extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                                uint32_t n_chains, jmm_batch **out) {
+  return batch_create(cfg, chains, n_chains, out, nullptr);
 }
 
 extern "C" int jmm_batch_destroy(jmm_batch *b) {
@@ -840,26 +859,9 @@ extern "C" int jmm_batch_run_host(const jmm_batch_config *cfg, const jmm_chain_d
                                   uint32_t n_chains, const float *x_in, uint64_t n_sweeps,
                                   jmm_chain_result *results, float *x_out) {
   jmm_batch *b = nullptr;
-  int rc = jmm_batch_create(cfg, chains, n_chains, &b);
+  // the positions in x_in are the batch's starting positions (no lattice)
+  int rc = batch_create(cfg, chains, n_chains, &b, x_in);
   if (rc) return rc;
-  if (x_in) {
-    std::vector<float> staged(b->total_floats, 0.0f);
-    uint64_t src = 0;
-    for (uint32_t k = 0; k < n_chains; ++k) {
-      memcpy(staged.data() + b->x_off[k], x_in + src, chains[k].n * sizeof(float));
-      src += chains[k].n;
-    }
-    cudaError_t e = cudaMemcpy(b->d_x, staged.data(), staged.size() * sizeof(float),
-                               cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-      batch_free(b);
-      return cuda_status(e, "jmm_batch_run_host upload", __FILE__, __LINE__);
-    }
-    rc = energies(b, b->stream);
-    if (rc == JMM_OK)
-      set_energies_kernel<<<(n_chains + 255) / 256, 256, 0, b->stream>>>(b->d_res, b->d_e,
-                                                                          n_chains);
-  }
   if (rc == JMM_OK) rc = jmm_batch_run(b, n_sweeps);
   if (rc == JMM_OK && results) rc = jmm_batch_results(b, results, n_chains);
   if (rc == JMM_OK && x_out) {

@@ -304,20 +304,28 @@ __global__ void sweep_stats_kernel(const LargeChain *__restrict__ chains,
   }
 }
 
-// Fresh energy of each chain from the FP64 positions: FP32 pair terms of the
-// FP64 separations, FP32 per-particle sums, FP64 lane and chain sums.
-__global__ void large_energy_kernel(const LargeChain *__restrict__ chains,
-                                    const int64_t *__restrict__ q, double *__restrict__ e_out,
-                                    uint32_t n_chains) {
-  const uint32_t c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+// FP64 energies of the chains in two passes: warp (chain c, segment g) sums
+// the pair energies of particles [g kEnergySeg, (g + 1) kEnergySeg) with their
+// right-hand partners (FP32 pair terms, FP64 lane and warp sums); then one
+// warp per chain adds its segments in order.  Both orders are fixed, so the
+// sums are the same on every run.
+constexpr uint32_t kEnergySeg = 4096;
+
+__global__ void energy_part_kernel(const LargeChain *__restrict__ chains,
+                                   const int64_t *__restrict__ q, double *__restrict__ part,
+                                   uint32_t n_chains, uint32_t n_seg) {
+  const uint64_t w = (uint64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const uint32_t c = (uint32_t)(w / n_seg), g = (uint32_t)(w % n_seg);
   if (c >= n_chains) return;
   const LargeChain ch = chains[c];
   const ChainParams P = domain_params(ch, 0, ch.n);
   const int64_t *qc = q + ch.x_base;
   const int lane = threadIdx.x & 31;
   const int n = (int)ch.n;
+  const int i0 = (int)(g * kEnergySeg);
+  const int i1 = min(n, i0 + (int)kEnergySeg);
   double u = 0.0;
-  for (int i = lane; i < n; i += 32) {
+  for (int i = i0 + lane; i < i1; i += 32) {
     const int64_t qi = qc[i];
     float e = 0.0f;
     for (int j = i + 1; j < n; ++j) {
@@ -328,6 +336,17 @@ __global__ void large_energy_kernel(const LargeChain *__restrict__ chains,
     }
     u = __dadd_rn(u, (double)e);
   }
+  u = group_sum_d<32>(u, 0xffffffffu);
+  if (lane == 0) part[(uint64_t)c * n_seg + g] = u;
+}
+
+__global__ void energy_sum_kernel(const double *__restrict__ part, double *__restrict__ e_out,
+                                  uint32_t n_chains, uint32_t n_seg) {
+  const uint32_t c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (c >= n_chains) return;
+  const int lane = threadIdx.x & 31;
+  double u = 0.0;
+  for (uint32_t g = lane; g < n_seg; g += 32) u = __dadd_rn(u, part[(uint64_t)c * n_seg + g]);
   u = group_sum_d<32>(u, 0xffffffffu);
   if (lane == 0) e_out[c] = u;
 }
@@ -438,6 +457,7 @@ struct jmm_large {
   double *d_stage = nullptr; // host-format positions (same layout), allocated on first use
   uint32_t *d_bad = nullptr; // flags of the position checks
   double *d_e = nullptr;
+  double *d_part = nullptr;  // per-segment partial energies (energy_sums)
   uint32_t max_n = 0;
   cudaStream_t stream = nullptr;
   uint64_t sweeps_since_resum = 0;
@@ -453,6 +473,7 @@ static void large_free(jmm_large *h) {
   cudaFree(h->d_stage);
   cudaFree(h->d_bad);
   cudaFree(h->d_e);
+  cudaFree(h->d_part);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -475,9 +496,22 @@ static int32_t seq_base_of(const jmm_large *h, int mode) {
 }
 
 // FP64 re-summation on stream s: new base energies, open changes folded.
+// The chains' FP64 energies into d_e, on stream s.
+static int energy_sums(jmm_large *h, cudaStream_t s) {
+  const uint32_t n_seg = (h->max_n + kEnergySeg - 1) / kEnergySeg;
+  const uint64_t warps = (uint64_t)h->n_chains * n_seg;
+  energy_part_kernel<<<(uint32_t)((warps + kStatWarps - 1) / kStatWarps), 32 * kStatWarps, 0, s>>>(
+      h->d_chains, h->d_q, h->d_part, h->n_chains, n_seg);
+  energy_sum_kernel<<<(h->n_chains + kStatWarps - 1) / kStatWarps, 32 * kStatWarps, 0, s>>>(
+      h->d_part, h->d_e, h->n_chains, n_seg);
+  JMM_CUDA(cudaGetLastError());
+  return JMM_OK;
+}
+
 static int resum(jmm_large *h, cudaStream_t s, bool note) {
   const uint32_t blocks = (h->n_chains + kStatWarps - 1) / kStatWarps;
-  large_energy_kernel<<<blocks, 32 * kStatWarps, 0, s>>>(h->d_chains, h->d_q, h->d_e, h->n_chains);
+  const int rc = energy_sums(h, s);
+  if (rc) return rc;
   rebase_kernel<<<blocks, 32 * kStatWarps, 0, s>>>(h->d_chains, h->d_states, h->d_rec, h->d_e,
                                                    h->n_chains, seq_base_of(h, h->mode), note);
   JMM_CUDA(cudaGetLastError());
@@ -580,8 +614,11 @@ static int enqueue(jmm_large *h, uint64_t n_sweeps, int mode, cudaStream_t s) {
   return JMM_OK;
 }
 
-extern "C" int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
-                                uint32_t n_chains, uint32_t domain_size, jmm_large **out) {
+// Creates the chains; with x_in (host FP64 positions, chains back to back)
+// they start there instead of on the configured lattice.
+static int large_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                        uint32_t n_chains, uint32_t domain_size, jmm_large **out,
+                        const double *x_in) {
   clear_error();
   JMM_CHECK_ARG(cfg && chains && out && n_chains > 0, "null argument or no chains");
   JMM_CHECK_ARG(n_chains <= 65535, "at most 65535 chains");
@@ -663,6 +700,9 @@ extern "C" int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_des
   if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_rec, n_rec * sizeof(jmm_chain_result));
   if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_q, off * sizeof(int64_t));
   if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_e, n_chains * sizeof(double));
+  if (e == cudaSuccess)
+    e = cudaMalloc((void **)&h->d_part, (size_t)n_chains * ((h->max_n + kEnergySeg - 1) / kEnergySeg) *
+                                            sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_bad, sizeof(uint32_t));
   if (e != cudaSuccess) {
     const int rc = cuda_status(e, "jmm_large_create allocation", __FILE__, __LINE__);
@@ -702,7 +742,9 @@ extern "C" int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_des
       h->d_chains, h->d_q, 0, cfg->seed, cfg->init, cfg->jitter);
   e = cudaMemsetAsync(h->d_bad, 0, sizeof(uint32_t), h->stream);
   if (e != cudaSuccess) rc = cuda_status(e, "jmm_large_create lattice", __FILE__, __LINE__);
-  if (rc == JMM_OK) rc = check_positions(h, 0, n_chains, "jmm_large_create (initial jitter)");
+  if (rc == JMM_OK)
+    rc = x_in ? upload_positions(h, x_in, 0, n_chains, "jmm_large_run_host")
+              : check_positions(h, 0, n_chains, "jmm_large_create (initial jitter)");
   if (rc == JMM_OK) rc = resum(h, h->stream, false);  // initial energies
   if (rc == JMM_OK) {
     e = cudaStreamSynchronize(h->stream);
@@ -714,6 +756,11 @@ extern "C" int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_des
   }
   *out = h;
   return JMM_OK;
+}
+
+extern "C" int jmm_large_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                                uint32_t n_chains, uint32_t domain_size, jmm_large **out) {
+  return large_create(cfg, chains, n_chains, domain_size, out, nullptr);
 }
 
 extern "C" int jmm_large_destroy(jmm_large *h) {
@@ -797,10 +844,8 @@ extern "C" int jmm_large_energies(jmm_large *h, double *e, uint32_t n_chains) {
   JMM_CHECK_ARG(h && e, "null argument");
   JMM_CHECK_ARG(n_chains == h->n_chains, "n_chains does not match");
   JMM_CUDA(cudaDeviceSynchronize());
-  const uint32_t blocks = (h->n_chains + kStatWarps - 1) / kStatWarps;
-  large_energy_kernel<<<blocks, 32 * kStatWarps, 0, h->stream>>>(h->d_chains, h->d_q, h->d_e,
-                                                                 h->n_chains);
-  JMM_CUDA(cudaGetLastError());
+  const int rc = energy_sums(h, h->stream);
+  if (rc) return rc;
   JMM_CUDA(cudaStreamSynchronize(h->stream));
   JMM_CUDA(cudaMemcpy(e, h->d_e, n_chains * sizeof(double), cudaMemcpyDeviceToHost));
   return JMM_OK;
@@ -841,12 +886,9 @@ extern "C" int jmm_large_run_host(const jmm_batch_config *cfg, const jmm_chain_d
                                   const double *x_in, uint64_t n_sweeps, jmm_large_result *results,
                                   double *x_out) {
   jmm_large *h = nullptr;
-  int rc = jmm_large_create(cfg, chains, n_chains, domain_size, &h);
+  // x_in gives the starting positions (no lattice, one FP64 energy sum)
+  int rc = large_create(cfg, chains, n_chains, domain_size, &h, x_in);
   if (rc) return rc;
-  if (x_in) {
-    rc = upload_positions(h, x_in, 0, n_chains, "jmm_large_run_host");
-    if (rc == JMM_OK) rc = resum(h, h->stream, false);
-  }
   if (rc == JMM_OK) rc = jmm_large_run(h, n_sweeps, mode);
   if (rc == JMM_OK && results) rc = jmm_large_results(h, results, n_chains);
   if (rc == JMM_OK && x_out) rc = download_positions(h, x_out, 0, n_chains);
