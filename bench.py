@@ -586,7 +586,7 @@ def run_grad(args, rank, world, local_rank):
     from jmmonedmc_gb300 import _native, build
     if not os.path.exists(_native.lib_path()):
         build.build_native()
-    from jmmonedmc_gb300.batch import ChainBatch
+    from jmmonedmc_gb300.batch import ChainBatch, chain_array, chain_view
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
@@ -643,26 +643,26 @@ def run_grad(args, rank, world, local_rank):
 
     # e2e: host buffers through the public API: a batch built from host
     # positions, the sampled run, the gradient statistics and results read back
-    xs = [b.positions(k) for k in range(len(chains))]
-    lbox = b.results()["l"].copy()  # the box lengths of these positions
+    n_tot = sum(int(c.n) for c in chains)
+    x_host = torch.empty(n_tot, dtype=torch.float32, pin_memory=True).numpy()
+    x_host[:] = np.concatenate([b.positions(k) for k in range(len(chains))])
+    desc = chain_array(chains)
+    chain_view(desc)["l0"] = b.results()["l"]  # the box lengths of these positions
     e2e_times, e2e_moves = [], 0
     for _ in range(args.e2e_steps):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        b2 = ChainBatch(cfg, chains)
-        for k in range(len(chains)):
-            b2.set_positions(k, xs[k], float(lbox[k]))
+        b2 = ChainBatch(cfg, desc, x=x_host)
         b2.run_sampled(S, every)
         r2, g2 = b2.results(), b2.grad_stats()
         e2e_times.append(time.perf_counter() - t0)
         e2e_moves += int(r2["steps"].sum())
         b2.close()
-    n_tot = sum(int(c.n) for c in chains)
     e2e = {"value": e2e_moves / sum(e2e_times) * world, "unit": UNIT,
            "h2d_bytes_per_step": n_tot * 4 + len(chains) * 8,
            "d2h_bytes_per_step": len(chains) * (C.sizeof(abi_result()) + C.sizeof(abi_gstats())),
-           "how": "ChainBatch from host positions (jmm_batch_create + set_positions), "
-                  "run_sampled, results and grad_stats read back, all inside the timed region"}
+           "how": "ChainBatch from pinned host positions (jmm_batch_create_at), run_sampled, "
+                  "results and grad_stats read back, all inside the timed region"}
     launch_ms = total_ms / args.steps
     achieved = pairs / args.steps * FLOP_PER_PAIR / (launch_ms * 1e-3) / 1e12
     line = {

@@ -293,6 +293,12 @@ typedef struct jmm_batch jmm_batch;
 
 int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
                      uint32_t n_chains, jmm_batch **out);
+/* As jmm_batch_create, starting from the caller's positions instead of the
+ * configured lattice: x holds the chains' positions back to back (FP32,
+ * sum of N floats, each chain strictly increasing, within +-l0/2 between
+ * walls), the box lengths are the chains' l0. */
+int jmm_batch_create_at(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                        uint32_t n_chains, const float *x, jmm_batch **out);
 /* n_sweeps sweeps of every chain (N steps, N+1 with volume moves), then wait. */
 int jmm_batch_run(jmm_batch *b, uint64_t n_sweeps);
 /* Same, enqueued on a CUDA stream (cudaStream_t passed as void*), no wait. */

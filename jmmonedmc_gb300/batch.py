@@ -15,6 +15,8 @@ from . import _native, abi
 P = C.POINTER
 _native.register({
     "jmm_batch_create": [P(abi.BatchConfig), P(abi.ChainDesc), C.c_uint32, P(C.c_void_p)],
+    "jmm_batch_create_at": [P(abi.BatchConfig), P(abi.ChainDesc), C.c_uint32, P(C.c_float),
+                            P(C.c_void_p)],
     "jmm_batch_run": [C.c_void_p, C.c_uint64],
     "jmm_batch_run_async": [C.c_void_p, C.c_uint64, C.c_void_p],
     "jmm_batch_results": [C.c_void_p, P(abi.ChainResult), C.c_uint32],
@@ -56,13 +58,23 @@ def results_to_numpy(buf):
 
 
 class ChainBatch:
-    def __init__(self, config: abi.BatchConfig, chains):
+    def __init__(self, config: abi.BatchConfig, chains, x=None):
+        """chains: a sequence of ChainDesc or a ctypes array of them.  x: the
+        chains' starting positions back to back (box lengths l0); None starts
+        them on the configured lattice."""
         self.config = config
-        self.chains = list(chains)
-        self._arr = chain_array(self.chains)
+        self._arr = chain_array(chains)
+        self.chains = self._arr
         self._h = C.c_void_p()
-        _native.call("jmm_batch_create", C.byref(config), self._arr, len(self.chains),
-                     C.byref(self._h))
+        if x is None:
+            _native.call("jmm_batch_create", C.byref(config), self._arr, len(self._arr),
+                         C.byref(self._h))
+        else:
+            x = np.ascontiguousarray(x, dtype=np.float32)
+            if x.size != int(chain_view(self._arr)["n"].sum()):
+                raise ValueError("x must hold every chain's positions back to back")
+            _native.call("jmm_batch_create_at", C.byref(config), self._arr, len(self._arr),
+                         x.ctypes.data_as(P(C.c_float)), C.byref(self._h))
 
     @property
     def n_chains(self):

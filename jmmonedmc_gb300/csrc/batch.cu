@@ -382,8 +382,39 @@ static void initial_positions(const jmm_batch_config *cfg, const jmm_chain_desc 
   }
 }
 
+// Positions a caller gives for one chain (index `chain`): finite, strictly
+// increasing, within the walls at +-L/2 (the kernel's own wall test, |x| <=
+// L/2 rounded to FP32, with room for the rounding of positions that a volume
+// move scaled in FP32), or spanning less than L on a ring.
+static int check_host_positions(const float *x, uint32_t n, double l, bool periodic,
+                                uint32_t chain) {
+  if (!(l > 0)) return fail(JMM_ERR_INVALID, "chain %u: box length must be positive", chain);
+  const float half = (float)(0.5 * l) * (1.0f + 1e-6f);
+  // branch-free passes first (comparisons with NaN are false, so NaN counts
+  // as bad); the element loop below only names the first bad position
+  uint32_t bad = n > 0 && !(x[0] == x[0]);
+  for (uint32_t i = 1; i < n; ++i) bad |= (uint32_t)!(x[i] > x[i - 1]);
+  if (!periodic)
+    for (uint32_t i = 0; i < n; ++i) bad |= (uint32_t)!(fabsf(x[i]) <= half);
+  else
+    bad |= (uint32_t)(n > 0 && !(x[n - 1] < x[0] + l));
+  if (!bad) return JMM_OK;
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!(x[i] == x[i]) || (i > 0 && !(x[i] > x[i - 1])))
+      return fail(JMM_ERR_INVALID, "chain %u: positions must be finite and strictly increasing",
+                  chain);
+    if (!periodic && !(fabsf(x[i]) <= half))
+      return fail(JMM_ERR_INVALID, "chain %u: position %u lies beyond the walls at +-L/2", chain,
+                  i);
+  }
+  if (periodic && n > 0 && !(x[n - 1] < x[0] + l))
+    return fail(JMM_ERR_INVALID, "chain %u: periodic positions must span less than L", chain);
+  return JMM_OK;
+}
+
 // Creates a batch; with x_packed (the chains' positions back to back, host
-// memory) the positions start there instead of the configured lattice.
+// memory, box lengths l0) the positions start there instead of the
+// configured lattice.
 static int batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
                         uint32_t n_chains, jmm_batch **out, const float *x_packed) {
   clear_error();
@@ -391,6 +422,15 @@ static int batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chain
   *out = nullptr;
   int rc = validate(cfg, chains, n_chains);
   if (rc) return rc;
+  if (x_packed) {
+    uint64_t src = 0;
+    for (uint32_t k = 0; k < n_chains; ++k) {
+      rc = check_host_positions(x_packed + src, chains[k].n, chains[k].l0,
+                                cfg->boundary == JMM_BOUNDARY_PERIODIC, k);
+      if (rc) return rc;
+      src += chains[k].n;
+    }
+  }
   if (!jmm_device_available()) return fail(JMM_ERR_CUDA, "jmm_batch_create: no CUDA device");
   jmm_batch *b = new (std::nothrow) jmm_batch();
   if (!b) return fail(JMM_ERR_NOMEM, "jmm_batch_create: host allocation failed");
@@ -497,6 +537,13 @@ static int batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chain
 extern "C" int jmm_batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
                                 uint32_t n_chains, jmm_batch **out) {
   return batch_create(cfg, chains, n_chains, out, nullptr);
+}
+
+extern "C" int jmm_batch_create_at(const jmm_batch_config *cfg, const jmm_chain_desc *chains,
+                                   uint32_t n_chains, const float *x, jmm_batch **out) {
+  clear_error();
+  JMM_CHECK_ARG(x, "null positions");
+  return batch_create(cfg, chains, n_chains, out, x);
 }
 
 extern "C" int jmm_batch_destroy(jmm_batch *b) {
@@ -666,25 +713,15 @@ extern "C" int jmm_batch_set_positions(jmm_batch *b, uint32_t chain, const float
   JMM_CHECK_ARG(b && x, "null argument");
   JMM_CHECK_ARG(chain < b->n_chains, "chain index out of range");
   JMM_CHECK_ARG(n == b->chains[chain].n, "N does not match the chain");
-  JMM_CHECK_ARG(l > 0, "box length must be positive");
-  const bool periodic = b->cfg.boundary == JMM_BOUNDARY_PERIODIC;
-  for (uint32_t i = 0; i < n; ++i) {
-    if (!(x[i] == x[i]) || (i > 0 && !(x[i] > x[i - 1])))
-      return fail(JMM_ERR_INVALID, "positions must be finite and strictly increasing");
-    // the kernel's own wall test, |x| <= L/2 rounded to FP32, with room for
-    // the rounding of positions that a volume move scaled in FP32
-    if (!periodic && !(fabsf(x[i]) <= (float)(0.5 * l) * (1.0f + 1e-6f)))
-      return fail(JMM_ERR_INVALID, "position %u lies beyond the walls at +-L/2", i);
-  }
-  if (periodic && !(x[n - 1] < x[0] + l))
-    return fail(JMM_ERR_INVALID, "periodic positions must span less than L");
+  int rc = check_host_positions(x, n, l, b->cfg.boundary == JMM_BOUNDARY_PERIODIC, chain);
+  if (rc) return rc;
   JMM_CUDA(cudaStreamSynchronize(b->stream));
   JMM_CUDA(cudaMemcpy(b->d_x + b->x_off[chain], x, n * sizeof(float), cudaMemcpyHostToDevice));
   jmm_chain_result r;
   JMM_CUDA(cudaMemcpy(&r, b->d_res + chain, sizeof(r), cudaMemcpyDeviceToHost));
   r.l = l;
   JMM_CUDA(cudaMemcpy(b->d_res + chain, &r, sizeof(r), cudaMemcpyHostToDevice));
-  int rc = energies(b, b->stream);
+  rc = energies(b, b->stream);
   if (rc) return rc;
   double e;
   JMM_CUDA(cudaMemcpyAsync(&e, b->d_e + chain, sizeof(double), cudaMemcpyDeviceToHost, b->stream));

@@ -183,6 +183,41 @@ def test_batch_rejects_bad_input(gpu):
         b.set_positions(0, np.linspace(1, -1, 16), 30.0)  # not increasing
 
 
+def test_batch_create_at_matches_set_positions(gpu):
+    """A batch created from host positions (jmm_batch_create_at) runs the
+    same EXACT chains as one created on the lattice whose positions are then
+    set chain by chain; bad positions are refused at creation."""
+    from jmmonedmc_gb300._native import JmmError
+    from jmmonedmc_gb300.batch import chain_array, chain_view
+    rng = np.random.default_rng(21)
+    chains = _mixed_chains(rng, 12, 32, 200, ensemble=abi.JMM_NPT)
+    cfg = abi.make_batch_config(seed=5, precision=abi.JMM_PREC_EXACT, init=abi.JMM_INIT_JITTER,
+                                jitter=0.05)
+    src = ChainBatch(cfg, chains)
+    src.run(3)
+    xs = [src.positions(k) for k in range(len(chains))]
+    lbox = src.results()["l"].copy()
+    desc = chain_array(chains)
+    chain_view(desc)["l0"] = lbox
+    a = ChainBatch(cfg, desc, x=np.concatenate(xs))
+    b = ChainBatch(cfg, chains)
+    for k in range(len(chains)):
+        b.set_positions(k, xs[k], float(lbox[k]))
+    ra, rb = a.results(), b.results()
+    assert np.array_equal(ra["e"].view(np.uint64), rb["e"].view(np.uint64))
+    a.run(5)
+    b.run(5)
+    _assert_same(a, b, chains)
+    bad = np.concatenate(xs)
+    bad[3], bad[4] = bad[4], bad[3]  # chain 0 no longer increasing
+    with pytest.raises(JmmError):
+        ChainBatch(cfg, desc, x=bad)
+    far = np.concatenate(xs)
+    far[0] = -float(lbox[0])  # beyond the left wall
+    with pytest.raises(JmmError):
+        ChainBatch(cfg, desc, x=far)
+
+
 def test_uneven_batch_at_full_size(gpu):
     """The uneven workload (1024 chains, N 32..2048, three potentials,
     rho 0.3-0.9, T 0.5-2, NVT) runs error-free in one graph of parallel
