@@ -348,6 +348,14 @@ static int validate(const jmm_batch_config *cfg, const jmm_chain_desc *chains, u
                 "unknown volume schedule");
   JMM_CHECK_ARG(cfg->precision == JMM_PREC_FAST || cfg->precision == JMM_PREC_EXACT,
                 "unknown precision");
+  if (cfg->lanes_per_chain) {
+    const uint32_t g = cfg->lanes_per_chain;
+    const uint32_t spr = cfg->steps_per_round ? cfg->steps_per_round : (g <= 32 ? 32 / g : 1);
+    if (!pick_kernel(g, spr, cfg->window, false, JMM_POT_LJCUT, false))
+      return fail(JMM_ERR_INVALID, "unsupported launch shape: lanes_per_chain x steps_per_round "
+                  "must be 2x16, 4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or 32x1, with a window "
+                  "of 0 (the default) or 8 for 2x16, 4x8 and 8x4");
+  }
   for (uint32_t k = 0; k < n_chains; ++k) {
     const jmm_chain_desc &c = chains[k];
     if (c.n < 2 || c.n > 16384)
