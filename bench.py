@@ -310,6 +310,30 @@ def profile_traffic(args, pair_evals_per_launch, sweeps):
     return args.chains * (per * sweeps + fixed)
 
 
+def issue_roofline(profile, moves_per_s, clocks, dev):
+    """Warp instructions issued per second by the dominant kernel against the
+    issue limit (4 schedulers per SM, one warp instruction each per clock):
+    the kernel's instructions per attempted move, from its committed ncu
+    summary, times the timed moves/s of one GPU."""
+    import torch
+    path = os.path.join(REPO, "profiles", profile)
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        m = re.search(r"warp_instructions_per_move:\s*([0-9.eE+-]+)", f.read())
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
+    if not m or not mhz:
+        return None
+    per_move = float(m.group(1))
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    peak = sms * 4 * float(mhz) * 1e6
+    achieved = per_move * moves_per_s
+    return {"achieved": achieved, "peak": peak, "unit": "warp instructions/s",
+            "frac": achieved / peak, "instructions_per_move": per_move,
+            "source": f"instructions per move from profiles/{profile} (ncu); peak = 4 issue "
+                      f"slots per SM per clock x {sms} SMs x the sampled SM clock"}
+
+
 # ---- the large-chain workload -------------------------------------------------------
 
 LARGE_METRIC = "attempted MC moves/s (large chains, alternating-domain sweep, FP32 pairs)"
@@ -503,6 +527,8 @@ def run_large(args, rank, world, local_rank):
             "pair_evals_per_launch": pairs_per_launch,
             "flop_per_pair": FLOP_PER_PAIR,
             "mufu_rcp_frac": pairs_per_launch / (launch_ms * 1e-3) / (rcp_peak.value * 1e12),
+            "issue": issue_roofline("domain_kernel_large_chains.md",
+                                    moves_all / world / (total_ms * 1e-3), clocks, dev),
             "kernel": "domain_kernel (one colour phase of one sweep)",
         },
         "sequential": {"value": seq_moves / (seq_ms * 1e-3), "unit": UNIT, "ms_per_sweep": seq_ms,
@@ -854,6 +880,9 @@ def run_ours(args, rank, world, local_rank):
             "mufu_rcp_frac": (pairs / args.steps) / (launch_ms * 1e-3) / (rcp_peak.value * 1e12),
             "pair_evals_per_s": (pairs / args.steps) / (launch_ms * 1e-3),
             "smem": smem_roofline(pairs / args.steps, launch_ms),
+            "issue": issue_roofline("chains_kernel_batched_npt.md",
+                                    moves_all / world / (total_ms * 1e-3), clocks, dev)
+            if args.workload == "npt" else None,
             "kernel": "jmm::batch::chains_kernel",
         },
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
