@@ -764,7 +764,9 @@ def run_ours(args, rank, world, local_rank):
     if args.no_autotune:
         lanes, spr, cpb = 0, 0, 0
     else:
-        lanes, spr, cpb = b.autotune(trial_sweeps=5)
+        # trials of about a millisecond each, so that block sizes whose
+        # difference is a few per cent are told apart
+        lanes, spr, cpb = b.autotune(trial_sweeps=20 if args.workload == "npt" else 5)
     class_names = {abi.JMM_POT_LJCUT: "ljcut", abi.JMM_POT_SOFTSPHERE: "softsphere",
                    abi.JMM_POT_GAUSS: "gauss"}
     class_shapes = {class_names[p]: "%dx%d, %d per block, window %d" % v
