@@ -109,6 +109,9 @@ struct jmm_batch {
   // energy gradients and their sampled statistics
   jmm_chain_desc *d_desc = nullptr;     // user order
   uint64_t *d_xoff = nullptr;           // user order
+  uint64_t *d_poff = nullptr;           // user order: offsets in the packed layout
+  float *d_pack = nullptr;              // positions back to back (host-buffer copies)
+  uint64_t n_packed = 0;
   double *d_gout = nullptr;             // 4 per chain
   jmm_grad_stats *d_gstats = nullptr;   // user order
   std::map<std::pair<uint64_t, uint32_t>, cudaGraphExec_t> sampled;  // (sweeps, every)
@@ -390,6 +393,39 @@ static void initial_positions(const jmm_batch_config *cfg, const jmm_chain_desc 
   }
 }
 
+// Positions between the packed layout (chains back to back) and the padded
+// one; one warp per chain.
+__global__ void unpack_positions_kernel(const float *__restrict__ pack, float *__restrict__ x,
+                                        const uint64_t *__restrict__ poff,
+                                        const uint64_t *__restrict__ xoff,
+                                        const jmm_chain_desc *__restrict__ desc, uint32_t n_chains) {
+  const uint32_t c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (c >= n_chains) return;
+  const uint32_t n = desc[c].n;
+  for (uint32_t i = threadIdx.x & 31; i < n; i += 32) x[xoff[c] + i] = pack[poff[c] + i];
+}
+
+__global__ void pack_positions_kernel(const float *__restrict__ x, float *__restrict__ pack,
+                                      const uint64_t *__restrict__ poff,
+                                      const uint64_t *__restrict__ xoff,
+                                      const jmm_chain_desc *__restrict__ desc, uint32_t n_chains) {
+  const uint32_t c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (c >= n_chains) return;
+  const uint32_t n = desc[c].n;
+  for (uint32_t i = threadIdx.x & 31; i < n; i += 32) pack[poff[c] + i] = x[xoff[c] + i];
+}
+
+// A fresh result record per chain: zero sums, the box length l0.
+__global__ void init_results_kernel(jmm_chain_result *__restrict__ res,
+                                    const jmm_chain_desc *__restrict__ desc, uint32_t n_chains) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_chains) return;
+  jmm_chain_result r;
+  memset(&r, 0, sizeof(r));
+  r.l = desc[c].l0;
+  res[c] = r;
+}
+
 // Positions a caller gives for one chain (index `chain`): finite, strictly
 // increasing, within the walls at +-L/2 (the kernel's own wall test, |x| <=
 // L/2 rounded to FP32, with room for the rounding of positions that a volume
@@ -466,12 +502,19 @@ static int batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chain
   }
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   // one allocation, carved into the batch's arrays at 256-byte boundaries
-  const size_t sizes[8] = {n_chains * sizeof(ChainParams), n_chains * sizeof(jmm_chain_result),
-                           b->total_floats * sizeof(float), n_chains * sizeof(double),
-                           n_chains * sizeof(jmm_chain_desc), n_chains * sizeof(uint64_t),
-                           4 * n_chains * sizeof(double), n_chains * sizeof(jmm_grad_stats)};
-  size_t offs[8], bytes = 0;
-  for (int k = 0; k < 8; ++k) {
+  std::vector<uint64_t> p_off(n_chains);
+  b->n_packed = 0;
+  for (uint32_t k = 0; k < n_chains; ++k) {
+    p_off[k] = b->n_packed;
+    b->n_packed += chains[k].n;
+  }
+  const size_t sizes[10] = {n_chains * sizeof(ChainParams), n_chains * sizeof(jmm_chain_result),
+                            b->total_floats * sizeof(float), n_chains * sizeof(double),
+                            n_chains * sizeof(jmm_chain_desc), n_chains * sizeof(uint64_t),
+                            4 * n_chains * sizeof(double), n_chains * sizeof(jmm_grad_stats),
+                            n_chains * sizeof(uint64_t), b->n_packed * sizeof(float)};
+  size_t offs[10], bytes = 0;
+  for (int k = 0; k < 10; ++k) {
     offs[k] = bytes;
     bytes += (sizes[k] + 255) & ~(size_t)255;
   }
@@ -485,33 +528,42 @@ static int batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chain
     b->d_xoff = reinterpret_cast<uint64_t *>(b->d_block + offs[5]);
     b->d_gout = reinterpret_cast<double *>(b->d_block + offs[6]);
     b->d_gstats = reinterpret_cast<jmm_grad_stats *>(b->d_block + offs[7]);
+    b->d_poff = reinterpret_cast<uint64_t *>(b->d_block + offs[8]);
+    b->d_pack = reinterpret_cast<float *>(b->d_block + offs[9]);
   }
   if (e == cudaSuccess)
     e = cudaMemcpy(b->d_desc, chains, n_chains * sizeof(jmm_chain_desc), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(b->d_xoff, b->x_off.data(), n_chains * sizeof(uint64_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_poff, p_off.data(), n_chains * sizeof(uint64_t), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(b->d_gstats, 0, n_chains * sizeof(jmm_grad_stats));
   if (e != cudaSuccess) {
     rc = cuda_status(e, "jmm_batch_create allocation", __FILE__, __LINE__);
     batch_free(b);
     return rc;
   }
-  std::vector<float> x(b->total_floats, 0.0f);
-  std::vector<jmm_chain_result> res(n_chains);
-  uint64_t src = 0;
-  for (uint32_t k = 0; k < n_chains; ++k) {
-    if (x_packed)
-      memcpy(x.data() + b->x_off[k], x_packed + src, chains[k].n * sizeof(float));
-    else
+  if (x_packed) {
+    // the caller's positions in one copy, spread into the padded layout on
+    // the device
+    e = cudaMemcpyAsync(b->d_pack, x_packed, b->n_packed * sizeof(float), cudaMemcpyHostToDevice,
+                        b->stream);
+    if (e == cudaSuccess) {
+      unpack_positions_kernel<<<(n_chains + 7) / 8, 256, 0, b->stream>>>(
+          b->d_pack, b->d_x, b->d_poff, b->d_xoff, b->d_desc, n_chains);
+      e = cudaGetLastError();
+    }
+  } else {
+    std::vector<float> x(b->total_floats, 0.0f);
+    for (uint32_t k = 0; k < n_chains; ++k)
       initial_positions(cfg, chains[k], k, x.data() + b->x_off[k]);
-    src += chains[k].n;
-    memset(&res[k], 0, sizeof(jmm_chain_result));
-    res[k].l = chains[k].l0;
+    e = cudaMemcpy(b->d_x, x.data(), x.size() * sizeof(float), cudaMemcpyHostToDevice);
   }
-  e = cudaMemcpy(b->d_x, x.data(), x.size() * sizeof(float), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(b->d_res, res.data(), res.size() * sizeof(jmm_chain_result),
-                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    init_results_kernel<<<(n_chains + 255) / 256, 256, 0, b->stream>>>(b->d_res, b->d_desc,
+                                                                       n_chains);
+    e = cudaGetLastError();
+  }
   if (e != cudaSuccess) {
     rc = cuda_status(e, "jmm_batch_create upload", __FILE__, __LINE__);
     batch_free(b);
@@ -907,22 +959,43 @@ extern "C" int jmm_batch_run_host(const jmm_batch_config *cfg, const jmm_chain_d
   // the positions in x_in are the batch's starting positions (no lattice)
   int rc = batch_create(cfg, chains, n_chains, &b, x_in);
   if (rc) return rc;
-  if (rc == JMM_OK) rc = jmm_batch_run(b, n_sweeps);
-  if (rc == JMM_OK && results) rc = jmm_batch_results(b, results, n_chains);
-  if (rc == JMM_OK && x_out) {
-    std::vector<float> staged(b->total_floats);
-    cudaError_t e = cudaMemcpy(staged.data(), b->d_x, staged.size() * sizeof(float),
-                               cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) {
-      rc = cuda_status(e, "jmm_batch_run_host download", __FILE__, __LINE__);
-    } else {
-      uint64_t dst = 0;
-      for (uint32_t k = 0; k < n_chains; ++k) {
-        memcpy(x_out + dst, staged.data() + b->x_off[k], chains[k].n * sizeof(float));
-        dst += chains[k].n;
+  // one run: launched directly, without building a graph to replay
+  if (n_sweeps > 0) {
+    for (const auto &c : b->chains)
+      if (n_sweeps * (uint64_t)(c.n + 1) >= (1ull << 31)) {
+        batch_free(b);
+        return fail(JMM_ERR_INVALID, "one run may hold at most 2^31 steps per chain: split it");
       }
-    }
+    rc = launch(b, n_sweeps, b->stream);
   }
+  std::vector<jmm_chain_result> own;
+  jmm_chain_result *res = results;
+  if (!res) {
+    own.resize(n_chains);
+    res = own.data();
+  }
+  cudaError_t e = cudaSuccess;
+  if (rc == JMM_OK) {
+    e = cudaMemcpyAsync(res, b->d_res, n_chains * sizeof(jmm_chain_result),
+                        cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess && x_out) {
+      pack_positions_kernel<<<(n_chains + 7) / 8, 256, 0, b->stream>>>(
+          b->d_x, b->d_pack, b->d_poff, b->d_xoff, b->d_desc, n_chains);
+      e = cudaGetLastError();
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(x_out, b->d_pack, b->n_packed * sizeof(float),
+                            cudaMemcpyDeviceToHost, b->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) rc = cuda_status(e, "jmm_batch_run_host", __FILE__, __LINE__);
+  }
+  if (rc == JMM_OK)
+    for (uint32_t k = 0; k < n_chains; ++k)
+      if (res[k].error) {
+        rc = fail((int)res[k].error, "chain %u reported error %u (energy %g)", k, res[k].error,
+                  res[k].e);
+        break;
+      }
   batch_free(b);
   return rc;
 }
