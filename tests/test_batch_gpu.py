@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 from jmmonedmc_gb300 import abi
-from jmmonedmc_gb300.batch import ChainBatch, rng_words, run_host
+from jmmonedmc_gb300.batch import ChainBatch, averages, rng_words, run_host
 from tests import oracle_lib
 
 pytestmark = pytest.mark.gpu
@@ -239,6 +239,45 @@ def test_uneven_batch_at_full_size(gpu):
         e64 = oracle_lib.energy64(chains[k], x, res["l"][k])
         assert abs(fresh[k] - e64) <= 1e-6 * max(1.0, abs(e64)), (k, fresh[k], e64)
         assert np.all(np.diff(x) > 0)
+
+
+def test_npt_batch_at_full_size(gpu):
+    """The benchmark workload at its configured length (4096 chains x N =
+    256, LJ rc 3, walls, T log-spaced 0.5-2, P U(0.5, 2), ln L moves once
+    per sweep, 1e4 sweeps): every chain made every step without error, its
+    particles stay ordered inside the walls, the running energies agree with
+    fresh sums and a sample with the FP64 oracle of the GPU's own positions,
+    the same seed and shape replay bit for bit, and each chain's mean density
+    lies between that of hard rods of diameter sigma at its (P, T),
+    P / (T + P sigma), and close packing."""
+    import argparse
+    import bench
+    args = argparse.Namespace(chains=4096, seed=1, workload="npt", n=256)
+    cfg, chains = bench.workload(args)
+    cfg.lanes_per_chain, cfg.steps_per_round, cfg.chains_per_block = 4, 8, 2
+    runs = []
+    for _ in range(2):
+        b = ChainBatch(cfg, chains)
+        b.run(10000)
+        runs.append((b, b.results()))
+    (b, res), (_, res2) = runs
+    assert np.all(res["error"] == 0)
+    assert np.all(res["steps"] == 10000 * 257)
+    for f in ("e", "l", "sum_e", "sum_e2", "sum_l", "disp_acc", "vol_acc"):
+        assert np.array_equal(res[f], res2[f]), f
+    fresh = b.energies()
+    scale = np.maximum(1.0, np.abs(fresh))
+    assert np.all(np.abs(res["e"] - fresh) <= 1e-5 * scale)
+    for k in range(0, 4096, 409):
+        x = b.positions(k).astype(np.float64)
+        assert np.all(np.diff(x) > 0) and np.all(np.abs(x) <= res["l"][k] / 2 * (1 + 1e-6))
+        e64 = oracle_lib.energy64(chains[k], x, res["l"][k])
+        assert abs(fresh[k] - e64) <= 1e-6 * max(1.0, abs(e64)), (k, fresh[k], e64)
+    avg = averages(res)
+    t = np.array([c.t for c in chains])
+    p = np.array([c.p for c in chains])
+    rho_rods = p / (t + p)  # the LJ core keeps neighbours about sigma apart; attraction adds
+    assert np.all(avg["rho"] > 0.9 * rho_rods) and np.all(avg["rho"] < 1.3)
 
 
 def _swendsen(step, actual, ideal=0.5):

@@ -90,6 +90,32 @@ def test_plain_gpu_matches_oracle(gpu, cfg):
     np.testing.assert_array_equal(gc.bits(g.separations()), gc.bits(o.separations()))
 
 
+def test_plain_gpu_config1_full_length(gpu):
+    """The reference's CPU-runnable case at its full length: NLT, N = 64,
+    L = 64/0.6, LJcut 3.0, T 1, MAXSTEP 0.3, seed 1, 2e4 sweeps = 1.28e6
+    steps, ENGCHECK 64000, RHONB 10, GNS 1, GNB 10 (bin widths covering the
+    box).  The GPU plain form and the oracle end bit for bit equal: counters,
+    RNG position, thermo sums, positions, separations, histogram counts."""
+    params = abi.make_params(n=64, l=64 / 0.6, t=1.0, cutoff=3.0, max_step=0.3, seed=1,
+                             eci=64000)
+    g, o = PlainChain(params), oracle_lib.OraclePlain(params)
+    for c in (g, o):
+        c.fad()
+        c.histograms(10, 11.0, 1, 110.0, 10, 0.5)
+    for _ in range(20):
+        g.steps(64000)
+        o.steps(64000)
+    gs, os_ = g.state(), o.state()
+    assert list(gs.d_acc) == list(os_.d_acc) and list(gs.v_acc) == list(os_.v_acc)
+    assert gs.rng_block == os_.rng_block and gs.rng_slot == os_.rng_slot
+    np.testing.assert_array_equal(gc.bits(np.array(gs.tot)), gc.bits(np.array(os_.tot)))
+    np.testing.assert_array_equal(gc.bits(np.array(gs.thermo)), gc.bits(np.array(os_.thermo)))
+    np.testing.assert_array_equal(gc.bits(g.positions()), gc.bits(o.positions()))
+    np.testing.assert_array_equal(gc.bits(g.separations()), gc.bits(o.separations()))
+    np.testing.assert_array_equal(np.asarray(g.take_rho()), np.asarray(o.take_rho()))
+    np.testing.assert_array_equal(np.asarray(g.take_g()), np.asarray(o.take_g()))
+
+
 def test_plain_gpu_replay_mode(gpu):
     """Fed an explicit table of draws (nm, rn, ran), both sides consume it alike."""
     params = abi.make_params(n=48, ensemble=abi.JMM_NPT, p=1.2, t=1.1, cutoff=3.0,
