@@ -162,3 +162,30 @@ class PlainChain:
 
     def move_volume(self, l):
         _native.call("jmm_plain_move_volume", self._h, l)
+
+
+def _main(argv=None):
+    """Steps/s of one plain chain: python -m jmmonedmc_gb300.plain [--n 256] [--npt]."""
+    import argparse
+    import time
+    ap = argparse.ArgumentParser(description=_main.__doc__)
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--npt", action="store_true", help="NPT with linear dL moves (default NLT)")
+    ap.add_argument("--rho", type=float, default=0.6)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=200)
+    args = ap.parse_args(argv)
+    params = abi.make_params(n=args.n, ensemble=abi.JMM_NPT if args.npt else abi.JMM_NLT,
+                             l=args.n / args.rho, p=1.0, t=1.0, cutoff=3.0, max_step=0.3,
+                             max_dl=1.0, seed=1, eci=0)
+    chain = PlainChain(params)
+    chain.fad()
+    chain.steps(args.warmup)
+    t0 = time.perf_counter()
+    chain.steps(args.steps)
+    dt = time.perf_counter() - t0
+    print(f"plain form, N = {args.n} {'NPT' if args.npt else 'NLT'}: {args.steps / dt:.0f} steps/s")
+
+
+if __name__ == "__main__":
+    _main()
