@@ -135,7 +135,7 @@ __device__ __forceinline__ float q_to_f(int64_t dq, float grid) {
   return __fmul_rn(__ll2float_rn(dq), grid);
 }
 
-template <int POT>
+template <int POT, int WIN>
 __global__ void __maxnreg__(72)
     domain_kernel(const LargeChain *__restrict__ chains, const LargeState *__restrict__ states,
                   jmm_chain_result *__restrict__ rec, int64_t *__restrict__ q, uint32_t n_chains,
@@ -194,7 +194,7 @@ __global__ void __maxnreg__(72)
   if (cl == 0) rp->l = (left_wall || right_wall) ? __dmul_rn(2.0, (double)q_to_f(H, ch.grid)) : 2e30;
   __syncwarp();
   const ChainParams P = domain_params(ch, ch.rec0 + d, (uint32_t)n);
-  run_chain<kG, kS, POT, false, false, true>(P, rec, nullptr, xs, ring, cfg, cl, 0xffffffffu);
+  run_chain<kG, kS, POT, false, false, true, WIN>(P, rec, nullptr, xs, ring, cfg, cl, 0xffffffffu);
   __syncwarp();
   const float inv_grid = __frcp_rn(ch.grid);
   for (int i = cl; i < n; i += 32) qc[i] = O + __float2ll_rn(__fmul_rn(xs[i], inv_grid));
@@ -431,15 +431,29 @@ __global__ void unsnap_kernel(const LargeChain *__restrict__ chains, const int64
   x[ch.x_base + i] = __dmul_rn((double)q[ch.x_base + i], (double)ch.grid);
 }
 
+typedef void (*DomainKernel)(const LargeChain *, const LargeState *, jmm_chain_result *, int64_t *,
+                             uint32_t, uint32_t, uint32_t, uint32_t, KernelCfg);
+
+// Neighbours per side a domain step looks at before it extends its window,
+// for a potential class: 3, 4 or 8, from the densest chain's neighbours
+// within the cut-off (as the batched form's defaults: rc / 0.85 sigma for a
+// 12-power core, 1.5 rho rc for the Gaussian core).
+uint32_t window_for(double need) { return need <= 3.0 ? 3u : (need <= 4.0 ? 4u : 8u); }
+
+template <int POT>
+DomainKernel domain_kernel_for(uint32_t win) {
+  return win <= 3 ? domain_kernel<POT, 3> : (win <= 4 ? domain_kernel<POT, 4> : domain_kernel<POT, 8>);
+}
+
 template <int POT>
 void launch_phase(const LargeChain *d_chains, const LargeState *d_states, jmm_chain_result *d_rec,
                   int64_t *d_q, uint32_t n_chains, uint32_t b, uint32_t phase, uint32_t doms_per_chain,
-                  const KernelCfg &kc, cudaStream_t s) {
+                  uint32_t win, const KernelCfg &kc, cudaStream_t s) {
   const uint64_t warps = (uint64_t)n_chains * doms_per_chain;
   const uint32_t blocks = (uint32_t)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock);
   const size_t smem = (size_t)kWarpsPerBlock * warp_words(b) * sizeof(float);
-  domain_kernel<POT><<<blocks, 32 * kWarpsPerBlock, smem, s>>>(d_chains, d_states, d_rec, d_q,
-                                                               n_chains, b, phase, doms_per_chain, kc);
+  domain_kernel_for<POT>(win)<<<blocks, 32 * kWarpsPerBlock, smem, s>>>(
+      d_chains, d_states, d_rec, d_q, n_chains, b, phase, doms_per_chain, kc);
 }
 
 }  // namespace
@@ -450,6 +464,8 @@ struct jmm_large {
   std::vector<LargeChain> host_chains;
   uint64_t total = 0;        // doubles in the padded position buffer
   bool pots[3] = {false, false, false};
+  uint32_t win[3] = {3, 3, 3};  // domain window per potential class (window_for)
+  double need[3] = {0.0, 0.0, 0.0};
   LargeChain *d_chains = nullptr;
   LargeState *d_states = nullptr;
   jmm_chain_result *d_rec = nullptr;  // domain records, then one per chain for the sequential sweep
@@ -583,13 +599,13 @@ static int enqueue(jmm_large *h, uint64_t n_sweeps, int mode, cudaStream_t s) {
       for (uint32_t phase = 0; phase < 2; ++phase) {
         if (h->pots[0])
           launch_phase<JMM_POT_LJCUT>(h->d_chains, h->d_states, h->d_rec, h->d_q, h->n_chains, h->b,
-                                      phase, h->doms_per_chain, kc, s);
+                                      phase, h->doms_per_chain, h->win[0], kc, s);
         if (h->pots[1])
           launch_phase<JMM_POT_SOFTSPHERE>(h->d_chains, h->d_states, h->d_rec, h->d_q, h->n_chains,
-                                           h->b, phase, h->doms_per_chain, kc, s);
+                                           h->b, phase, h->doms_per_chain, h->win[1], kc, s);
         if (h->pots[2])
           launch_phase<JMM_POT_GAUSS>(h->d_chains, h->d_states, h->d_rec, h->d_q, h->n_chains, h->b,
-                                      phase, h->doms_per_chain, kc, s);
+                                      phase, h->doms_per_chain, h->win[2], kc, s);
       }
     } else {
       const uint32_t base = h->records;
@@ -679,7 +695,11 @@ static int large_create(const jmm_batch_config *cfg, const jmm_chain_desc *chain
     lc.grid = ldexpf(1.0f, -kexp);
     lc.wall_q = (int64_t)floor(0.5 * c.l0 * ldexp(1.0, kexp));
     h->host_chains.push_back(lc);
-    h->pots[c.potential == JMM_POT_LJCUT ? 0 : (c.potential == JMM_POT_SOFTSPHERE ? 1 : 2)] = true;
+    const int pc = c.potential == JMM_POT_LJCUT ? 0 : (c.potential == JMM_POT_SOFTSPHERE ? 1 : 2);
+    h->pots[pc] = true;
+    h->need[pc] = std::max(h->need[pc], c.potential == JMM_POT_GAUSS ? 1.5 * c.n / c.l0 * c.cutoff
+                                                                   : c.cutoff / (0.85 * c.sigma));
+    h->win[pc] = window_for(h->need[pc]);
     rec += lc.n_dom;
     max_dom = std::max(max_dom, lc.n_dom);
     h->max_n = std::max(h->max_n, c.n);
@@ -721,13 +741,13 @@ static int large_create(const jmm_batch_config *cfg, const jmm_chain_desc *chain
     e = cudaMemcpy(h->d_states, st.data(), n_chains * sizeof(LargeState), cudaMemcpyHostToDevice);
   const size_t smem = (size_t)kWarpsPerBlock * warp_words(domain_size) * sizeof(float);
   if (e == cudaSuccess && smem > 48 * 1024) {
-    e = cudaFuncSetAttribute(domain_kernel<JMM_POT_LJCUT>,
+    e = cudaFuncSetAttribute(domain_kernel_for<JMM_POT_LJCUT>(h->win[0]),
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(domain_kernel<JMM_POT_SOFTSPHERE>,
+      e = cudaFuncSetAttribute(domain_kernel_for<JMM_POT_SOFTSPHERE>(h->win[1]),
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(domain_kernel<JMM_POT_GAUSS>,
+      e = cudaFuncSetAttribute(domain_kernel_for<JMM_POT_GAUSS>(h->win[2]),
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
   if (e != cudaSuccess) {
