@@ -380,6 +380,25 @@ int jmm_batch_run_sampled_async(jmm_batch *b, uint64_t n_sweeps, uint32_t sample
                                 void *stream);
 int jmm_batch_grad_stats(jmm_batch *b, jmm_grad_stats *out, uint32_t n_chains);
 
+/* Sampled rho(x) and g(x) histograms of every chain, the layout of the
+ * reference's printRho / printG (src/jmmMCState.cpp:1021-1061) and its bin
+ * rules (fgrho / qagrho, :1069-1127, :2297-2384): rhonb position bins
+ * floor(x / rbw + rhonb/2); gns slices floor(x / gsw + gns/2) x gnb
+ * separation bins floor(|x_j - x_i| / gbw), each pair counted in the slice
+ * of both particles (FP32 arithmetic on the chains' positions).  Unlike the
+ * reference, which adds the counts of every step, a batch adds a sample
+ * when asked: jmm_batch_sample_histograms, and after every sample_every
+ * sweeps of jmm_batch_run_sampled once histograms are configured.
+ * Configuring (again) clears them. */
+int jmm_batch_histograms(jmm_batch *b, uint32_t rhonb, double rbw, uint32_t gns, double gsw,
+                         uint32_t gnb, double gbw);
+/* Adds the current configuration of every chain, enqueued on stream
+ * (cudaStream_t as void*, NULL = the batch's own), no wait. */
+int jmm_batch_sample_histograms(jmm_batch *b, void *stream);
+/* Per chain (user order) one row of 1 + rhonb + gns*gnb counts: samples,
+ * rho bins, then g bins slice by slice; n = n_chains * row length. */
+int jmm_batch_take_histograms(jmm_batch *b, uint64_t *out, uint64_t n);
+
 /* Host-buffer convenience: create, upload positions (NULL = the configured
  * initial lattice), run n_sweeps, copy results and positions back, destroy. */
 int jmm_batch_run_host(const jmm_batch_config *cfg, const jmm_chain_desc *chains,

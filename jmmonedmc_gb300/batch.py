@@ -17,6 +17,10 @@ _native.register({
     "jmm_batch_create": [P(abi.BatchConfig), P(abi.ChainDesc), C.c_uint32, P(C.c_void_p)],
     "jmm_batch_create_at": [P(abi.BatchConfig), P(abi.ChainDesc), C.c_uint32, P(C.c_float),
                             P(C.c_void_p)],
+    "jmm_batch_histograms": [C.c_void_p, C.c_uint32, C.c_double, C.c_uint32, C.c_double,
+                             C.c_uint32, C.c_double],
+    "jmm_batch_sample_histograms": [C.c_void_p, C.c_void_p],
+    "jmm_batch_take_histograms": [C.c_void_p, P(C.c_uint64), C.c_uint64],
     "jmm_batch_run": [C.c_void_p, C.c_uint64],
     "jmm_batch_run_async": [C.c_void_p, C.c_uint64, C.c_void_p],
     "jmm_batch_results": [C.c_void_p, P(abi.ChainResult), C.c_uint32],
@@ -176,6 +180,30 @@ class ChainBatch:
         buf = (abi.GradStats * self.n_chains)()
         _native.call("jmm_batch_grad_stats", self._h, buf, self.n_chains)
         return np.frombuffer(buf, dtype=np.dtype(abi.GRAD_STATS_DTYPE)).copy()
+
+    # --- sampled rho(x) / g(x) histograms
+    def histograms(self, rhonb, rbw, gns, gsw, gnb, gbw):
+        """Configures (and clears) the chains' sampled histograms: rhonb
+        position bins of width rbw, gns slices of width gsw x gnb separation
+        bins of width gbw (the reference's RHONB/RBW/GNS/GSW/GNB/GBW)."""
+        _native.call("jmm_batch_histograms", self._h, rhonb, rbw, gns, gsw, gnb, gbw)
+        self._hist = (rhonb, gns, gnb)
+
+    def sample_histograms(self, stream=None):
+        """Adds the current configuration of every chain (enqueued)."""
+        _native.call("jmm_batch_sample_histograms", self._h,
+                     C.c_void_p(stream) if stream else None)
+
+    def take_histograms(self):
+        """{"samples": (chains,), "rho": (chains, rhonb), "g": (chains, gns, gnb)}."""
+        rhonb, gns, gnb = self._hist
+        width = 1 + rhonb + gns * gnb
+        out = np.empty(self.n_chains * width, dtype=np.uint64)
+        _native.call("jmm_batch_take_histograms", self._h, out.ctypes.data_as(P(C.c_uint64)),
+                     out.size)
+        rows = out.reshape(self.n_chains, width)
+        return {"samples": rows[:, 0].copy(), "rho": rows[:, 1:1 + rhonb].copy(),
+                "g": rows[:, 1 + rhonb:].reshape(self.n_chains, gns, gnb).copy()}
 
     def autotune(self, trial_sweeps=4):
         """(lanes_per_chain, steps_per_round, chains_per_block) chosen."""

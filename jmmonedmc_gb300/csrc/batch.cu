@@ -115,6 +115,10 @@ struct jmm_batch {
   double *d_gout = nullptr;             // 4 per chain
   jmm_grad_stats *d_gstats = nullptr;   // user order
   std::map<std::pair<uint64_t, uint32_t>, cudaGraphExec_t> sampled;  // (sweeps, every)
+  // sampled rho(x) / g(x) histograms (jmm_batch_histograms): one row per chain
+  uint64_t *d_hist = nullptr;
+  uint32_t h_rhonb = 0, h_gns = 0, h_gnb = 0;
+  float h_rbw = 0.0f, h_gsw = 0.0f, h_gbw = 0.0f;
 };
 
 static void drop_graphs(jmm_batch *b) {
@@ -128,6 +132,7 @@ static void batch_free(jmm_batch *b) {
   if (!b) return;
   drop_graphs(b);
   cudaFree(b->d_block);  // every device array of the batch
+  cudaFree(b->d_hist);
   for (int k = 0; k < 3; ++k) {
     if (b->side[k]) cudaStreamDestroy(b->side[k]);
     if (b->join[k]) cudaEventDestroy(b->join[k]);
@@ -1093,6 +1098,113 @@ extern "C" int jmm_batch_energy_grad(jmm_batch *b, double *out, uint32_t n_chain
   return JMM_OK;
 }
 
+// ---- sampled rho(x) and g(x) histograms ------------------------------------
+
+// Bin floor(x / w + nb / 2) of a position (rho) or a slice (g), in FP32 as
+// the oracle restates it; -1 outside [0, nb).
+__device__ __forceinline__ int hist_bin(float x, float w, uint32_t nb) {
+  const float f = floorf(__fadd_rn(__fdiv_rn(x, w), __fmul_rn(0.5f, (float)nb)));
+  return (f >= 0.0f && f < (float)nb) ? (int)f : -1;
+}
+
+// One warp per chain (user order): adds the current configuration to the
+// chain's row [samples, rho bins, g bins].  Pairs are taken in index order
+// from each particle to the right (on a ring, through the wrap, at most half
+// way round) until the separation reaches gnb * gbw.
+__global__ void batch_hist_kernel(const jmm_chain_desc *__restrict__ desc,
+                                  const uint64_t *__restrict__ xoff, const float *__restrict__ x,
+                                  const jmm_chain_result *__restrict__ res, uint32_t n_chains,
+                                  int32_t boundary, uint32_t rhonb, float rbw, uint32_t gns,
+                                  float gsw, uint32_t gnb, float gbw, uint64_t *__restrict__ hist) {
+  const uint32_t c = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  if (c >= n_chains) return;
+  const int lane = threadIdx.x & 31;
+  const int n = (int)desc[c].n;
+  const float *xc = x + xoff[c];
+  const bool periodic = boundary == JMM_BOUNDARY_PERIODIC;
+  const float lf = (float)res[c].l;
+  const float range = __fmul_rn((float)gnb, gbw);
+  uint64_t *row = hist + (uint64_t)c * (1u + rhonb + gns * gnb);
+  uint64_t *g = row + 1 + rhonb;
+  if (lane == 0) row[0] += 1;
+  for (int i = lane; i < n; i += 32) {
+    const float xi = xc[i];
+    const int rb = hist_bin(xi, rbw, rhonb);
+    if (rb >= 0) atomicAdd((unsigned long long *)&row[1 + rb], 1ull);
+    const int si = hist_bin(xi, gsw, gns);
+    for (int k = 1; k < n; ++k) {
+      if (periodic && 2 * k > n) break;  // the other way round is shorter
+      int j = i + k;
+      float shift = 0.0f;
+      if (j >= n) {
+        if (!periodic) break;
+        j -= n;
+        shift = lf;
+      }
+      const float xj = xc[j];
+      const float d = __fsub_rn(__fadd_rn(xj, shift), xi);
+      if (!(d < range)) break;
+      const float gf = floorf(__fdiv_rn(d, gbw));
+      if (!(gf < (float)gnb)) continue;
+      const int gb = (int)gf;
+      if (si >= 0) atomicAdd((unsigned long long *)&g[(uint64_t)si * gnb + gb], 1ull);
+      const int sj = hist_bin(xj, gsw, gns);  // the partner's own slice
+      if (sj >= 0) atomicAdd((unsigned long long *)&g[(uint64_t)sj * gnb + gb], 1ull);
+    }
+  }
+}
+
+static int launch_hist(jmm_batch *b, cudaStream_t s) {
+  const uint32_t per_block = 8;
+  const uint32_t blocks = (b->n_chains + per_block - 1) / per_block;
+  batch_hist_kernel<<<blocks, 32 * per_block, 0, s>>>(
+      b->d_desc, b->d_xoff, b->d_x, b->d_res, b->n_chains, b->cfg.boundary, b->h_rhonb, b->h_rbw,
+      b->h_gns, b->h_gsw, b->h_gnb, b->h_gbw, b->d_hist);
+  JMM_CUDA(cudaGetLastError());
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_histograms(jmm_batch *b, uint32_t rhonb, double rbw, uint32_t gns,
+                                    double gsw, uint32_t gnb, double gbw) {
+  clear_error();
+  JMM_CHECK_ARG(b, "null handle");
+  JMM_CHECK_ARG(rhonb > 0 && gns > 0 && gnb > 0, "bin counts must be positive");
+  JMM_CHECK_ARG(rbw > 0 && gsw > 0 && gbw > 0, "bin widths must be positive");
+  JMM_CHECK_ARG((uint64_t)rhonb + (uint64_t)gns * gnb <= (1u << 20), "at most 2^20 bins per chain");
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  cudaFree(b->d_hist);
+  b->d_hist = nullptr;
+  const uint64_t words = (uint64_t)b->n_chains * (1u + rhonb + gns * gnb);
+  JMM_CUDA(cudaMalloc((void **)&b->d_hist, words * sizeof(uint64_t)));
+  JMM_CUDA(cudaMemset(b->d_hist, 0, words * sizeof(uint64_t)));
+  b->h_rhonb = rhonb;
+  b->h_gns = gns;
+  b->h_gnb = gnb;
+  b->h_rbw = (float)rbw;
+  b->h_gsw = (float)gsw;
+  b->h_gbw = (float)gbw;
+  drop_graphs(b);  // sampled runs now take histograms too
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_sample_histograms(jmm_batch *b, void *stream) {
+  clear_error();
+  JMM_CHECK_ARG(b, "null handle");
+  JMM_CHECK_ARG(b->d_hist, "no histograms configured (jmm_batch_histograms)");
+  return launch_hist(b, stream ? (cudaStream_t)stream : b->stream);
+}
+
+extern "C" int jmm_batch_take_histograms(jmm_batch *b, uint64_t *out, uint64_t n) {
+  clear_error();
+  JMM_CHECK_ARG(b && out, "null argument");
+  JMM_CHECK_ARG(b->d_hist, "no histograms configured (jmm_batch_histograms)");
+  const uint64_t words = (uint64_t)b->n_chains * (1u + b->h_rhonb + b->h_gns * b->h_gnb);
+  JMM_CHECK_ARG(n == words, "out must hold n_chains * (1 + rhonb + gns * gnb) counts");
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  JMM_CUDA(cudaMemcpy(out, b->d_hist, words * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  return JMM_OK;
+}
+
 extern "C" int jmm_batch_run_sampled(jmm_batch *b, uint64_t n_sweeps, uint32_t sample_every) {
   int rc = jmm_batch_run_sampled_async(b, n_sweeps, sample_every, nullptr);
   if (rc) return rc;
@@ -1122,6 +1234,7 @@ extern "C" int jmm_batch_run_sampled_async(jmm_batch *b, uint64_t n_sweeps, uint
     while (rc == JMM_OK && done + sample_every <= n_sweeps) {
       rc = launch(b, sample_every, b->stream);
       if (rc == JMM_OK) rc = launch_grad(b, true, b->stream);
+      if (rc == JMM_OK && b->d_hist) rc = launch_hist(b, b->stream);
       done += sample_every;
     }
     if (rc == JMM_OK && done < n_sweeps) rc = launch(b, n_sweeps - done, b->stream);

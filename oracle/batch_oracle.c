@@ -683,3 +683,49 @@ void jmmo_energy_grad64(const jmm_chain_desc *c, const double *x, double l, int 
   out[2] = gs;
   out[3] = rd / l;
 }
+
+/* One histogram sample of one chain (the batched form's
+ * jmm_batch_sample_histograms): row[0] += 1; position bins
+ * floor(x / rbw + rhonb/2) and slice bins floor(x / gsw + gns/2) in FP32;
+ * pairs to the right of each particle (on a ring through the wrap, at most
+ * half way round) until the FP32 separation reaches gnb * gbw, bin
+ * floor(d / gbw), counted in the slice of both particles.  The layout and
+ * bin rules are those of the reference's printRho / printG and fgrho
+ * (src/jmmMCState.cpp:1021-1061, :1069-1127). */
+static int hist_bin32(float x, float w, uint32_t nb) {
+  const float f = floorf(x / w + 0.5f * (float)nb);
+  return (f >= 0.0f && f < (float)nb) ? (int)f : -1;
+}
+
+void jmmo_batch_hist_sample(const float *x, uint32_t n, float l, int periodic, uint32_t rhonb,
+                            float rbw, uint32_t gns, float gsw, uint32_t gnb, float gbw,
+                            uint64_t *row) {
+  uint64_t *g = row + 1 + rhonb;
+  const float range = (float)gnb * gbw;
+  row[0] += 1;
+  for (uint32_t i = 0; i < n; ++i) {
+    const float xi = x[i];
+    const int rb = hist_bin32(xi, rbw, rhonb);
+    if (rb >= 0) row[1 + rb] += 1;
+    const int si = hist_bin32(xi, gsw, gns);
+    for (uint32_t k = 1; k < n; ++k) {
+      if (periodic && 2 * k > n) break;
+      uint32_t j = i + k;
+      float shift = 0.0f;
+      if (j >= n) {
+        if (!periodic) break;
+        j -= n;
+        shift = l;
+      }
+      const float xj = x[j];
+      const float d = (xj + shift) - xi;
+      if (!(d < range)) break;
+      const float gf = floorf(d / gbw);
+      if (!(gf < (float)gnb)) continue;
+      const int gb = (int)gf;
+      if (si >= 0) g[(uint64_t)si * gnb + gb] += 1;
+      const int sj = hist_bin32(xj, gsw, gns);
+      if (sj >= 0) g[(uint64_t)sj * gnb + gb] += 1;
+    }
+  }
+}

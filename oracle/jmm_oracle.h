@@ -54,6 +54,9 @@ int jmmo_batch_set_positions(jmmo_batch *b, uint32_t chain, const double *x, uin
                              double l);
 int jmmo_batch_energies(jmmo_batch *b, double *e, uint32_t n_chains);
 double jmmo_energy64(const jmm_chain_desc *c, const double *x, double l, int periodic);
+void jmmo_batch_hist_sample(const float *x, uint32_t n, float l, int periodic, uint32_t rhonb,
+                            float rbw, uint32_t gns, float gsw, uint32_t gnb, float gbw,
+                            uint64_t *row);
 void jmmo_energy_grad64(const jmm_chain_desc *c, const double *x, double l, int periodic,
                         double out[4]);
 float jmmo_portable_logf(float x);

@@ -223,6 +223,9 @@ extra_sigs({
     "jmmo_batch_energies": ([vp, P(dbl), u32], C.c_int),
     "jmmo_energy64": ([P(abi.ChainDesc), P(dbl), dbl, C.c_int], dbl),
     "jmmo_energy_grad64": ([P(abi.ChainDesc), P(dbl), dbl, C.c_int, P(dbl)], None),
+    "jmmo_batch_hist_sample": ([P(C.c_float), C.c_uint32, C.c_float, C.c_int, C.c_uint32,
+                                C.c_float, C.c_uint32, C.c_float, C.c_uint32, C.c_float,
+                                P(C.c_uint64)], None),
     "jmmo_portable_logf": ([C.c_float], C.c_float),
     "jmmo_portable_expf": ([C.c_float], C.c_float),
 })
@@ -289,6 +292,19 @@ def energy64(chain_desc, x, l, periodic=False):
     x = np.ascontiguousarray(x, dtype=np.float64)
     return lib.jmmo_energy64(C.byref(chain_desc), x.ctypes.data_as(P(dbl)), float(l),
                              1 if periodic else 0)
+
+
+def hist_sample(x, l, periodic, rhonb, rbw, gns, gsw, gnb, gbw, row=None):
+    """Adds one histogram sample of a chain's FP32 positions to row (the
+    batched form's layout: samples, rho bins, g bins); returns row."""
+    lib = load()
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    if row is None:
+        row = np.zeros(1 + rhonb + gns * gnb, dtype=np.uint64)
+    lib.jmmo_batch_hist_sample(x.ctypes.data_as(P(C.c_float)), x.size, float(l),
+                               1 if periodic else 0, rhonb, rbw, gns, gsw, gnb, gbw,
+                               row.ctypes.data_as(P(C.c_uint64)))
+    return row
 
 
 def energy_grad64(chain_desc, x, l, periodic=False):

@@ -280,6 +280,41 @@ def test_npt_batch_at_full_size(gpu):
     assert np.all(avg["rho"] > 0.9 * rho_rods) and np.all(avg["rho"] < 1.3)
 
 
+@pytest.mark.parametrize("boundary", [abi.JMM_BOUNDARY_WALLS, abi.JMM_BOUNDARY_PERIODIC])
+def test_batch_histograms_match_oracle(gpu, boundary):
+    """Sampled rho(x) / g(x) histograms of a mixed batch equal the oracle's
+    counts of the same positions, sample by sample; run_sampled adds one
+    sample every sample_every sweeps; configuring again clears them."""
+    periodic = boundary == abi.JMM_BOUNDARY_PERIODIC
+    rng = np.random.default_rng(31)
+    chains = _mixed_chains(rng, 16, 40, 300,
+                           pots=(abi.JMM_POT_LJCUT, abi.JMM_POT_SOFTSPHERE, abi.JMM_POT_GAUSS))
+    b = ChainBatch(abi.make_batch_config(seed=9, boundary=boundary, resum_sweeps=4), chains)
+    hp = (30, 12.0, 3, 150.0, 25, 0.2)  # rhonb, rbw, gns, gsw, gnb, gbw
+    b.histograms(*hp)
+    width = 1 + hp[0] + hp[2] * hp[4]
+    ref = [np.zeros(width, dtype=np.uint64) for _ in chains]
+    for sweeps in (0, 3, 10):
+        if sweeps:
+            b.run(sweeps)
+        b.sample_histograms()
+        res = b.results()
+        for k in range(len(chains)):
+            oracle_lib.hist_sample(b.positions(k), res["l"][k], periodic, *hp, row=ref[k])
+    got = b.take_histograms()
+    for k in range(len(chains)):
+        assert got["samples"][k] == ref[k][0] == 3
+        assert np.array_equal(got["rho"][k], ref[k][1:1 + hp[0]]), k
+        assert np.array_equal(got["g"][k].ravel(), ref[k][1 + hp[0]:]), k
+    assert got["g"].sum() > 0 and got["rho"].sum() > 0
+    b.histograms(*hp)
+    b.run_sampled(20, 5)
+    again = b.take_histograms()
+    assert np.all(again["samples"] == 4)
+    n = np.array([c.n for c in chains], dtype=np.uint64)
+    assert np.all(again["rho"].sum(axis=1) <= 4 * n)
+
+
 def _swendsen(step, actual, ideal=0.5):
     """maxDisAdjust's rescale (src/jmmMCState.cpp:2100-2116)."""
     return step * np.log(0.672924 * ideal + 0.0644284) / np.log(0.672924 * (actual + 0.0644284))
