@@ -480,17 +480,38 @@ struct jmm_large {
   int mode = 0;              // records holding the open changes: 0 domains, 1 sequential
 };
 
+// A handle's device memory comes from the device's stream-ordered pool,
+// which keeps up to 16 GiB of freed blocks for the next handle, so that
+// repeated one-call runs (jmm_large_run_host) do not map and unmap
+// gigabytes each time.
+static cudaError_t pool_alloc(void **p, size_t bytes, cudaStream_t s) {
+  static bool configured = false;
+  if (!configured) {
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = 16ull << 30;
+      cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      if (keep < (16ull << 30)) {
+        keep = 16ull << 30;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      }
+    }
+    configured = true;
+  }
+  return cudaMallocAsync(p, bytes, s);
+}
+
 static void large_free(jmm_large *h) {
   if (!h) return;
-  cudaFree(h->d_chains);
-  cudaFree(h->d_states);
-  cudaFree(h->d_rec);
-  cudaFree(h->d_q);
-  cudaFree(h->d_stage);
-  cudaFree(h->d_bad);
-  cudaFree(h->d_e);
-  cudaFree(h->d_part);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  void *bufs[8] = {h->d_chains, h->d_states, h->d_rec, h->d_q,
+                   h->d_stage,  h->d_bad,    h->d_e,   h->d_part};
+  for (void *p : bufs)
+    if (p) cudaFreeAsync(p, h->stream);
+  if (h->stream) {
+    cudaStreamSynchronize(h->stream);
+    cudaStreamDestroy(h->stream);
+  }
   delete h;
 }
 
@@ -557,7 +578,7 @@ static int check_positions(jmm_large *h, uint32_t c0, uint32_t c1, const char *w
 // device: one copy per chain into the staging buffer, then snapped.
 static int upload_positions(jmm_large *h, const double *x, uint32_t c0, uint32_t c1,
                             const char *what) {
-  if (!h->d_stage) JMM_CUDA(cudaMalloc((void **)&h->d_stage, h->total * sizeof(double)));
+  if (!h->d_stage) JMM_CUDA(pool_alloc((void **)&h->d_stage, h->total * sizeof(double), h->stream));
   JMM_CUDA(cudaMemsetAsync(h->d_bad, 0, sizeof(uint32_t), h->stream));
   uint64_t src = 0;
   for (uint32_t k = c0; k < c1; ++k) {
@@ -572,7 +593,7 @@ static int upload_positions(jmm_large *h, const double *x, uint32_t c0, uint32_t
 }
 
 static int download_positions(jmm_large *h, double *x, uint32_t c0, uint32_t c1) {
-  if (!h->d_stage) JMM_CUDA(cudaMalloc((void **)&h->d_stage, h->total * sizeof(double)));
+  if (!h->d_stage) JMM_CUDA(pool_alloc((void **)&h->d_stage, h->total * sizeof(double), h->stream));
   unsnap_kernel<<<chain_grid(h, c0, c1, 0), 256, 0, h->stream>>>(h->d_chains, h->d_q, h->d_stage, c0);
   JMM_CUDA(cudaGetLastError());
   uint64_t dst = 0;
@@ -715,15 +736,18 @@ static int large_create(const jmm_batch_config *cfg, const jmm_chain_desc *chain
 
   const uint64_t n_rec = rec + n_chains;
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_chains, n_chains * sizeof(LargeChain));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_states, n_chains * sizeof(LargeState));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_rec, n_rec * sizeof(jmm_chain_result));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_q, off * sizeof(int64_t));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_e, n_chains * sizeof(double));
+  cudaStream_t hs = h->stream;
+  if (e == cudaSuccess) e = pool_alloc((void **)&h->d_chains, n_chains * sizeof(LargeChain), hs);
+  if (e == cudaSuccess) e = pool_alloc((void **)&h->d_states, n_chains * sizeof(LargeState), hs);
+  if (e == cudaSuccess) e = pool_alloc((void **)&h->d_rec, n_rec * sizeof(jmm_chain_result), hs);
+  if (e == cudaSuccess) e = pool_alloc((void **)&h->d_q, off * sizeof(int64_t), hs);
+  if (e == cudaSuccess) e = pool_alloc((void **)&h->d_e, n_chains * sizeof(double), hs);
   if (e == cudaSuccess)
-    e = cudaMalloc((void **)&h->d_part, (size_t)n_chains * ((h->max_n + kEnergySeg - 1) / kEnergySeg) *
-                                            sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&h->d_bad, sizeof(uint32_t));
+    e = pool_alloc((void **)&h->d_part,
+                   (size_t)n_chains * ((h->max_n + kEnergySeg - 1) / kEnergySeg) * sizeof(double), hs);
+  if (e == cudaSuccess) e = pool_alloc((void **)&h->d_bad, sizeof(uint32_t), hs);
+  // the copies below run on the legacy stream: the allocations first
+  if (e == cudaSuccess) e = cudaStreamSynchronize(hs);
   if (e != cudaSuccess) {
     const int rc = cuda_status(e, "jmm_large_create allocation", __FILE__, __LINE__);
     large_free(h);
