@@ -271,7 +271,8 @@ typedef struct jmm_batch_config {
   double jitter;             /* half-width of the initial jitter               */
   uint32_t window;           /* neighbours W per side a trial move looks at
                                 before it extends its window: 0 = max(4, G/2);
-                                8 with the shapes 2x16, 4x8 and 8x4            */
+                                8 with the shapes 2x16, 4x8 and 8x4, 3 with
+                                2x16                                           */
   uint32_t reserved;         /* 0                                               */
 } jmm_batch_config;
 

@@ -49,6 +49,7 @@ ChainsKernel pick_kernel(uint32_t g, uint32_t s, uint32_t w, bool exact, int pot
     return exact ? pick_pot<G_, S_, true, W_>(pot, per) : pick_pot<G_, S_, false, W_>(pot, per);
   JMM_SHAPE(4, 8, 4)
   JMM_SHAPE(2, 16, 4)
+  JMM_SHAPE(2, 16, 3)
   JMM_SHAPE(4, 4, 4)
   JMM_SHAPE(4, 2, 4)
   JMM_SHAPE(8, 4, 4)
@@ -177,7 +178,7 @@ static int apply_layout(jmm_batch *b, const Shape shapes[3]) {
     if (!pick_kernel(g, spr, win, false, JMM_POT_LJCUT, false))
       return fail(JMM_ERR_INVALID, "unsupported launch shape: lanes_per_chain x steps_per_round "
                   "must be 2x16, 4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or 32x1, with a window "
-                  "of 0 (the default) or 8 for 2x16, 4x8 and 8x4");
+                  "of 0 (the default), 8 for 2x16, 4x8 and 8x4, or 3 for 2x16");
     if (cpb == 0 || cpb * g * spr > 256)
       return fail(JMM_ERR_INVALID, "chains_per_block * lanes per chain must be <= 256");
     const uint64_t ring_floats = (uint64_t)cpb * kRingWords;
@@ -278,7 +279,8 @@ static void default_shapes(const jmm_batch *b, Shape sh[3]) {
     }
     const uint32_t gg = need > 8.0 ? 32u : (n_max >= 1024 ? 2u : 4u);
     const uint32_t ss = 32 / gg;
-    const uint32_t ww = need > 8.0 ? 16u : (need > 4.0 ? 8u : 4u);
+    // two lanes a step may look at 3 neighbours per side where 3 suffice
+    const uint32_t ww = need > 8.0 ? 16u : (need > 4.0 ? 8u : (need > 3.0 || gg != 2 ? 4u : 3u));
     sh[pi] = Shape{gg, ss, 128 / (gg * ss), ww};
   }
 }
@@ -362,7 +364,7 @@ static int validate(const jmm_batch_config *cfg, const jmm_chain_desc *chains, u
     if (!pick_kernel(g, spr, cfg->window, false, JMM_POT_LJCUT, false))
       return fail(JMM_ERR_INVALID, "unsupported launch shape: lanes_per_chain x steps_per_round "
                   "must be 2x16, 4x8, 4x4, 4x2, 8x4, 8x2, 16x2, 16x1 or 32x1, with a window "
-                  "of 0 (the default) or 8 for 2x16, 4x8 and 8x4");
+                  "of 0 (the default), 8 for 2x16, 4x8 and 8x4, or 3 for 2x16");
   }
   for (uint32_t k = 0; k < n_chains; ++k) {
     const jmm_chain_desc &c = chains[k];
@@ -821,7 +823,7 @@ extern "C" int jmm_batch_device_views(jmm_batch *b, void **positions, void **res
 }
 
 // Launch shapes tried by the autotuner: G x S, and threads per block.
-static const uint32_t kTuneShapes[][3] = {{4, 8, 4}, {2, 16, 4}, {4, 4, 4}, {4, 2, 4},
+static const uint32_t kTuneShapes[][3] = {{4, 8, 4}, {2, 16, 4}, {2, 16, 3}, {4, 4, 4}, {4, 2, 4},
                                           {8, 4, 4}, {8, 2, 4}, {16, 2, 8}, {16, 1, 8},
                                           {32, 1, 16}, {4, 8, 8}, {2, 16, 8}, {8, 4, 8}};
 static const uint32_t kTuneThreads[] = {32u, 64u, 128u, 256u};

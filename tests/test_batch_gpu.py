@@ -71,7 +71,7 @@ EXACT_CASES = {
 
 # (lanes, steps per round, neighbours per side; 0 = the default of the lanes)
 SHAPES = [(4, 8, 0), (2, 16, 0), (4, 4, 0), (4, 2, 0), (8, 4, 0), (8, 2, 0), (16, 2, 0),
-          (16, 1, 0), (32, 1, 0), (4, 8, 8), (2, 16, 8), (8, 4, 8)]
+          (16, 1, 0), (32, 1, 0), (4, 8, 8), (2, 16, 8), (8, 4, 8), (2, 16, 3)]
 
 
 @pytest.mark.parametrize("shape", SHAPES, ids=[f"{g}x{s}w{w}" for g, s, w in SHAPES])
