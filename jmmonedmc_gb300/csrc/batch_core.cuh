@@ -29,10 +29,11 @@
 // Every FP32/FP64 operation is an explicit round-to-nearest intrinsic so
 // that the EXACT precision mode can be replayed bit for bit by the oracle;
 // the FAST mode differs in using the hardware reciprocal, exp and log, in
-// scaling a window's summed pair shapes by the potential's strength once, and
-// in summing a round's per-step statistics by a scan over its slots into
-// per-lane shares instead of step by step (the same quantities, rounded in
-// another order).
+// scaling a window's summed pair shapes by the potential's strength once, in
+// summing a volume move's pair terms per lane in FP32 before the FP64 lane
+// sum, and in summing a round's per-step statistics by a scan over its slots
+// into per-lane shares instead of step by step (the same quantities, rounded
+// in another order).
 #pragma once
 #include <math.h>
 #include <stdint.h>
