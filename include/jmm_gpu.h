@@ -305,6 +305,13 @@ int jmm_batch_run(jmm_batch *b, uint64_t n_sweeps);
 /* Same, enqueued on a CUDA stream (cudaStream_t passed as void*), no wait. */
 int jmm_batch_run_async(jmm_batch *b, uint64_t n_sweeps, void *stream);
 int jmm_batch_results(jmm_batch *b, jmm_chain_result *out, uint32_t n_chains);
+/* Replaces every chain's record (state and sums: energy, box length, step
+ * count, accumulators, counters), e.g. from a checkpoint taken with
+ * jmm_batch_results together with the positions: the chains then continue
+ * exactly as the checkpointed ones (the step count selects the Philox
+ * blocks).  Box lengths must be positive; with walls every chain's positions
+ * must lie within +-l/2 of the record's box length. */
+int jmm_batch_set_results(jmm_batch *b, const jmm_chain_result *in, uint32_t n_chains);
 /* Zero the statistics (sums, samples, counters) but keep the state. */
 int jmm_batch_reset_stats(jmm_batch *b);
 int jmm_batch_get_positions(jmm_batch *b, uint32_t chain, float *x, uint32_t n);

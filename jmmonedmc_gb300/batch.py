@@ -24,6 +24,7 @@ _native.register({
     "jmm_batch_run": [C.c_void_p, C.c_uint64],
     "jmm_batch_run_async": [C.c_void_p, C.c_uint64, C.c_void_p],
     "jmm_batch_results": [C.c_void_p, P(abi.ChainResult), C.c_uint32],
+    "jmm_batch_set_results": [C.c_void_p, P(abi.ChainResult), C.c_uint32],
     "jmm_batch_reset_stats": [C.c_void_p],
     "jmm_batch_get_positions": [C.c_void_p, C.c_uint32, P(C.c_float), C.c_uint32],
     "jmm_batch_set_positions": [C.c_void_p, C.c_uint32, P(C.c_float), C.c_uint32, C.c_double],
@@ -113,6 +114,47 @@ class ChainBatch:
         buf = (abi.ChainResult * self.n_chains)()
         _native.call("jmm_batch_results", self._h, buf, self.n_chains)
         return results_to_numpy(buf)
+
+    def set_results(self, res):
+        """Replaces every chain's record (a structured array as results() gives)."""
+        res = np.ascontiguousarray(res, dtype=np.dtype(abi.CHAIN_RESULT_DTYPE))
+        if res.shape != (self.n_chains,):
+            raise ValueError("one record per chain")
+        buf = (abi.ChainResult * self.n_chains).from_buffer_copy(res.tobytes())
+        _native.call("jmm_batch_set_results", self._h, buf, self.n_chains)
+
+    # --- checkpoint / resume
+    def checkpoint(self, path):
+        """Saves the batch (configuration with its launch shape, chains with
+        their current step sizes and box lengths, positions, records) to a
+        .npz file; restore() continues it exactly.  (A FAST batch whose
+        potential classes were tuned to different shapes restarts on the
+        per-class defaults: the same chains statistically, not bit for bit.)"""
+        res = self.results()
+        config = abi.BatchConfig.from_buffer_copy(bytes(self.config))
+        shapes = set(self.shapes().values())
+        if len(shapes) == 1:
+            (config.lanes_per_chain, config.steps_per_round, config.chains_per_block,
+             config.window) = shapes.pop()
+        desc = (abi.ChainDesc * self.n_chains).from_buffer_copy(bytes(self._arr))
+        view = chain_view(desc)
+        view["max_step"], view["vol_step"] = self.step_sizes()
+        view["l0"] = res["l"]
+        x = np.concatenate([self.positions(k) for k in range(self.n_chains)])
+        np.savez(path, config=np.frombuffer(bytes(config), dtype=np.uint8),
+                 chains=np.frombuffer(bytes(desc), dtype=np.uint8), positions=x, results=res)
+
+    @classmethod
+    def restore(cls, path):
+        """A batch from a checkpoint() file, in the checkpointed state."""
+        with np.load(path) as f:
+            config = abi.BatchConfig.from_buffer_copy(f["config"].tobytes())
+            raw = f["chains"].tobytes()
+            n = len(raw) // C.sizeof(abi.ChainDesc)
+            desc = (abi.ChainDesc * n).from_buffer_copy(raw)
+            b = cls(config, desc, x=f["positions"])
+            b.set_results(f["results"])
+        return b
 
     def reset_stats(self):
         _native.call("jmm_batch_reset_stats", self._h)

@@ -9,6 +9,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <map>
 #include <new>
 #include <numeric>
@@ -675,6 +676,31 @@ extern "C" int jmm_batch_results(jmm_batch *b, jmm_chain_result *out, uint32_t n
   JMM_CHECK_ARG(n_chains == b->n_chains, "n_chains does not match the batch");
   JMM_CUDA(cudaStreamSynchronize(b->stream));
   JMM_CUDA(cudaMemcpy(out, b->d_res, n_chains * sizeof(jmm_chain_result), cudaMemcpyDeviceToHost));
+  return JMM_OK;
+}
+
+extern "C" int jmm_batch_set_results(jmm_batch *b, const jmm_chain_result *in, uint32_t n_chains) {
+  clear_error();
+  JMM_CHECK_ARG(b && in, "null argument");
+  JMM_CHECK_ARG(n_chains == b->n_chains, "n_chains does not match the batch");
+  const bool walls = b->cfg.boundary != JMM_BOUNDARY_PERIODIC;
+  std::vector<float> x;
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  if (walls) {
+    x.resize(b->total_floats);
+    JMM_CUDA(cudaMemcpy(x.data(), b->d_x, x.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  }
+  for (uint32_t k = 0; k < n_chains; ++k) {
+    if (!(in[k].l > 0) || !std::isfinite(in[k].l) || !std::isfinite(in[k].e))
+      return fail(JMM_ERR_INVALID, "chain %u: box length and energy must be finite, L > 0", k);
+    if (walls) {  // ordered positions: the end particles decide
+      const float *xc = x.data() + b->x_off[k];
+      const float half = (float)(0.5 * in[k].l) * (1.0f + 1e-6f);
+      if (!(fabsf(xc[0]) <= half) || !(fabsf(xc[b->chains[k].n - 1]) <= half))
+        return fail(JMM_ERR_INVALID, "chain %u: positions lie beyond the walls of the record's L", k);
+    }
+  }
+  JMM_CUDA(cudaMemcpy(b->d_res, in, n_chains * sizeof(jmm_chain_result), cudaMemcpyHostToDevice));
   return JMM_OK;
 }
 

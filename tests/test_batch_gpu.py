@@ -315,6 +315,32 @@ def test_batch_histograms_match_oracle(gpu, boundary):
     assert np.all(again["rho"].sum(axis=1) <= 4 * n)
 
 
+@pytest.mark.parametrize("precision", [abi.JMM_PREC_EXACT, abi.JMM_PREC_FAST])
+def test_batch_checkpoint_resumes_exactly(gpu, tmp_path, precision):
+    """A batch saved mid-run (after its step sizes were adjusted on the
+    device) and restored continues bit for bit like the original."""
+    rng = np.random.default_rng(17)
+    chains = _mixed_chains(rng, 20, 40, 200)
+    cfg = abi.make_batch_config(seed=12, precision=precision, lanes_per_chain=4,
+                                steps_per_round=8, resum_sweeps=3)
+    a = ChainBatch(cfg, chains)
+    a.run(7)
+    a.adjust_steps()
+    a.run(5)
+    path = tmp_path / "batch.npz"
+    a.checkpoint(path)
+    a.run(9)
+    b = ChainBatch.restore(path)
+    b.run(9)
+    _assert_same(a, b, chains)
+    np.testing.assert_array_equal(np.array(a.step_sizes()), np.array(b.step_sizes()))
+    from jmmonedmc_gb300._native import JmmError
+    bad = b.results()
+    bad["l"][3] = 0.5  # positions would lie beyond the walls
+    with pytest.raises(JmmError):
+        b.set_results(bad)
+
+
 def _swendsen(step, actual, ideal=0.5):
     """maxDisAdjust's rescale (src/jmmMCState.cpp:2100-2116)."""
     return step * np.log(0.672924 * ideal + 0.0644284) / np.log(0.672924 * (actual + 0.0644284))
