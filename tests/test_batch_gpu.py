@@ -66,6 +66,9 @@ EXACT_CASES = {
                                 pots=(abi.JMM_POT_LJCUT, abi.JMM_POT_SOFTSPHERE, abi.JMM_POT_GAUSS)),
     "nvt_gauss_dense": dict(cfg=dict(resum_sweeps=2), n=(64, 128), ens=abi.JMM_NLT,
                             pots=(abi.JMM_POT_GAUSS,)),
+    # the smallest chains: windows reach past both ends at every step
+    "tiny_walls": dict(cfg=dict(resum_sweeps=5), n=(2, 8), ens=None,
+                       pots=(abi.JMM_POT_LJCUT, abi.JMM_POT_SOFTSPHERE, abi.JMM_POT_GAUSS)),
 }
 
 
