@@ -622,7 +622,8 @@ def run_grad(args, rank, world, local_rank):
     fp32_peak, rcp_peak = C.c_double(), C.c_double()
     _native.call("jmm_measure_peaks", C.byref(fp32_peak), C.byref(rcp_peak))
     b = ChainBatch(cfg, chains)
-    lanes, spr, cpb = (0, 0, 0) if args.no_autotune else b.autotune(trial_sweeps=3)
+    # trials of a few milliseconds each: the shapes' differences are a few per cent
+    lanes, spr, cpb = (0, 0, 0) if args.no_autotune else b.autotune(trial_sweeps=20)
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
