@@ -88,6 +88,7 @@ struct Ctl {
   double dl, lnew, lrat1;
   double ran, bf;
   double sum[9];
+  double part[2][9];  // qad2: the partner sums over i < nm and over i > nm
   int32_t wall, accept, kind, outcome, reset, pad;
 };
 
@@ -399,27 +400,35 @@ __device__ void qad2(const Args &a, Ctl &ctl, double *s_new, double *s_rij, cons
     }
   }
   __syncthreads();
-  if (threadIdx.x < 9) {
-    // the reference's order: (sum - old) + new, partners i < nm, then i > nm
-    const int k = threadIdx.x;
+  // the reference's order: (sum - old) + new over the partners i < nm (lanes
+  // 0-8 of warp 0) and, as a separate sum, over i > nm (lanes 0-8 of warp 1):
+  // two dependent FP64 chains, which overlap only in different warps
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane < 9 && warp < 2) {
+    const int k = lane;
     const double *nw = s_new + (uint64_t)k * nm1;
-    double sa = 0.0, sb = 0.0;
+    const uint64_t p0 = warp == 0 ? 0 : nm, p1 = warp == 0 ? nm : nm1;
+    double sp = 0.0;
     if (a.stage_old) {
       const double *old = s_old + (uint64_t)k * nm1;
 #pragma unroll 8
-      for (uint64_t p = 0; p < nm; ++p) sa = __dadd_rn(__dsub_rn(sa, old[p]), nw[p]);
-#pragma unroll 8
-      for (uint64_t p = nm; p < nm1; ++p) sb = __dadd_rn(__dsub_rn(sb, old[p]), nw[p]);
+      for (uint64_t p = p0; p < p1; ++p) sp = __dadd_rn(__dsub_rn(sp, old[p]), nw[p]);
     } else {
       const double *old = a.q + (uint64_t)k * a.nn;
+      if (warp == 0) {
 #pragma unroll 16
-      for (uint64_t p = 0; p < nm; ++p) sa = __dadd_rn(__dsub_rn(sa, old[p * n + nm]), nw[p]);
+        for (uint64_t p = p0; p < p1; ++p) sp = __dadd_rn(__dsub_rn(sp, old[p * n + nm]), nw[p]);
+      } else {
 #pragma unroll 16
-      for (uint64_t p = nm; p < nm1; ++p)
-        sb = __dadd_rn(__dsub_rn(sb, old[nm * n + p + 1]), nw[p]);
+        for (uint64_t p = p0; p < p1; ++p)
+          sp = __dadd_rn(__dsub_rn(sp, old[nm * n + p + 1]), nw[p]);
+      }
     }
-    ctl.sum[k] = __dadd_rn(sa, sb);
+    ctl.part[warp][k] = sp;
   }
+  __syncthreads();
+  if (threadIdx.x < 9)
+    ctl.sum[threadIdx.x] = __dadd_rn(ctl.part[0][threadIdx.x], ctl.part[1][threadIdx.x]);
   __syncthreads();
   if (threadIdx.x == 0) {
     const double de = ctl.sum[JMM_Q_E];
