@@ -253,6 +253,22 @@ __device__ void update_thermo(Scalars *S, uint64_t n) {
   acc[11] = __dadd_rn(acc[11], __dmul_rn(hv, hv));
 }
 
+// Accumulator k < 12 of update_thermo, for lane k: the same add of the same
+// term, with the term written as x * y (y = 1 for the plain sums, and x * 1 is
+// exact), so that the twelve adds are one FP64 instruction and no branch.
+__device__ __forceinline__ void update_thermo_lane(Scalars *S, uint64_t n, int k) {
+  const double l = S->l, e = S->tot[JMM_Q_E], vir = S->tot[JMM_Q_VIR], hv = S->tot[JMM_Q_HV];
+  const double rho = __ddiv_rn((double)n, l);
+  const double x = k < 2 ? rho : k < 4 ? l : k < 6 ? e : k == 6 ? l : k < 9 ? vir : k == 9 ? e : hv;
+  const double y = k == 1                 ? rho
+                   : k == 3               ? l
+                   : (k == 5 || k == 6)   ? e
+                   : (k == 8 || k == 9)   ? vir
+                   : k == 11              ? hv
+                                          : 1.0;
+  S->thermo[k] = __dadd_rn(S->thermo[k], __dmul_rn(x, y));
+}
+
 // ---- rho(x) and g(x) histograms ---------------------------------------------
 
 // Bin indices as the reference forms them: (long) floor(x/w + nb/2.0).
@@ -441,8 +457,6 @@ __device__ void qad2(const Args &a, Ctl &ctl, double *s_new, double *s_rij, cons
     const bool acc = (de <= 0) || (S->bf > S->ran);
     if (acc) {
       S->d_acc[0] += 1;
-#pragma unroll
-      for (int k = 0; k < 9; ++k) S->tot[k] = __dadd_rn(S->tot[k], ctl.sum[k]);
       a.r[nm] = ctl.rt;
       ctl.outcome = JMM_OUT_ACCEPT;
     } else {
@@ -453,6 +467,9 @@ __device__ void qad2(const Args &a, Ctl &ctl, double *s_new, double *s_rij, cons
   }
   __syncthreads();
   if (ctl.accept) {
+    // E += dE and the other eight totals, one per lane (one FP64 add each).
+    if (threadIdx.x < 9)
+      S->tot[threadIdx.x] = __dadd_rn(S->tot[threadIdx.x], ctl.sum[threadIdx.x]);
     for (uint64_t p = threadIdx.x; p < nm1; p += blockDim.x) {
       const uint64_t i = p < nm ? p : p + 1;
       const uint64_t ind = i < nm ? i * n + nm : nm * n + i;
@@ -687,8 +704,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();
     if (a.eci && (S->sn % a.eci) == 0) echeck(a, ctl);
+    if (threadIdx.x < 12) update_thermo_lane(S, a.n, threadIdx.x);
     if (threadIdx.x == 0) {
-      update_thermo(S, a.n);
       if (log) {
         jmm_step_record rec;
         rec.sn = S->sn;
