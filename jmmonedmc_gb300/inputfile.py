@@ -25,9 +25,18 @@ POTENTIALS = {"LJcut": abi.JMM_POT_LJCUT, "LJ": abi.JMM_POT_LJ,
               "HARMONIC": abi.JMM_POT_HARMONIC}
 
 
+_HEX = re.compile(r"\s*([-+]?)0[xX]([0-9a-fA-F]+\.?[0-9a-fA-F]*|\.[0-9a-fA-F]+)([pP][-+]?\d+)?")
+_DEC = re.compile(r"\s*[-+]?(\d+\.?\d*([eE][-+]?\d+)?|\.\d+([eE][-+]?\d+)?|inf(inity)?|nan)",
+                  re.IGNORECASE)
+
+
 def _strtod(tok):
-    m = re.match(r"\s*[-+]?(\d+\.?\d*([eE][-+]?\d+)?|\.\d+([eE][-+]?\d+)?|inf(inity)?|nan)",
-                 tok, re.IGNORECASE)
+    """C strtod on the longest valid prefix: decimal, hexadecimal (0x, with an
+    optional binary exponent), inf/infinity, nan; 0.0 when none."""
+    m = _HEX.match(tok)
+    if m:
+        return float.fromhex(m.group(1) + "0x" + m.group(2) + (m.group(3) or ""))
+    m = _DEC.match(tok)
     return float(m.group(0)) if m else 0.0
 
 
