@@ -378,6 +378,10 @@ static int validate(const jmm_batch_config *cfg, const jmm_chain_desc *chains, u
       return fail(JMM_ERR_INVALID, "chain %u: unknown ensemble", k);
     if (!(c.t > 0) || !(c.l0 > 0) || !(c.sigma > 0) || !(c.cutoff > 0) || !(c.max_step > 0))
       return fail(JMM_ERR_INVALID, "chain %u: T, L, sigma, cut-off and step must be positive", k);
+    if (!std::isfinite(c.t) || !std::isfinite(c.l0) || !std::isfinite(c.sigma) ||
+        !std::isfinite(c.cutoff) || !std::isfinite(c.max_step) || !std::isfinite(c.eps) ||
+        !std::isfinite(c.p) || !std::isfinite(c.vol_step) || !(c.vol_step >= 0))
+      return fail(JMM_ERR_INVALID, "chain %u: parameters must be finite (volume step >= 0)", k);
     if (cfg->boundary == JMM_BOUNDARY_PERIODIC && !(c.l0 > 2 * c.cutoff))
       return fail(JMM_ERR_INVALID, "chain %u: a periodic ring needs L > 2 cut-off", k);
     const double spacing = c.l0 / c.n;

@@ -676,6 +676,9 @@ static int large_create(const jmm_batch_config *cfg, const jmm_chain_desc *chain
     if (!(c.t > 0) || !(c.l0 > 0) || !(c.sigma > 0) || !(c.cutoff > 0) || !(c.max_step > 0))
       return fail(JMM_ERR_INVALID,
                   "jmm_large_create: chain %u: T, L, sigma, cut-off and step must be positive", k);
+    if (!isfinite(c.t) || !isfinite(c.l0) || !isfinite(c.sigma) || !isfinite(c.cutoff) ||
+        !isfinite(c.max_step) || !isfinite(c.eps))
+      return fail(JMM_ERR_INVALID, "jmm_large_create: chain %u: parameters must be finite", k);
   }
   if (!jmm_device_available()) return fail(JMM_ERR_CUDA, "jmm_large_create: no CUDA device");
   jmm_large *h = new (std::nothrow) jmm_large();

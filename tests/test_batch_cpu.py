@@ -48,3 +48,17 @@ def test_unsupported_window(native):
     # a window of 8 exists only for 2x16, 4x8 and 8x4
     _expect_invalid(abi.make_batch_config(seed=1, lanes_per_chain=4, steps_per_round=4, window=8), c)
     _expect_invalid(abi.make_batch_config(seed=1, lanes_per_chain=4, steps_per_round=8, window=6), c)
+
+
+@pytest.mark.parametrize("field, value", [
+    ("cutoff", float("inf")), ("l0", float("inf")), ("t", float("inf")),
+    ("sigma", float("nan")), ("eps", float("nan")), ("eps", float("inf")),
+    ("p", float("nan")), ("vol_step", float("nan")), ("vol_step", -0.01),
+    ("max_step", float("inf")), ("cutoff", 0.0), ("t", -1.0),
+])
+def test_chain_parameters_must_be_finite(native, field, value):
+    """Non-finite chain parameters (an infinite cut-off would make every
+    neighbour a partner) and a negative volume step are refused on the host."""
+    c = abi.make_chain(64, rho=0.5, ensemble=abi.JMM_NPT)
+    setattr(c, field, value)
+    _expect_invalid(abi.make_batch_config(seed=1), [abi.make_chain(32, rho=0.5), c])

@@ -31,3 +31,13 @@ def test_unsupported_chains(native):
     _expect_invalid(abi.make_batch_config(seed=1, boundary=abi.JMM_BOUNDARY_PERIODIC),
                     [_chain()], 256)
     _expect_invalid(abi.make_batch_config(seed=1, precision=abi.JMM_PREC_EXACT), [_chain()], 256)
+
+
+@pytest.mark.parametrize("field, value", [
+    ("cutoff", float("inf")), ("l0", float("inf")), ("t", float("inf")),
+    ("eps", float("nan")), ("sigma", float("inf")), ("max_step", float("inf")),
+])
+def test_chain_parameters_must_be_finite(native, field, value):
+    c = _chain()
+    setattr(c, field, value)
+    _expect_invalid(abi.make_batch_config(seed=1), [_chain(), c], 256)
