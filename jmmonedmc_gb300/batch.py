@@ -71,6 +71,7 @@ class ChainBatch:
         self._arr = chain_array(chains)
         self.chains = self._arr
         self._h = C.c_void_p()
+        self._hist = None
         if x is None:
             _native.call("jmm_batch_create", C.byref(config), self._arr, len(self._arr),
                          C.byref(self._h))
@@ -238,6 +239,8 @@ class ChainBatch:
 
     def take_histograms(self):
         """{"samples": (chains,), "rho": (chains, rhonb), "g": (chains, gns, gnb)}."""
+        if self._hist is None:
+            raise RuntimeError("take_histograms: histograms() has not configured this batch")
         rhonb, gns, gnb = self._hist
         width = 1 + rhonb + gns * gnb
         out = np.empty(self.n_chains * width, dtype=np.uint64)

@@ -62,3 +62,10 @@ def test_chain_parameters_must_be_finite(native, field, value):
     c = abi.make_chain(64, rho=0.5, ensemble=abi.JMM_NPT)
     setattr(c, field, value)
     _expect_invalid(abi.make_batch_config(seed=1), [abi.make_chain(32, rho=0.5), c])
+
+
+def test_take_histograms_needs_configuration():
+    b = ChainBatch.__new__(ChainBatch)  # no device handle: the check comes first
+    b._h, b._hist, b.chains = None, None, []
+    with pytest.raises(RuntimeError, match="histograms"):
+        b.take_histograms()
