@@ -276,6 +276,8 @@ def run_host(config, chains, n_sweeps, x_in=None):
     xin_ptr = None
     if x_in is not None:
         x_in = np.ascontiguousarray(x_in, dtype=np.float32)
+        if x_in.size != n_tot:
+            raise ValueError(f"x_in holds {x_in.size} positions, the chains {n_tot}")
         xin_ptr = x_in.ctypes.data_as(P(C.c_float))
     _native.call("jmm_batch_run_host", C.byref(config), arr, len(chains), xin_ptr, n_sweeps,
                  res, x_out.ctypes.data_as(P(C.c_float)))

@@ -108,9 +108,13 @@ def run_host(config, chains, n_sweeps, domain_size=256, mode="domains", x_in=Non
     n_tot = sum(int(c.n) for c in chains)
     if x_in is not None:
         x_in = np.ascontiguousarray(x_in, dtype=np.float64)
-        assert x_in.size == n_tot
+        if x_in.size != n_tot:
+            raise ValueError(f"x_in holds {x_in.size} positions, the chains {n_tot}")
     if x_out is None:
         x_out = np.empty(n_tot, dtype=np.float64)
+    elif not (isinstance(x_out, np.ndarray) and x_out.dtype == np.float64 and x_out.size == n_tot
+              and x_out.flags.c_contiguous and x_out.flags.writeable):
+        raise ValueError(f"x_out must be a writeable C-contiguous float64 array of {n_tot}")
     res = (abi.LargeResult * len(chains))()
     _native.call("jmm_large_run_host", C.byref(config), arr, len(chains), int(domain_size),
                  MODES[mode], x_in.ctypes.data_as(P(C.c_double)) if x_in is not None else None,

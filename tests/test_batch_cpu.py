@@ -69,3 +69,10 @@ def test_take_histograms_needs_configuration():
     b._h, b._hist, b.chains = None, None, []
     with pytest.raises(RuntimeError, match="histograms"):
         b.take_histograms()
+
+
+def test_run_host_checks_positions_size():
+    from jmmonedmc_gb300.batch import run_host
+    chains = [abi.make_chain(16, rho=0.5), abi.make_chain(24, rho=0.5)]
+    with pytest.raises(ValueError, match="x_in"):
+        run_host(abi.make_batch_config(seed=1), chains, 1, x_in=np.zeros(39, dtype=np.float32))

@@ -41,3 +41,16 @@ def test_chain_parameters_must_be_finite(native, field, value):
     c = _chain()
     setattr(c, field, value)
     _expect_invalid(abi.make_batch_config(seed=1), [_chain(), c], 256)
+
+
+def test_run_host_checks_host_buffers():
+    """Host buffers of the wrong size or type are refused before any native call."""
+    import numpy as np
+    from jmmonedmc_gb300.large import run_host
+    cfg = abi.make_batch_config(seed=1)
+    chains = [_chain(), _chain()]
+    with pytest.raises(ValueError, match="x_in"):
+        run_host(cfg, chains, 1, domain_size=256, x_in=np.zeros(100))
+    for bad in (np.zeros(8191), np.zeros(8192, dtype=np.float32), np.zeros(16384)[::2]):
+        with pytest.raises(ValueError, match="x_out"):
+            run_host(cfg, chains, 1, domain_size=256, x_out=bad)
