@@ -68,8 +68,22 @@ class Layout:
         return torch.as_tensor(raw, device=device)
 
 
+def _check(layout, x, l, eps, sigma):
+    """The kernel reads x and the table on the device with no sizes of its
+    own, so shapes and the device are checked here, before any launch."""
+    n_pos = sum(layout.sizes)
+    if x.numel() != n_pos:
+        raise ValueError(f"x holds {x.numel()} positions, the layout {n_pos}")
+    for name, t in (("l", l), ("eps", eps), ("sigma", sigma)):
+        if t.numel() != layout.n_chains:
+            raise ValueError(f"{name} needs one value per chain ({layout.n_chains})")
+    if not x.is_cuda:
+        raise ValueError("x must be a CUDA tensor: the gradient kernel reads it on the device")
+
+
 def _launch(layout, x, l, eps, sigma, want_forces):
     import torch
+    _check(layout, x, l, eps, sigma)
     dev = x.device
     table = layout.table(l, eps, sigma, dev)
     out = torch.empty((layout.n_chains, 4), dtype=torch.float64, device=dev)

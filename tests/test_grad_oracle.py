@@ -44,3 +44,19 @@ def test_fp64_gradient_matches_central_differences(pot, cutoff, periodic):
             assert abs(got - want) <= 1e-6 * max(1.0, abs(want)), (got, want)
         checked += 1
     assert checked >= 5
+
+
+def test_launch_checks_shapes_and_device():
+    """Wrong sizes and host tensors are refused before any launch."""
+    import torch
+    from jmmonedmc_gb300.grad import Layout, chain_energy, energy_and_gradients
+    lay = Layout([4, 6])
+    ones = torch.ones(2, dtype=torch.float64)
+    with pytest.raises(ValueError, match="positions"):
+        energy_and_gradients(torch.zeros(9), ones, ones, ones, lay)
+    with pytest.raises(ValueError, match="eps"):
+        energy_and_gradients(torch.zeros(10), ones, torch.ones(3), ones, lay)
+    with pytest.raises(ValueError, match="CUDA"):
+        energy_and_gradients(torch.zeros(10), ones, ones, ones, lay)
+    with pytest.raises(ValueError, match="CUDA"):
+        chain_energy(torch.zeros(10, requires_grad=True), ones, ones, ones, lay)
