@@ -373,7 +373,10 @@ typedef struct jmm_grad_stats {
  * configuration, as out[4k .. 4k+3] (FP64), with FP32 pair terms and FP64
  * sums; forces: NULL, or -dU/dx per particle at the chains' offsets.
  * chains, x, out and forces are device pointers; enqueued on stream (a
- * cudaStream_t as void*, NULL = the default stream), no wait. */
+ * cudaStream_t as void*, NULL = the default stream), no wait.  The call
+ * cannot see their sizes: the caller guarantees n_chains records in chains,
+ * x_off + n positions of x for every record (forces likewise) and 4 n_chains
+ * doubles of out. */
 int jmm_energy_grad(const jmm_grad_chain *chains, uint32_t n_chains, const float *x,
                     int32_t boundary, double *out, float *forces, void *stream);
 /* The same for a batch's current configurations, into host memory. */
