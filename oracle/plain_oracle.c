@@ -23,7 +23,8 @@
  *
  * Every FP64 expression keeps the reference's operand order; the file is
  * compiled with -ffp-contract=off so no multiply-add is fused.
- * Pair (i, j), i < j, lives at index i*N + j of the dense pair arrays.
+ * Pair (i, j), i < j, lives at the reference's packed index
+ * i(N-1) - i(i+1)/2 + j - 1 (pidx) of the pair arrays.
  */
 #include "jmm_oracle.h"
 
@@ -50,10 +51,10 @@ struct jmmo_plain {
   double echeck_e, echeck_e_before;
   double *r;
   double *r_trial;
-  double *rij;          /* N*N, stored separations                 */
-  double *q;            /* 9*N*N stored pair quantities            */
-  double *rij_trial;    /* N*N                                      */
-  double *q_trial;      /* 9*N*N                                    */
+  double *rij;          /* N(N-1)/2 packed, stored separations     */
+  double *q;            /* 9 x N(N-1)/2 stored pair quantities     */
+  double *rij_trial;    /* N(N-1)/2                                 */
+  double *q_trial;      /* 9 x N(N-1)/2                             */
   /* rho(x) and g(x) histograms: current counts (rhol, gl) and their sums
    * since the last take (rhoA, gA), int as in the reference, g slice-major */
   int hist_on;
@@ -117,6 +118,13 @@ static void phi_eval(const jmmo_plain *h, double d, int virial, double l, double
     phi_lj(d, h->prm.potential == JMM_POT_LJ ? INFINITY : h->prm.cutoff, virial, phi);
 }
 
+/* Index of pair (i < j) in the packed row-major triangle, the reference's
+ * ind(i, j) = i(N-1) - i(i+1)/2 + j - 1 (src/jmmMCState.cpp:142-148): the
+ * pair state takes N(N-1)/2 entries per quantity, as in the reference. */
+static inline uint64_t pidx(uint64_t n, uint64_t i, uint64_t j) {
+  return i * (n - 1) - i * (i + 1) / 2 + j - 1;
+}
+
 /* Pairs beyond the neighbour-number limit carry zeros (jmmMCState.cpp:1217). */
 static int pair_cut(const jmmo_plain *h, uint64_t i, uint64_t j) {
   return h->prm.nbn >= 0 && (j - i) > (uint64_t)h->prm.nbn;
@@ -152,7 +160,7 @@ static double draw_uniform(jmmo_plain *h) {
 static void rebuild_separations(jmmo_plain *h) {
   uint64_t n = h->n;
   for (uint64_t i = 0; i < n; ++i)
-    for (uint64_t j = i + 1; j < n; ++j) h->rij[i * n + j] = h->r[j] - h->r[i];
+    for (uint64_t j = i + 1; j < n; ++j) h->rij[pidx(n, i, j)] = h->r[j] - h->r[i];
 }
 
 jmmo_plain *jmmo_plain_create(const jmm_params *prm) {
@@ -171,10 +179,10 @@ jmmo_plain *jmmo_plain_create(const jmm_params *prm) {
   h->rng_slot = 4;
   h->r = (double *)calloc(n, sizeof(double));
   h->r_trial = (double *)calloc(n, sizeof(double));
-  h->rij = (double *)calloc(n * n, sizeof(double));
-  h->rij_trial = (double *)calloc(n * n, sizeof(double));
-  h->q = (double *)calloc(9 * n * n, sizeof(double));
-  h->q_trial = (double *)calloc(9 * n * n, sizeof(double));
+  h->rij = (double *)calloc(n * (n - 1) / 2, sizeof(double));
+  h->rij_trial = (double *)calloc(n * (n - 1) / 2, sizeof(double));
+  h->q = (double *)calloc(9 * (n * (n - 1) / 2), sizeof(double));
+  h->q_trial = (double *)calloc(9 * (n * (n - 1) / 2), sizeof(double));
   if (!h->r || !h->r_trial || !h->rij || !h->rij_trial || !h->q || !h->q_trial) {
     jmmo_plain_destroy(h);
     return NULL;
@@ -252,7 +260,7 @@ static void fgrho(jmmo_plain *h) {
     for (uint64_t j = i + 1; j < n; ++j) {
       long gs1 = slice_of(h, h->r[i]);
       long gs2 = slice_of(h, h->r[j]);
-      long gb = (long)floor(h->rij[i * n + j] / h->gbw);
+      long gb = (long)floor(h->rij[pidx(n, i, j)] / h->gbw);
       if (gb >= 0 && gb < (long)h->gnb) {
         if (gs1 >= 0 && gs1 < h->gns) h->gl[gs1 * h->gnb + gb]++;
         if (gs2 >= 0 && gs2 < h->gns) h->gl[gs2 * h->gnb + gb]++;
@@ -343,7 +351,7 @@ int jmmo_plain_hist_counts(jmmo_plain *h, int32_t *rho, uint64_t rhonb, int32_t 
 /* ---- moves -------------------------------------------------------------- */
 
 static void commit_pair(jmmo_plain *h, uint64_t ind) {
-  uint64_t nn = h->n * h->n;
+  uint64_t nn = h->n * (h->n - 1) / 2;
   h->rij[ind] = h->rij_trial[ind];
   for (int k = 0; k < 9; ++k) h->q[k * nn + ind] = h->q_trial[k * nn + ind];
 }
@@ -351,7 +359,7 @@ static void commit_pair(jmmo_plain *h, uint64_t ind) {
 /* fad, src/jmmMCState.cpp:853-1003 */
 int jmmo_plain_fad(jmmo_plain *h, uint64_t nm, double d) {
   if (!h || nm >= h->n) return JMM_ERR_INVALID;
-  uint64_t n = h->n, nn = n * n;
+  uint64_t n = h->n, nn = n * (n - 1) / 2;
   double rn = d;
   memcpy(h->r_trial, h->r, n * sizeof(double));
   double md = (rn - 0.5) * 2 * h->max_step;
@@ -364,7 +372,7 @@ int jmmo_plain_fad(jmmo_plain *h, uint64_t nm, double d) {
   double phi[9];
   for (uint64_t i = 0; i < n; ++i) {
     for (uint64_t j = i + 1; j < n; ++j) {
-      uint64_t ind = i * n + j;
+      uint64_t ind = pidx(n, i, j);
       h->rij_trial[ind] = h->r_trial[j] - h->r_trial[i];
       if (pair_cut(h, i, j)) {
         for (int k = 0; k < 9; ++k) h->q_trial[k * nn + ind] = 0;
@@ -386,7 +394,7 @@ int jmmo_plain_fad(jmmo_plain *h, uint64_t nm, double d) {
     for (int k = 0; k < 9; ++k) h->tot[k] = sum[k];
     h->r[nm] = h->r_trial[nm];
     for (uint64_t i = 0; i < n; ++i)
-      for (uint64_t j = i + 1; j < n; ++j) commit_pair(h, i * n + j);
+      for (uint64_t j = i + 1; j < n; ++j) commit_pair(h, pidx(n, i, j));
   } else {
     h->d_acc[1]++;
   }
@@ -413,7 +421,7 @@ static void set_record(jmm_step_record *rec, const jmmo_plain *h, uint64_t nm, d
  * :1453 in qad2 below) */
 static int qad2_move(jmmo_plain *h, uint64_t nm, double rn, const jmm_draw *rp,
                      double *ran_out, double *bf_out) {
-  uint64_t n = h->n, nn = n * n;
+  uint64_t n = h->n, nn = n * (n - 1) / 2;
   double md = (rn - 0.5) * 2 * h->max_step;
   h->r_trial[nm] = h->r[nm] + md;
   if (fabs(h->r_trial[nm]) > h->l / 2.0) {
@@ -424,7 +432,7 @@ static int qad2_move(jmmo_plain *h, uint64_t nm, double rn, const jmm_draw *rp,
   double da[9] = {0}, db[9] = {0}, dsum[9];
   /* loop A: partners i < nm, separation r[nm] - r[i] grows by md */
   for (uint64_t i = 0; i < nm; ++i) {
-    uint64_t ind = i * n + nm;
+    uint64_t ind = pidx(n, i, nm);
     h->rij_trial[ind] = h->rij[ind] + md;
     if (pair_cut(h, i, nm)) {
       for (int k = 0; k < 9; ++k) h->q_trial[k * nn + ind] = 0;
@@ -437,7 +445,7 @@ static int qad2_move(jmmo_plain *h, uint64_t nm, double rn, const jmm_draw *rp,
   }
   /* loop B: partners i > nm, separation r[i] - r[nm] shrinks by md */
   for (uint64_t i = nm + 1; i < n; ++i) {
-    uint64_t ind = nm * n + i;
+    uint64_t ind = pidx(n, nm, i);
     h->rij_trial[ind] = h->rij[ind] - md;
     if (pair_cut(h, nm, i)) {
       for (int k = 0; k < 9; ++k) h->q_trial[k * nn + ind] = 0;
@@ -460,8 +468,8 @@ static int qad2_move(jmmo_plain *h, uint64_t nm, double rn, const jmm_draw *rp,
     h->d_acc[0]++;
     for (int k = 0; k < 9; ++k) h->tot[k] += dsum[k];
     h->r[nm] = h->r_trial[nm];
-    for (uint64_t i = 0; i < nm; ++i) commit_pair(h, i * n + nm);
-    for (uint64_t i = nm + 1; i < n; ++i) commit_pair(h, nm * n + i);
+    for (uint64_t i = 0; i < nm; ++i) commit_pair(h, pidx(n, i, nm));
+    for (uint64_t i = nm + 1; i < n; ++i) commit_pair(h, pidx(n, nm, i));
     if (h->hist_on) qagrho(h, nm, md);
     return JMM_OUT_ACCEPT;
   }
@@ -481,7 +489,7 @@ static int qad2(jmmo_plain *h, uint64_t nm, double rn, const jmm_draw *rp,
 /* fav, src/jmmMCState.cpp:2161-2293 */
 static int fav(jmmo_plain *h, double rn, const jmm_draw *rp, double *ran_out,
                double *bf_out) {
-  uint64_t n = h->n, nn = n * n;
+  uint64_t n = h->n, nn = n * (n - 1) / 2;
   double dl = (rn - 0.5) * 2 * h->max_dl;
   double lnew = h->l + dl;
   double lrat1 = lnew / h->l;
@@ -490,7 +498,7 @@ static int fav(jmmo_plain *h, double rn, const jmm_draw *rp, double *ran_out,
   double phi[9];
   for (uint64_t i = 0; i < n; ++i) {
     for (uint64_t j = i + 1; j < n; ++j) {
-      uint64_t ind = i * n + j;
+      uint64_t ind = pidx(n, i, j);
       if (pair_cut(h, i, j)) {
         for (int k = 0; k < 9; ++k) h->q_trial[k * nn + ind] = 0;
       } else {
@@ -517,7 +525,7 @@ static int fav(jmmo_plain *h, double rn, const jmm_draw *rp, double *ran_out,
     memcpy(h->r, h->r_trial, n * sizeof(double));
     for (uint64_t i = 0; i < n; ++i) {
       for (uint64_t j = i + 1; j < n; ++j) {
-        uint64_t ind = i * n + j;
+        uint64_t ind = pidx(n, i, j);
         h->rij[ind] = h->r[j] - h->r[i];
         for (int k = 0; k < 9; ++k) h->q[k * nn + ind] = h->q_trial[k * nn + ind];
       }
@@ -534,7 +542,7 @@ static int fav(jmmo_plain *h, double rn, const jmm_draw *rp, double *ran_out,
  * volume move, so nothing here is pinned to it. */
 static int qav_lj(jmmo_plain *h, double rn, const jmm_draw *rp, double *ran_out,
                   double *bf_out) {
-  uint64_t n = h->n, nn = n * n;
+  uint64_t n = h->n, nn = n * (n - 1) / 2;
   double dl = (rn - 0.5) * 2 * h->max_dl;
   double lrat1 = (h->l + dl) / h->l;
   double lrat3 = lrat1 * lrat1 * lrat1;
@@ -564,7 +572,7 @@ static int qav_lj(jmmo_plain *h, double rn, const jmm_draw *rp, double *ran_out,
     double phi[9];
     for (uint64_t i = 0; i < n; ++i) {
       for (uint64_t j = i + 1; j < n; ++j) {
-        uint64_t ind = i * n + j;
+        uint64_t ind = pidx(n, i, j);
         h->rij[ind] = lrat1 * h->rij[ind];
         phi_eval(h, h->rij[ind], 1, h->l, phi);
         for (int k = 0; k < 9; ++k) h->q[k * nn + ind] = phi[k];
@@ -583,7 +591,7 @@ static int qav_lj(jmmo_plain *h, double rn, const jmm_draw *rp, double *ran_out,
 
 /* ECheck, src/jmmMCState.cpp:1965-2095 */
 int jmmo_plain_echeck(jmmo_plain *h, double *e_test_out, int32_t *reset_out) {
-  uint64_t n = h->n, nn = n * n;
+  uint64_t n = h->n, nn = n * (n - 1) / 2;
   double phi[9];
   double etest = 0;
   for (uint64_t i = 0; i < n; ++i) {
@@ -602,7 +610,7 @@ int jmmo_plain_echeck(jmmo_plain *h, double *e_test_out, int32_t *reset_out) {
     double sum[9] = {0};
     for (uint64_t i = 0; i < n; ++i) {
       for (uint64_t j = i + 1; j < n; ++j) {
-        uint64_t ind = i * n + j;
+        uint64_t ind = pidx(n, i, j);
         if (pair_cut(h, i, j)) {
           for (int k = 0; k < 9; ++k) h->q[k * nn + ind] = 0;
         } else {
@@ -720,7 +728,7 @@ int jmmo_plain_get_separations(jmmo_plain *h, double *rij, uint64_t n_pairs) {
   if (n_pairs != n * (n - 1) / 2) return JMM_ERR_INVALID;
   uint64_t k = 0;
   for (uint64_t i = 0; i < n; ++i)
-    for (uint64_t j = i + 1; j < n; ++j) rij[k++] = h->rij[i * n + j];
+    for (uint64_t j = i + 1; j < n; ++j) rij[k++] = h->rij[pidx(n, i, j)];
   return JMM_OK;
 }
 
@@ -772,14 +780,14 @@ double jmmo_plain_trial_volume_energy(jmmo_plain *h, double dl) {
  * length l, every pair and total recomputed (separations of pairs beyond NBN
  * are left as they were). */
 int jmmo_plain_move_volume(jmmo_plain *h, double l) {
-  uint64_t n = h->n, nn = n * n;
+  uint64_t n = h->n, nn = n * (n - 1) / 2;
   double lrat1 = l / h->l;
   for (uint64_t i = 0; i < n; ++i) h->r[i] = h->r[i] * lrat1;
   h->l = l;
   double sum[9] = {0}, phi[9];
   for (uint64_t i = 0; i < n; ++i) {
     for (uint64_t j = i + 1; j < n; ++j) {
-      uint64_t ind = i * n + j;
+      uint64_t ind = pidx(n, i, j);
       if (pair_cut(h, i, j)) {
         for (int k = 0; k < 9; ++k) h->q[k * nn + ind] = 0;
         continue;
