@@ -20,6 +20,9 @@ int jmmo_plain_fad(jmmo_plain *h, uint64_t nm, double d);
 int jmmo_plain_steps(jmmo_plain *h, uint64_t n_steps, const jmm_draw *replay,
                      jmm_step_record *log);
 int jmmo_plain_move(jmmo_plain *h, int32_t kind, uint64_t nm, double rn, jmm_step_record *rec);
+/* The plain form's pair functions alone (phiLJcut / phiLJinfcutoff /
+ * phiHarmoniccut): phi[0..8] of separation d. */
+void jmmo_phi(int32_t potential, double d, double cut, int32_t virial, double l, double *phi);
 int jmmo_plain_update_thermo(jmmo_plain *h);
 int jmmo_plain_reset_thermo(jmmo_plain *h);
 int jmmo_plain_echeck(jmmo_plain *h, double *e_test, int32_t *reset);

@@ -118,6 +118,16 @@ static void phi_eval(const jmmo_plain *h, double d, int virial, double l, double
     phi_lj(d, h->prm.potential == JMM_POT_LJ ? INFINITY : h->prm.cutoff, virial, phi);
 }
 
+/* The pair functions alone, for their tests: potential and cut-off as in
+ * jmm_params, virial the params[0] > 0.1 test, l phiHarmoniccut's box. */
+void jmmo_phi(int32_t potential, double d, double cut, int32_t virial, double l, double *phi) {
+  jmmo_plain h;
+  memset(&h, 0, sizeof(h));
+  h.prm.potential = potential;
+  h.prm.cutoff = cut;
+  phi_eval(&h, d, virial, l, phi);
+}
+
 /* Index of pair (i < j) in the packed row-major triangle, the reference's
  * ind(i, j) = i(N-1) - i(i+1)/2 + j - 1 (src/jmmMCState.cpp:142-148): the
  * pair state takes N(N-1)/2 entries per quantity, as in the reference. */

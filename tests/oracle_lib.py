@@ -38,6 +38,7 @@ SIGS = {
     "jmmo_plain_hist_counts": ([vp, P(i32), u64, P(i32), u64], C.c_int),
     "jmmo_plain_trial_volume_energy": ([vp, dbl], dbl),
     "jmmo_plain_move_volume": ([vp, dbl], C.c_int),
+    "jmmo_phi": ([i32, dbl, dbl, i32, dbl, P(dbl)], None),
     "jmmo_plain_relax_volume": ([vp, vp, P(i32)], C.c_int),
     "jmmo_philox_raw": ([P(u32), P(u32), P(u32)], None),
     "jmmo_step_words_export": ([u64, u64, u32, P(u32)], None),
@@ -314,4 +315,12 @@ def energy_grad64(chain_desc, x, l, periodic=False):
     out = (dbl * 4)()
     lib.jmmo_energy_grad64(C.byref(chain_desc), x.ctypes.data_as(P(dbl)), float(l),
                            1 if periodic else 0, out)
+    return np.array(out)
+
+
+def phi(potential, d, cut, virial=True, l=1.0):
+    """The plain form's pair function: phi[0..8] at separation d."""
+    lib = load()
+    out = (dbl * 9)()
+    lib.jmmo_phi(potential, float(d), float(cut), 1 if virial else 0, float(l), out)
     return np.array(out)
