@@ -138,3 +138,16 @@ def test_strtod_prefixes():
     assert s("0x40") == 64.0 and s("0x1.8p3") == 12.0 and s("-0x.8") == -0.5
     assert s("0x") == 0.0 and s("1e") == 1.0 and s("abc") == 0.0
     assert math.isinf(s("inf")) and math.isinf(s("-Infinity")) and math.isnan(s("nan"))
+
+
+@pytest.mark.parametrize("drop, ensemble", [("N", "NPT"), ("SEED", "NPT"), ("P", "NPT"),
+                                            ("MAXDV", "NPT"), ("L", "NLT"), ("POT", "NLT")])
+def test_to_params_refuses_missing_keywords(drop, ensemble):
+    """A keyword the move loop needs but the file omits is refused: the
+    reference would read it from an uninitialised field."""
+    lines = {"ENSEMBLE": ensemble, "N": "64", "P": "1.0", "L": "100.0", "T": "1.0",
+             "POT": "LJcut 3.0", "NBN": "-1", "MAXSTEP": "0.3", "MAXDV": "0.5", "SEED": "1"}
+    del lines[drop]
+    kw = inputfile.parse_text("".join(f"{k} {v}\n" for k, v in lines.items()))
+    with pytest.raises(ValueError, match=drop):
+        inputfile.to_params(kw)
