@@ -224,11 +224,12 @@ def _run_bench(argv, env_extra=None, timeout=300):
                           capture_output=True, text=True, timeout=timeout, env=env, cwd=REPO)
 
 
-def test_reference_arm_prints_one_json_line():
+@pytest.mark.parametrize("workload", ["npt", "uneven", "grad", "large"])
+def test_reference_arm_prints_one_json_line(workload):
     """--impl reference: the reference's algorithm on the host cores for the
     same chains, one JSON line with the contract's keys and e2e without copies."""
-    p = _run_bench(["--impl", "reference", "--steps", "1", "--warmup", "0",
-                    "--chains", "64", "--cpu-seconds", "0.4"])
+    p = _run_bench(["--impl", "reference", "--workload", workload, "--steps", "1",
+                    "--warmup", "0", "--cpu-seconds", "0.4"])
     assert p.returncode == 0, p.stderr[-2000:]
     lines = [ln for ln in p.stdout.splitlines() if ln.strip()]
     assert len(lines) == 1
