@@ -252,3 +252,14 @@ def test_reference_arm_other_ranks_exit_quietly():
     p = _run_bench(["--impl", "reference", "--steps", "1", "--warmup", "0"],
                    {"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}, timeout=120)
     assert p.returncode == 0 and p.stdout.strip() == ""
+
+
+def test_own_arm_without_a_gpu_fails_loudly():
+    """No CPU fallback: without a CUDA device the GPU arm exits non-zero and
+    prints no JSON line."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    p = _run_bench(["--steps", "1", "--warmup", "3", "--chains", "64"], timeout=120)
+    assert p.returncode != 0
+    assert not any(ln.strip().startswith("{") for ln in p.stdout.splitlines())
