@@ -151,3 +151,54 @@ def test_to_params_refuses_missing_keywords(drop, ensemble):
     kw = inputfile.parse_text("".join(f"{k} {v}\n" for k, v in lines.items()))
     with pytest.raises(ValueError, match=drop):
         inputfile.to_params(kw)
+
+
+def _random_value(rng, integer, signed):
+    """A value spelled as strtod reads it: decimal, exponent, hexadecimal,
+    leading dot, trailing text.  Integer fields get no negative, huge or
+    non-finite values (their conversion is undefined in the reference)."""
+    mag = float(rng.choice([0.5, 3.0, 64.0, 1000.0])) * float(rng.random())
+    if signed and rng.random() < 0.3:
+        mag = -mag
+    form = rng.integers(0, 5)
+    if form == 0:
+        return repr(round(mag, 6))
+    if form == 1:
+        return f"{mag:.3e}"
+    if form == 2:
+        return float(mag).hex() if not integer else hex(int(abs(mag)))
+    if form == 3:
+        return f"{mag:.4f}".replace("0.", ".", 1) if 0 <= mag < 1 else f"{mag:.2f}"
+    return f"{mag:.3f}xyz"
+
+
+def test_random_inputs_match_reference_readinput(dump, tmp_path):
+    rng = np.random.default_rng(2024)
+    keys_int = sorted(inputfile.KEYS_INT)
+    keys_float = sorted(inputfile.KEYS_FLOAT)
+    for trial in range(150):
+        lines = []
+        for _ in range(int(rng.integers(3, 14))):
+            r = rng.random()
+            if r < 0.4:
+                k = str(rng.choice(keys_int))
+                lines.append(f"{k} {_random_value(rng, True, k == 'NBN')}")
+            elif r < 0.75:
+                k = str(rng.choice(keys_float))
+                lines.append(f"{k}\t{_random_value(rng, False, True)}")
+            elif r < 0.82:
+                pot = str(rng.choice(["LJcut", "LJ", "HARMONIC", "Morse"]))
+                cut = f" {_random_value(rng, False, False)}" if rng.random() < 0.7 else ""
+                lines.append(f"POT {pot}{cut}")
+            elif r < 0.88:
+                lines.append(f"ENSEMBLE {rng.choice(['NPT', 'NLT', 'NVT'])}")
+            elif r < 0.94:
+                lines.append(f"RESTART {rng.choice(['TRUE', 'FALSE', 'false', 'False', 'no'])}")
+            elif r < 0.97:
+                lines.append("RELAX")
+            else:
+                lines.append(f"[{rng.choice(keys_int)}] [{int(rng.integers(1, 500))}]")
+        text = "\n".join(lines) + "\n"
+        assert all(len(line) < 99 for line in lines)
+        check_against_reference(inputfile.parse_text(text), reference_read(dump, tmp_path, text),
+                                text)
