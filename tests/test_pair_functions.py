@@ -67,3 +67,18 @@ def test_harmonic_matches_reference(reference_phi):
           float(np.nextafter(cut, np.inf)), 2.0]
     compare(reference_phi, [(abi.JMM_POT_HARMONIC, d, cut, 1, l) for d in ds
                             for l in (10.0, 106.66666666666667)])
+
+
+def test_random_separations_match_reference(reference_phi):
+    """3000 seeded separations, log-uniform over 0.3-30 with either sign,
+    random cut-offs, all three functions, bit for bit."""
+    rng = np.random.default_rng(11)
+    cases = []
+    for _ in range(3000):
+        d = float(np.exp(rng.uniform(np.log(0.3), np.log(30.0))))
+        d = -d if rng.random() < 0.3 else d
+        cut = float(rng.uniform(1.0, 5.0))
+        pot = int(rng.choice([abi.JMM_POT_LJCUT, abi.JMM_POT_LJ, abi.JMM_POT_HARMONIC]))
+        virial = 1 if pot == abi.JMM_POT_HARMONIC else int(rng.integers(0, 2))
+        cases.append((pot, d, cut, virial, float(rng.uniform(5.0, 500.0))))
+    compare(reference_phi, cases)
