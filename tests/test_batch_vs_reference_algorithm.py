@@ -6,10 +6,13 @@ order and finds partners in an index window; the plain restatement
 the reference build by tests/test_oracle_vs_reference.py).  For LJ particles
 that never pass each other, with linear volume moves drawn with probability
 1/(N+1) per step as the reference's Step does, both sample the same
-ensemble; so <E> and <L> of independent replicas must agree within their
+ensemble, and so do ln L volume moves closing every sweep (each move keeps
+detailed balance; the batched NPT workload uses them); so <E> and <L> of
+independent replicas must agree within their
 combined standard error (the replicas' spread carries each chain's
 autocorrelation).  The GPU's batched kernels are pinned to the batched
 restatement separately, so this links them to the reference's algorithm."""
+import functools
 import math
 
 import numpy as np
@@ -22,6 +25,7 @@ N, T, P, CUT, MAX_STEP = 32, 1.0, 1.0, 3.0, 0.3
 REPLICAS, EQUIL_SWEEPS, SWEEPS = 48, 300, 3000
 
 
+@functools.lru_cache(maxsize=None)
 def plain_replicas(ensemble, l0, max_dl):
     types = N + 1 if ensemble == abi.JMM_NPT else N
     e, l = [], []
@@ -39,12 +43,11 @@ def plain_replicas(ensemble, l0, max_dl):
     return np.array(e), np.array(l)
 
 
-def batch_replicas(ensemble, l0, max_dl):
+def batch_replicas(ensemble, l0, vol_step, vol_move, schedule):
     chains = [abi.make_chain(N, potential=abi.JMM_POT_LJCUT, ensemble=ensemble, cutoff=CUT,
-                             t=T, p=P, l0=l0, max_step=MAX_STEP, vol_step=max_dl)
+                             t=T, p=P, l0=l0, max_step=MAX_STEP, vol_step=vol_step)
               for _ in range(REPLICAS)]
-    cfg = abi.make_batch_config(seed=77, vol_move=abi.JMM_VOLMOVE_LINEAR,
-                                vol_schedule=abi.JMM_VOLSCHED_RANDOM,
+    cfg = abi.make_batch_config(seed=77, vol_move=vol_move, vol_schedule=schedule,
                                 precision=abi.JMM_PREC_EXACT, resum_sweeps=10)
     b = oracle_lib.OracleBatch(cfg, chains, fp64=True)
     b.run(EQUIL_SWEEPS)
@@ -61,12 +64,17 @@ def agree(a, b):
     return abs(a.mean() - b.mean()), sem
 
 
-@pytest.mark.parametrize("ensemble", [abi.JMM_NLT, abi.JMM_NPT])
-def test_batched_chain_samples_the_reference_ensemble(ensemble):
+@pytest.mark.parametrize("ensemble, vol_move, schedule, vol_step", [
+    (abi.JMM_NLT, abi.JMM_VOLMOVE_LINEAR, abi.JMM_VOLSCHED_RANDOM, 0.5),
+    # the reference's own volume move: linear dL, drawn with P = 1/(N+1)
+    (abi.JMM_NPT, abi.JMM_VOLMOVE_LINEAR, abi.JMM_VOLSCHED_RANDOM, 0.5),
+    # the batched NPT workload's: ln L steps of 0.01, one closing every sweep
+    (abi.JMM_NPT, abi.JMM_VOLMOVE_LNL, abi.JMM_VOLSCHED_SWEEP, 0.01),
+])
+def test_batched_chain_samples_the_reference_ensemble(ensemble, vol_move, schedule, vol_step):
     l0 = N / 0.6 if ensemble == abi.JMM_NLT else float(N)
-    max_dl = 0.5
-    pe, pl = plain_replicas(ensemble, l0, max_dl)
-    be, bl = batch_replicas(ensemble, l0, max_dl)
+    pe, pl = plain_replicas(ensemble, l0, 0.5)
+    be, bl = batch_replicas(ensemble, l0, vol_step, vol_move, schedule)
     d, sem = agree(pe, be)
     print(f"<E>: reference algorithm {pe.mean():.4f}, batched {be.mean():.4f}, "
           f"diff {d:.4f}, standard error {sem:.4f}")
