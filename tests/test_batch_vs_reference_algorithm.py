@@ -43,13 +43,13 @@ def plain_replicas(ensemble, l0, max_dl):
     return np.array(e), np.array(l)
 
 
-def batch_replicas(ensemble, l0, vol_step, vol_move, schedule):
+def batch_replicas(ensemble, l0, vol_step, vol_move, schedule, fp64):
     chains = [abi.make_chain(N, potential=abi.JMM_POT_LJCUT, ensemble=ensemble, cutoff=CUT,
                              t=T, p=P, l0=l0, max_step=MAX_STEP, vol_step=vol_step)
               for _ in range(REPLICAS)]
     cfg = abi.make_batch_config(seed=77, vol_move=vol_move, vol_schedule=schedule,
                                 precision=abi.JMM_PREC_EXACT, resum_sweeps=10)
-    b = oracle_lib.OracleBatch(cfg, chains, fp64=True)
+    b = oracle_lib.OracleBatch(cfg, chains, fp64=fp64)
     b.run(EQUIL_SWEEPS)
     r0 = b.results()
     b.run(SWEEPS)
@@ -64,6 +64,7 @@ def agree(a, b):
     return abs(a.mean() - b.mean()), sem
 
 
+@pytest.mark.parametrize("fp64", [True, False], ids=["fp64", "fp32_exact_kernel"])
 @pytest.mark.parametrize("ensemble, vol_move, schedule, vol_step", [
     (abi.JMM_NLT, abi.JMM_VOLMOVE_LINEAR, abi.JMM_VOLSCHED_RANDOM, 0.5),
     # the reference's own volume move: linear dL, drawn with P = 1/(N+1)
@@ -71,10 +72,13 @@ def agree(a, b):
     # the batched NPT workload's: ln L steps of 0.01, one closing every sweep
     (abi.JMM_NPT, abi.JMM_VOLMOVE_LNL, abi.JMM_VOLSCHED_SWEEP, 0.01),
 ])
-def test_batched_chain_samples_the_reference_ensemble(ensemble, vol_move, schedule, vol_step):
+def test_batched_chain_samples_the_reference_ensemble(ensemble, vol_move, schedule, vol_step,
+                                                      fp64):
+    """fp64: the batched FP64 restatement; fp32_exact_kernel: its FP32 mode,
+    which the EXACT GPU kernel equals bit for bit."""
     l0 = N / 0.6 if ensemble == abi.JMM_NLT else float(N)
     pe, pl = plain_replicas(ensemble, l0, 0.5)
-    be, bl = batch_replicas(ensemble, l0, vol_step, vol_move, schedule)
+    be, bl = batch_replicas(ensemble, l0, vol_step, vol_move, schedule, fp64)
     d, sem = agree(pe, be)
     print(f"<E>: reference algorithm {pe.mean():.4f}, batched {be.mean():.4f}, "
           f"diff {d:.4f}, standard error {sem:.4f}")
