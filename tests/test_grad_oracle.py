@@ -60,3 +60,37 @@ def test_launch_checks_shapes_and_device():
         energy_and_gradients(torch.zeros(10), ones, ones, ones, lay)
     with pytest.raises(ValueError, match="CUDA"):
         chain_energy(torch.zeros(10, requires_grad=True), ones, ones, ones, lay)
+
+
+def test_fluctuation_gradients_formula():
+    """d<A>/dtheta = <dA/dtheta> - beta (<A dU/dtheta> - <A><dU/dtheta>) from
+    the accumulated sums, against the same formula on the samples directly."""
+    from jmmonedmc_gb300.grad import fluctuation_gradients
+    rng = np.random.default_rng(3)
+    n_chains, m = 5, 400
+    t = rng.uniform(0.5, 2.0, n_chains)
+    stats = np.zeros(n_chains, dtype=np.dtype(abi.GRAD_STATS_DTYPE))
+    want = {}
+    for c in range(n_chains):
+        u = rng.normal(-100, 5, m)
+        g = np.stack([u / 1.3 + rng.normal(0, 1, m), rng.normal(40, 3, m),
+                      rng.normal(-2, 1, m)], axis=1)
+        l = rng.normal(50, 2, m)
+        rho = 32 / l
+        s = stats[c]
+        s["samples"] = m
+        s["sum_u"], s["sum_u2"], s["sum_rho"] = u.sum(), (u * u).sum(), rho.sum()
+        s["sum_rho2"], s["sum_l"] = (rho * rho).sum(), l.sum()
+        s["sum_g"], s["sum_u_g"] = g.sum(0), (u[:, None] * g).sum(0)
+        s["sum_rho_g"], s["sum_l_g"] = (rho[:, None] * g).sum(0), (l[:, None] * g).sum(0)
+        stats[c] = s
+        b = 1 / t[c]
+        for k, th in enumerate(("eps", "sigma")):
+            cov = lambda a: (a * g[:, k]).mean() - a.mean() * g[:, k].mean()
+            want.setdefault(f"dU_d{th}", []).append(g[:, k].mean() - b * cov(u))
+            want.setdefault(f"drho_d{th}", []).append(-b * cov(rho))
+            want.setdefault(f"dL_d{th}", []).append(-b * cov(l))
+    got = fluctuation_gradients(stats, t)
+    assert set(got) == set(want)
+    for key, vals in want.items():
+        np.testing.assert_allclose(got[key], vals, rtol=1e-9, atol=1e-9)
