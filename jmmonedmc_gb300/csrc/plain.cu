@@ -25,6 +25,15 @@
 // (i<j) at i*N+j; a step touches N-1 pairs, a volume move or energy check
 // all N(N-1)/2.  This TU is compiled with -fmad=false: no FP64 expression is
 // contracted into a fused multiply-add, matching the reference's x86-64 build.
+//
+// The in-order sums leave out the pairs whose terms are all +0.0 (pairs
+// beyond the cut-off or NBN): no term of any pair is ever -0.0 (each is a
+// positive product, a difference x - y of such numbers, or a copy of one), so
+// a partial sum that starts at +0.0 is never -0.0, and s - (+0.0) + (+0.0)
+// is s bit for bit; every sum is therefore the reference's own, add for add.
+// A step's partners are picked by warp ballots; a full sum's pairs are
+// marked in a bitmask as their terms are formed and compacted in pair order
+// by a block-wide scan.
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -54,6 +63,8 @@ struct Scalars {
   uint64_t echeck_count, echeck_resets;
   double echeck_e, echeck_e_before;
   uint64_t hist_ticks;  // histogram accumulations (ugrho calls) since set-up
+  uint64_t rho_l_bits;  // update_thermo's N / L, kept for the box length with these bits
+  double rho;
 };
 
 struct Args {
@@ -63,6 +74,9 @@ struct Args {
   double *rij;      // N*N, stored separation r_j - r_i at i*N+j (i<j)
   double *q;        // 9*N*N stored pair quantities
   double *scratch;  // 9*P pair terms of a full sum, packed row-major over (i<j)
+  uint32_t *mask;   // bit p: pair p of scratch has a term other than +0.0
+  double *comp;     // the marked pairs' terms in pair order (9 per pair)
+  uint64_t nwords;  // words of mask
   uint64_t n, nn, npairs, num_trial_types;
   int32_t potential, nbn;
   int32_t use_qavlj;
@@ -89,18 +103,22 @@ struct Ctl {
   double ran, bf;
   double sum[9];
   double part[2][9];  // qad2: the partner sums over i < nm and over i > nm
+  uint64_t ncomp;     // pairs compacted for a full sum
+  uint32_t wsum[32];  // per-warp counts of the compaction scan
   int32_t wall, accept, kind, outcome, reset, pad;
 };
 
 // ---- pair potentials (FP64, the reference's operand order) --------------
 
+// The reference forms r^-6 and r^-12 for every pair and uses them only within
+// the cut-off; here they are formed there only (same values where used).
 __device__ __forceinline__ void phi_lj(double d, double cut, bool virial, double *phi) {
-  double d3 = __dmul_rn(__dmul_rn(d, d), d);
-  double r6 = __ddiv_rn(1.0, __dmul_rn(d3, d3));
-  double r12 = __dmul_rn(r6, r6);
   double phitot = 0, phi6 = 0, phi12 = 0, vir6 = 0, vir12 = 0, virtot = 0;
   double hv6 = 0, hv12 = 0, hvtot = 0;
   if (d <= cut) {
+    const double d3 = __dmul_rn(__dmul_rn(d, d), d);
+    const double r6 = __ddiv_rn(1.0, __dmul_rn(d3, d3));
+    const double r12 = __dmul_rn(r6, r6);
     phi6 = __dmul_rn(4.0, r6);
     phi12 = __dmul_rn(4.0, r12);
     phitot = __dsub_rn(phi12, phi6);
@@ -184,11 +202,41 @@ __device__ double draw_uniform(Scalars *S, uint64_t seed) {
 
 // ---- block-wide pieces ----------------------------------------------------
 
+__device__ __forceinline__ bool any_term(const double *phi) {
+  unsigned long long bits = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) bits |= (unsigned long long)__double_as_longlong(phi[k]);
+  return bits != 0;  // some term other than +0.0
+}
+
+// Clears the pair mask before a full pass over the pairs (all threads).
+__device__ void clear_mask(const Args &a) {
+  for (uint64_t w = threadIdx.x; w < a.nwords; w += blockDim.x) a.mask[w] = 0u;
+  __syncthreads();
+}
+
+// Marks pair q (packed index) when nz.  Called in a row loop where the lanes
+// of one iteration hold consecutive pair indices from lane 0 on, and
+// `left` pairs of the row remain from lane 0's: the lanes of the iteration
+// are 0 .. min(left, 32) - 1.
+__device__ __forceinline__ void mark_pairs(const Args &a, uint64_t q, bool nz, uint64_t left) {
+  const unsigned act = left >= 32 ? 0xffffffffu : ((1u << left) - 1u);
+  const unsigned bits = __ballot_sync(act, nz);
+  if ((threadIdx.x & 31) == 0 && bits) {  // lane 0 holds the lowest index q
+    const uint64_t w = q >> 5;
+    const unsigned sh = (unsigned)(q & 31);
+    atomicOr(a.mask + w, bits << sh);
+    if (sh && (bits >> (32 - sh))) atomicOr(a.mask + w + 1, bits >> (32 - sh));
+  }
+}
+
 // Pair terms of every pair at positions `x` (box length `l` for HARMONIC's
-// virial) into scratch[k*9 + q]; pairs beyond NBN get zeros.
+// virial) into scratch[k*9 + q]; pairs beyond NBN get zeros.  Marks the
+// pairs with a term other than +0.0.
 __device__ void full_terms(const Args &a, const double *x, bool virial, double l) {
   const uint64_t n = a.n;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  clear_mask(a);
   for (uint64_t i = warp; i < n; i += nwarps) {
     const uint64_t row = packed_index(i, i + 1, n);
     for (uint64_t j = i + 1 + lane; j < n; j += 32) {
@@ -199,22 +247,69 @@ __device__ void full_terms(const Args &a, const double *x, bool virial, double l
       } else {
         phi_eval(a, __dsub_rn(x[j], x[i]), virial, l, phi);
       }
-      double *dst = a.scratch + (row + (j - i - 1)) * 9;
+      const uint64_t q = row + (j - i - 1);
+      double *dst = a.scratch + q * 9;
 #pragma unroll
       for (int k = 0; k < 9; ++k) dst[k] = phi[k];
+      mark_pairs(a, q, any_term(phi), n - (j - lane));
     }
   }
 }
 
-// Lanes 0..8 of warp 0: sequential sums of the scratch terms in pair order
-// (unrolled so that many of the independent loads are in flight ahead of
-// the dependent adds).
+// The marked pairs' terms, in pair order, into comp (pair of rank r at
+// comp[9r ..]); their number into ctl.ncomp.  A block-wide exclusive scan of
+// the mask words' bit counts gives each word its first rank.  All threads.
+__device__ void compact_terms(const Args &a, Ctl &ctl) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  uint64_t base = 0;
+  for (uint64_t w0 = 0; w0 < a.nwords; w0 += blockDim.x) {
+    const uint64_t w = w0 + threadIdx.x;
+    const uint32_t m = w < a.nwords ? a.mask[w] : 0u;
+    const uint32_t c = (uint32_t)__popc(m);
+    uint32_t x = c;  // inclusive scan within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) ctl.wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t t = lane < nwarps ? ctl.wsum[lane] : 0u;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      if (lane < nwarps) ctl.wsum[lane] = t;
+    }
+    __syncthreads();
+    uint64_t r = base + (warp ? ctl.wsum[warp - 1] : 0u) + (x - c);
+    for (uint32_t mm = m; mm; mm &= mm - 1u, ++r) {
+      const uint64_t p = w * 32 + (uint64_t)(__ffs(mm) - 1);
+      const double *src = a.scratch + p * 9;
+      double *dst = a.comp + r * 9;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) dst[k] = src[k];
+    }
+    base += ctl.wsum[nwarps - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) ctl.ncomp = base;
+  __syncthreads();
+}
+
+// The nine full sums of the scratch terms in pair order, by lanes 0..8 of
+// warp 0 over the compacted terms (unrolled so that many of the independent
+// loads are in flight ahead of the dependent adds).  All threads.
 __device__ void full_sums(const Args &a, Ctl &ctl) {
+  compact_terms(a, ctl);
   if (threadIdx.x < 9) {
     const int k = threadIdx.x;
+    const uint64_t nc = ctl.ncomp;
     double s = 0.0;
 #pragma unroll 32
-    for (uint64_t p = 0; p < a.npairs; ++p) s = __dadd_rn(s, a.scratch[p * 9 + k]);
+    for (uint64_t p = 0; p < nc; ++p) s = __dadd_rn(s, a.comp[p * 9 + k]);
     ctl.sum[k] = s;
   }
 }
@@ -256,9 +351,16 @@ __device__ void update_thermo(Scalars *S, uint64_t n) {
 // Accumulator k < 12 of update_thermo, for lane k: the same add of the same
 // term, with the term written as x * y (y = 1 for the plain sums, and x * 1 is
 // exact), so that the twelve adds are one FP64 instruction and no branch.
+// N / L is divided afresh only when L has changed (the same quotient).
 __device__ __forceinline__ void update_thermo_lane(Scalars *S, uint64_t n, int k) {
   const double l = S->l, e = S->tot[JMM_Q_E], vir = S->tot[JMM_Q_VIR], hv = S->tot[JMM_Q_HV];
-  const double rho = __ddiv_rn((double)n, l);
+  const uint64_t lbits = (uint64_t)__double_as_longlong(l);
+  const double rho = lbits == S->rho_l_bits ? S->rho : __ddiv_rn((double)n, l);
+  __syncwarp(0xfffu);
+  if (k == 0) {
+    S->rho_l_bits = lbits;
+    S->rho = rho;
+  }
   const double x = k < 2 ? rho : k < 4 ? l : k < 6 ? e : k == 6 ? l : k < 9 ? vir : k == 9 ? e : hv;
   const double y = k == 1                 ? rho
                    : k == 3               ? l
@@ -385,7 +487,7 @@ __device__ void qad2(const Args &a, Ctl &ctl, double *s_new, double *s_rij, cons
     ctl.kind = JMM_KIND_DISPLACEMENT;
     ctl.ran = NAN;
     ctl.bf = NAN;
-    ctl.wall = fabs(rt) > __ddiv_rn(S->l, 2.0);
+    ctl.wall = fabs(rt) > __dmul_rn(S->l, 0.5);  // L * 0.5 is L / 2.0 bit for bit
     if (ctl.wall) {
       S->d_acc[1] += 1;
       ctl.outcome = JMM_OUT_REJECT_WALL;
@@ -418,29 +520,38 @@ __device__ void qad2(const Args &a, Ctl &ctl, double *s_new, double *s_rij, cons
   __syncthreads();
   // the reference's order: (sum - old) + new over the partners i < nm (lanes
   // 0-8 of warp 0) and, as a separate sum, over i > nm (lanes 0-8 of warp 1):
-  // two dependent FP64 chains, which overlap only in different warps
+  // two dependent FP64 chains, which overlap only in different warps.  The
+  // 32 lanes of the warp test 32 partners at a time (any of the eighteen
+  // terms other than +0.0) and the nine summing lanes add the marked ones
+  // in index order; the others would add +0.0 twice.
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane < 9 && warp < 2) {
-    const int k = lane;
-    const double *nw = s_new + (uint64_t)k * nm1;
+  if (warp < 2) {
     const uint64_t p0 = warp == 0 ? 0 : nm, p1 = warp == 0 ? nm : nm1;
-    double sp = 0.0;
-    if (a.stage_old) {
-      const double *old = s_old + (uint64_t)k * nm1;
-#pragma unroll 8
-      for (uint64_t p = p0; p < p1; ++p) sp = __dadd_rn(__dsub_rn(sp, old[p]), nw[p]);
-    } else {
+    // stored term k of partner slot p
+    auto old_term = [&](int k, uint64_t p) -> double {
+      if (a.stage_old) return s_old[(uint64_t)k * nm1 + p];
       const double *old = a.q + (uint64_t)k * a.nn;
-      if (warp == 0) {
-#pragma unroll 16
-        for (uint64_t p = p0; p < p1; ++p) sp = __dadd_rn(__dsub_rn(sp, old[p * n + nm]), nw[p]);
-      } else {
-#pragma unroll 16
-        for (uint64_t p = p0; p < p1; ++p)
-          sp = __dadd_rn(__dsub_rn(sp, old[nm * n + p + 1]), nw[p]);
+      return warp == 0 ? old[p * n + nm] : old[nm * n + p + 1];
+    };
+    double sp = 0.0;
+    for (uint64_t c0 = p0; c0 < p1; c0 += 32) {
+      const uint64_t p = c0 + lane;
+      unsigned long long bits = 0;
+      if (p < p1) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+          bits |= (unsigned long long)__double_as_longlong(s_new[(uint64_t)k * nm1 + p]) |
+                  (unsigned long long)__double_as_longlong(old_term(k, p));
+      }
+      unsigned m = __ballot_sync(0xffffffffu, bits != 0);
+      if (lane < 9) {
+        for (; m; m &= m - 1u) {
+          const uint64_t pp = c0 + (uint64_t)(__ffs(m) - 1);
+          sp = __dadd_rn(__dsub_rn(sp, old_term(lane, pp)), s_new[(uint64_t)lane * nm1 + pp]);
+        }
       }
     }
-    ctl.part[warp][k] = sp;
+    if (lane < 9) ctl.part[warp][lane] = sp;
   }
   __syncthreads();
   if (threadIdx.x < 9)
@@ -621,9 +732,10 @@ __device__ void echeck(const Args &a, Ctl &ctl) {
   const uint64_t n = a.n;
   full_terms(a, a.r, false, S->l);
   __syncthreads();
+  compact_terms(a, ctl);
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (uint64_t p = 0; p < a.npairs; ++p) s = __dadd_rn(s, a.scratch[p * 9]);
+    for (uint64_t p = 0; p < ctl.ncomp; ++p) s = __dadd_rn(s, a.comp[p * 9]);
     S->echeck_count += 1;
     S->echeck_e = s;
     S->echeck_e_before = S->tot[JMM_Q_E];
@@ -634,6 +746,7 @@ __device__ void echeck(const Args &a, Ctl &ctl) {
   if (!ctl.reset) return;
   const double l = S->l;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  clear_mask(a);
   for (uint64_t i = warp; i < n; i += nwarps) {
     const uint64_t row = packed_index(i, i + 1, n);
     for (uint64_t j = i + 1 + lane; j < n; j += 32) {
@@ -647,12 +760,14 @@ __device__ void echeck(const Args &a, Ctl &ctl) {
         a.rij[ind] = rij;
         phi_eval(a, rij, true, l, phi);
       }
-      double *dst = a.scratch + (row + (j - i - 1)) * 9;
+      const uint64_t q = row + (j - i - 1);
+      double *dst = a.scratch + q * 9;
 #pragma unroll
       for (int k = 0; k < 9; ++k) {
         a.q[k * a.nn + ind] = phi[k];
         dst[k] = phi[k];
       }
+      mark_pairs(a, q, any_term(phi), n - (j - lane));
     }
   }
   __syncthreads();
@@ -848,6 +963,7 @@ __device__ void move_volume(const Args &a, Ctl &ctl, double l) {
   for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) a.r[i] = __dmul_rn(a.r[i], lrat1);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  clear_mask(a);
   for (uint64_t i = warp; i < n; i += nwarps) {
     const uint64_t row = packed_index(i, i + 1, n);
     for (uint64_t j = i + 1 + lane; j < n; j += 32) {
@@ -861,12 +977,14 @@ __device__ void move_volume(const Args &a, Ctl &ctl, double l) {
         a.rij[ind] = rij;
         phi_eval(a, rij, true, l, phi);
       }
-      double *dst = a.scratch + (row + (j - i - 1)) * 9;
+      const uint64_t q = row + (j - i - 1);
+      double *dst = a.scratch + q * 9;
 #pragma unroll
       for (int k = 0; k < 9; ++k) {
         a.q[k * a.nn + ind] = phi[k];
         dst[k] = phi[k];
       }
+      mark_pairs(a, q, any_term(phi), n - (j - lane));
     }
   }
   __syncthreads();
@@ -1004,6 +1122,8 @@ static void plain_free(jmm_plain *h) {
   cudaFree(h->a.rij);
   cudaFree(h->a.q);
   cudaFree(h->a.scratch);
+  cudaFree(h->a.mask);
+  cudaFree(h->a.comp);
   cudaFree(h->a.h_val);
   cudaFree(h->a.h_acc);
   cudaFree(h->a.h_last);
@@ -1080,6 +1200,9 @@ extern "C" int jmm_plain_create(const jmm_params *prm, jmm_plain **out) {
   ALLOC(a.rij, a.nn * sizeof(double));
   ALLOC(a.q, 9 * a.nn * sizeof(double));
   ALLOC(a.scratch, 9 * a.npairs * sizeof(double));
+  a.nwords = (a.npairs + 31) / 32;
+  ALLOC(a.mask, a.nwords * sizeof(uint32_t));
+  ALLOC(a.comp, 9 * a.npairs * sizeof(double));
 #undef ALLOC
 
   Scalars s;
