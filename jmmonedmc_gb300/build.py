@@ -1,7 +1,7 @@
-"""In-tree build of libjmmgpu.so (sm_103a) and of the oracle's CPU library.
+"""In-tree build of libjmmgpu.so (sm_103a).
 
-    python -m jmmonedmc_gb300.build          # CUDA library only
-    python -c "import __graft_entry__ as g; g.build()"   # everything
+    python -m jmmonedmc_gb300.build          # the CUDA library
+    python -c "import __graft_entry__ as g; g.build()"   # with the oracle (tests)
 
 The CUDA library is compiled with nvcc straight for sm_103a, one object per
 translation unit, in parallel, then linked with ``nvcc -shared``; no
@@ -80,23 +80,6 @@ def build_native(verbose=False, jobs=None):
         for u, log in logs.items():
             sys.stdout.write(f"== {u}\n{log}")
     return out
-
-
-def build_oracle():
-    """The oracle's CPU library (oracle/_build/libjmmoracle.so)."""
-    oracle = os.path.join(REPO, "oracle")
-    subprocess.run(["make", "-s", "-C", oracle], check=True)
-    return os.path.join(oracle, "_build", "libjmmoracle.so")
-
-
-def build_reference_if_present():
-    """The reference compiled from its own tree, where that tree exists."""
-    oracle = os.path.join(REPO, "oracle")
-    ref_src = os.environ.get("JMM_REF_SRC", "/root/reference/src")
-    if not os.path.isdir(ref_src):
-        return None
-    subprocess.run(["make", "-s", "-C", oracle, "ref", f"REF_SRC={ref_src}"], check=True)
-    return os.path.join(oracle, "_ref")
 
 
 if __name__ == "__main__":

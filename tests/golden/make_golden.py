@@ -4,8 +4,9 @@ Runs the reference's move loop, compiled from its own sources with the
 project's Philox stand-in for GSL (oracle/Makefile target ``ref``), on a set
 of INPUT files, and stores per-step trajectories, final positions, thermo
 accumulators and the reference's own output files as small compressed
-fixtures.  It needs the reference tree (REF_SRC, default
-/root/reference/src) and is run by hand:
+fixtures.  It needs the reference tree, which the oracle's build recipe
+(oracle/build_oracle.py: JMM_REF_SRC, or the checkout's usual place) finds,
+and is run by hand:
 
     python tests/golden/make_golden.py
 
@@ -24,6 +25,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 ORACLE = os.path.join(REPO, "oracle")
 HARNESS = os.path.join(ORACLE, "_ref", "ref_harness")
+
+
+def _recipe():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("build_oracle",
+                                                  os.path.join(ORACLE, "build_oracle.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
 
 REF_STEP_DTYPE = np.dtype([
     ("sn", "<u8"), ("nm", "<u8"), ("rn", "<f8"), ("e", "<f8"), ("vir", "<f8"),
@@ -88,7 +98,8 @@ def input_text(kw):
 
 
 def build_reference():
-    subprocess.run(["make", "-s", "-C", ORACLE, "ref"], check=True)
+    if _recipe().build_reference_if_present() is None:
+        sys.exit("make_golden: the reference tree is not present (set JMM_REF_SRC)")
 
 
 def run_case(name, overrides):

@@ -45,6 +45,17 @@ SIGS = {
 }
 
 
+def reference_sources():
+    """The reference's src directory where it is present (the oracle's build
+    recipe knows where), else None."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "build_oracle", os.path.join(REPO, "oracle", "build_oracle.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.reference_sources()
+
+
 def extra_sigs(sigs):
     SIGS.update(sigs)
     if _lib is not None:

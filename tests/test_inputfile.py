@@ -16,9 +16,10 @@ import numpy as np
 import pytest
 
 from jmmonedmc_gb300 import abi, inputfile
+from tests import oracle_lib
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SRC = os.environ.get("JMM_REF_SRC", "/root/reference/src")
+REF_SRC = oracle_lib.reference_sources() or ""
 DUMP = os.path.join(REPO, "oracle", "_ref", "input_dump")
 GOLDEN = os.path.join(REPO, "tests", "golden")
 

@@ -14,7 +14,7 @@ from jmmonedmc_gb300 import abi
 from tests import oracle_lib
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SRC = os.environ.get("JMM_REF_SRC", "/root/reference/src")
+REF_SRC = oracle_lib.reference_sources() or ""
 DUMP = os.path.join(REPO, "oracle", "_ref", "pot_dump")
 
 
