@@ -319,6 +319,15 @@ int jmm_batch_set_positions(jmm_batch *b, uint32_t chain, const float *x, uint32
                             double l);
 /* FP64 sums of the FP32 pair energies of every chain's current positions. */
 int jmm_batch_energies(jmm_batch *b, double *e, uint32_t n_chains);
+/* The two energies a volume move of every chain compares (fav's ETrial and
+ * E, src/jmmMCState.cpp:2193-2249), formed as the chain kernel's volume move
+ * forms them (same lanes, order and precision): out[3k .. 3k+2] = U_old of
+ * the current positions, U_new of the positions and box scaled by scale[k]
+ * (FP32 products x_i * s, box length l * s), and U_new - U_old (FP64; in
+ * FAST precision an FP64 sum of per-pair differences, and U_new = U_old +
+ * that).  The state is not changed.  NaN where the chain's window would
+ * reach half a periodic ring. */
+int jmm_batch_volume_energies(jmm_batch *b, const float *scale, double *out, uint32_t n_chains);
 /* Device addresses of the positions (float, chain k at offsets[k]) and of the
  * jmm_chain_result array, for zero-copy tooling (torch, benchmarks). */
 int jmm_batch_device_views(jmm_batch *b, void **positions, void **results,

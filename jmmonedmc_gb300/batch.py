@@ -29,6 +29,7 @@ _native.register({
     "jmm_batch_get_positions": [C.c_void_p, C.c_uint32, P(C.c_float), C.c_uint32],
     "jmm_batch_set_positions": [C.c_void_p, C.c_uint32, P(C.c_float), C.c_uint32, C.c_double],
     "jmm_batch_energies": [C.c_void_p, P(C.c_double), C.c_uint32],
+    "jmm_batch_volume_energies": [C.c_void_p, P(C.c_float), P(C.c_double), C.c_uint32],
     "jmm_batch_device_views": [C.c_void_p, P(C.c_void_p), P(C.c_void_p), P(C.c_uint64),
                                C.c_uint32],
     "jmm_batch_autotune": [C.c_void_p, C.c_uint32, P(C.c_uint32), P(C.c_uint32),
@@ -190,6 +191,18 @@ class ChainBatch:
         _native.call("jmm_batch_energies", self._h, e.ctypes.data_as(P(C.c_double)),
                      self.n_chains)
         return e
+
+    def volume_energies(self, scale):
+        """(U_old, U_new, U_new - U_old) per chain, float64 (n_chains, 3): the
+        energies a volume move of each chain would compare, positions and box
+        scaled by scale[k] (as the chain kernel's volume move forms them)."""
+        scale = np.ascontiguousarray(scale, dtype=np.float32)
+        if scale.shape != (self.n_chains,):
+            raise ValueError("one scale factor per chain")
+        out = np.empty((self.n_chains, 3), dtype=np.float64)
+        _native.call("jmm_batch_volume_energies", self._h, scale.ctypes.data_as(P(C.c_float)),
+                     out.ctypes.data_as(P(C.c_double)), self.n_chains)
+        return out
 
     def device_views(self):
         """(positions device address, results device address, offsets)."""

@@ -839,6 +839,118 @@ extern "C" int jmm_batch_energies(jmm_batch *b, double *e, uint32_t n_chains) {
   return JMM_OK;
 }
 
+// Trial energies of a volume move of every chain: one group of L = G*S lanes
+// per chain (its class's shape), through the chain_energies call that the
+// chain kernel's volume move makes, so lanes, summation order and precision
+// are the move's own.
+template <int L, int POT, bool PER, bool kExact>
+__global__ void volume_energies_kernel(const ChainParams *__restrict__ prm,
+                                       const jmm_chain_result *__restrict__ res,
+                                       const float *__restrict__ xg, const float *__restrict__ scale,
+                                       double *__restrict__ out, uint32_t n_chains) {
+  const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) / L;
+  if (c >= n_chains) return;  // whole groups leave together
+  const int cl = threadIdx.x % L;
+  const unsigned gmask =
+      (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << (((threadIdx.x & 31) / L) * L));
+  const ChainParams P = prm[c];
+  Hot H;
+  H.eps4 = P.eps4;
+  H.sigma2 = P.sigma2;
+  H.inv_sigma2 = P.inv_sigma2;
+  H.rc2 = P.rc2;
+  H.beta = P.beta;
+  H.two_max_step = P.two_max_step;
+  const double l = res[P.id].l;
+  const float s = scale[P.id];
+  const double lnew = __dmul_rn(l, (double)s);
+  double uo, un;
+  uint64_t pairs = 0;
+  uint32_t err = 0;
+  chain_energies<L, POT, PER, kExact, true>(xg + P.x_off, H, (int)P.n, cl, gmask, (float)l, s,
+                                            (float)lnew, uo, un, pairs, err);
+  const double du = __dsub_rn(un, uo);  // as the volume move forms it
+  if (cl == 0) {
+    double *o = out + 3 * (uint64_t)P.id;
+    o[0] = err ? (double)NAN : uo;
+    o[1] = err ? (double)NAN : un;
+    o[2] = err ? (double)NAN : du;
+  }
+}
+
+typedef void (*VolKernel)(const ChainParams *, const jmm_chain_result *, const float *,
+                          const float *, double *, uint32_t);
+
+template <int L, bool E>
+static VolKernel pick_vol_pot(int pot, bool per) {
+  switch (pot * 2 + (per ? 1 : 0)) {
+    case JMM_POT_LJCUT * 2: return volume_energies_kernel<L, JMM_POT_LJCUT, false, E>;
+    case JMM_POT_LJCUT * 2 + 1: return volume_energies_kernel<L, JMM_POT_LJCUT, true, E>;
+    case JMM_POT_SOFTSPHERE * 2: return volume_energies_kernel<L, JMM_POT_SOFTSPHERE, false, E>;
+    case JMM_POT_SOFTSPHERE * 2 + 1: return volume_energies_kernel<L, JMM_POT_SOFTSPHERE, true, E>;
+    case JMM_POT_GAUSS * 2: return volume_energies_kernel<L, JMM_POT_GAUSS, false, E>;
+    case JMM_POT_GAUSS * 2 + 1: return volume_energies_kernel<L, JMM_POT_GAUSS, true, E>;
+    default: return nullptr;
+  }
+}
+
+static VolKernel pick_vol(uint32_t lanes, bool exact, int pot, bool per) {
+  switch (lanes) {
+    case 32: return exact ? pick_vol_pot<32, true>(pot, per) : pick_vol_pot<32, false>(pot, per);
+    case 16: return exact ? pick_vol_pot<16, true>(pot, per) : pick_vol_pot<16, false>(pot, per);
+    case 8: return exact ? pick_vol_pot<8, true>(pot, per) : pick_vol_pot<8, false>(pot, per);
+    default: return nullptr;
+  }
+}
+
+extern "C" int jmm_batch_volume_energies(jmm_batch *b, const float *scale, double *out,
+                                         uint32_t n_chains) {
+  clear_error();
+  JMM_CHECK_ARG(b && scale && out, "null argument");
+  JMM_CHECK_ARG(n_chains == b->n_chains, "n_chains does not match the batch");
+  for (uint32_t k = 0; k < n_chains; ++k)
+    JMM_CHECK_ARG(std::isfinite(scale[k]) && scale[k] > 0.0f,
+                  "scale factors must be finite and positive");
+  float *d_scale = nullptr;
+  double *d_out = nullptr;
+  JMM_CUDA(cudaStreamSynchronize(b->stream));
+  cudaError_t e = cudaMalloc((void **)&d_scale, n_chains * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_out, 3 * (size_t)n_chains * sizeof(double));
+  int rc = JMM_OK;
+  if (e != cudaSuccess) rc = cuda_status(e, "cudaMalloc", __FILE__, __LINE__);
+  if (rc == JMM_OK) {
+    e = cudaMemcpyAsync(d_scale, scale, n_chains * sizeof(float), cudaMemcpyHostToDevice,
+                        b->stream);
+    if (e != cudaSuccess) rc = cuda_status(e, "cudaMemcpyAsync", __FILE__, __LINE__);
+  }
+  const bool per = b->cfg.boundary == JMM_BOUNDARY_PERIODIC;
+  const bool exact = b->cfg.precision == JMM_PREC_EXACT;
+  for (size_t k = 0; rc == JMM_OK && k < b->classes.size(); ++k) {
+    const PotClass &pc = b->classes[k];
+    const uint32_t lanes = pc.shape.g * pc.shape.spr;
+    VolKernel kf = pick_vol(lanes, exact, pc.pot, per);
+    if (!kf) {
+      rc = fail(JMM_ERR_INVALID, "no volume-energy kernel for this launch shape");
+      break;
+    }
+    const uint32_t threads = 128;
+    const uint32_t blocks = (uint32_t)(((uint64_t)pc.count * lanes + threads - 1) / threads);
+    kf<<<blocks, threads, 0, b->stream>>>(b->d_params + pc.first, b->d_res, b->d_x, d_scale, d_out,
+                                          pc.count);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) rc = cuda_status(e, "volume_energies_kernel", __FILE__, __LINE__);
+  }
+  if (rc == JMM_OK) {
+    e = cudaMemcpyAsync(out, d_out, 3 * (size_t)n_chains * sizeof(double), cudaMemcpyDeviceToHost,
+                        b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) rc = cuda_status(e, "volume energies read-back", __FILE__, __LINE__);
+  }
+  cudaFree(d_scale);
+  cudaFree(d_out);
+  return rc;
+}
+
 extern "C" int jmm_batch_device_views(jmm_batch *b, void **positions, void **results,
                                       uint64_t *offsets, uint32_t n_chains) {
   clear_error();
@@ -878,10 +990,13 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
   // Time of a trial: the whole batch (cls < 0), or class cls alone; the
-  // state is restored before each run, the first run warms the code path.
+  // state is restored before each run, the first run warms the code path and
+  // the best of the next three counts (a single short run can land on a
+  // clock ramp).
   auto trial = [&](int cls, float *ms_out) -> int {
-    float ms = 0.0f;
-    for (int rep = 0; rep < 2; ++rep) {
+    float best_run = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+      float ms = 0.0f;
       cudaMemcpyAsync(b->d_x, x_save, b->total_floats * sizeof(float), cudaMemcpyDeviceToDevice,
                       b->stream);
       cudaMemcpyAsync(b->d_res, r_save, b->n_chains * sizeof(jmm_chain_result),
@@ -898,8 +1013,9 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
       if (rc) return rc;
       cudaEventSynchronize(t1);
       cudaEventElapsedTime(&ms, t0, t1);
+      if (rep > 0 && ms < best_run) best_run = ms;
     }
-    *ms_out = ms;
+    *ms_out = best_run;
     return JMM_OK;
   };
   Shape best[3];
@@ -915,31 +1031,43 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
       for (const PotClass &pc : b->classes) present = present || pc.pot == kPots[pi];
       if (!present) continue;
     }
-    float best_ms = 1e30f;
+    // every candidate once, then the three fastest again, so that a drift
+    // of the clocks over the scan cannot decide
+    std::vector<std::pair<float, std::vector<Shape>>> timed;
     for (const auto &shape : kTuneShapes) {
       for (uint32_t threads : kTuneThreads) {
         const uint32_t cpb = threads / (shape[0] * shape[1]);
         if (cpb == 0) continue;
-        Shape sh[3];
+        std::vector<Shape> sh(3);
         for (int q = 0; q < 3; ++q)
           sh[q] = per_class ? best[q] : Shape{shape[0], shape[1], cpb, shape[2]};
         if (per_class) sh[pi] = Shape{shape[0], shape[1], cpb, shape[2]};
-        if (apply_layout(b, sh) != JMM_OK) {
+        if (apply_layout(b, sh.data()) != JMM_OK) {
           clear_error();
           continue;
         }
         float ms = 0.0f;
         rc = trial(per_class ? pi : -1, &ms);
         if (rc) break;
-        if (ms < best_ms) {
-          best_ms = ms;
-          if (per_class)
-            best[pi] = sh[pi];
-          else
-            for (int q = 0; q < 3; ++q) best[q] = sh[q];
-        }
+        timed.emplace_back(ms, sh);
       }
       if (rc) break;
+    }
+    if (rc) break;
+    std::sort(timed.begin(), timed.end(),
+              [](const auto &x, const auto &y) { return x.first < y.first; });
+    float best_ms = 1e30f;
+    for (size_t c = 0; c < timed.size() && c < 3 && rc == JMM_OK; ++c) {
+      if (apply_layout(b, timed[c].second.data()) != JMM_OK) {
+        clear_error();
+        continue;
+      }
+      float ms = 0.0f;
+      rc = trial(per_class ? pi : -1, &ms);
+      if (rc == JMM_OK && ms < best_ms) {
+        best_ms = ms;
+        for (int q = 0; q < 3; ++q) best[q] = timed[c].second[q];
+      }
     }
   }
   if (per_class && rc == JMM_OK && b->classes.size() > 1) {

@@ -30,10 +30,10 @@
 // that the EXACT precision mode can be replayed bit for bit by the oracle;
 // the FAST mode differs in using the hardware reciprocal, exp and log, in
 // scaling a window's summed pair shapes by the potential's strength once, in
-// summing a volume move's pair terms per lane in FP32 before the FP64 lane
-// sum, and in summing a round's per-step statistics by a scan over its slots
-// into per-lane shares instead of step by step (the same quantities, rounded
-// in another order).
+// forming a volume move's U_new - U_old from per-pair differences (FP32 in
+// a lane, FP64 across lanes), and in summing a round's per-step statistics by a scan over
+// its slots into per-lane shares instead of step by step (the same
+// quantities, rounded in another order).
 #pragma once
 #include <math.h>
 #include <stdint.h>
@@ -287,15 +287,21 @@ __device__ __forceinline__ float threshold_of(uint32_t w) {
 
 // group_energies for the step loop: potential and boundary fixed at compile
 // time.  EXACT precision sums in the same order (per-particle FP32, lane and
-// chain FP64); FAST sums each lane's pair shapes in FP32, scales them by eps4
-// in FP64 and sums the lanes in FP64.
+// chain FP64) and forms U_new - U_old as the difference of the two FP64 sums.
+// FAST sums each lane's pair shapes in FP32 and, apart, the differences of
+// its scaled and unscaled pair shapes (each a small fraction of its pair's
+// energy, so that their FP32 sum carries an error far below that of the
+// shapes' own), scales both by eps4 in FP64 and sums the lanes in FP64:
+// U_new - U_old is the FP64 sum of the per-pair differences, and
+// U_new = U_old + du (a caller's U_new - U_old gives du back to within an
+// ulp of U).
 template <int L, int POT, bool PER, bool kExact, bool kScaled>
 __device__ __noinline__ void chain_energies(const float *xs, const Hot &H, int n, int gl,
                                                unsigned gmask, float lf, float s, float lnf,
                                                double &u_old, double &u_new, uint64_t &pairs,
                                                uint32_t &err) {
-  double uo = 0.0, un = 0.0;
-  float fo = 0.0f, fn = 0.0f;  // FAST: the lane's shape sums
+  double uo = 0.0, un = 0.0;   // EXACT: U_old and U_new lane sums
+  float fo = 0.0f, fd = 0.0f;  // FAST: the lane's shapes and shape differences
   uint32_t cnt = 0;
   for (int i = gl; i < n; i += L) {
     const float xi = xs[i];
@@ -332,8 +338,9 @@ __device__ __noinline__ void chain_energies(const float *xs, const Hot &H, int n
         eo = __fadd_rn(eo, pair_energy_h<POT, true>(d2, H));
         if (kScaled) en = __fadd_rn(en, pair_energy_h<POT, true>(dn2, H));
       } else {
-        fo = __fadd_rn(fo, pair_shape_fast<POT>(d2, H));
-        if (kScaled) fn = __fadd_rn(fn, pair_shape_fast<POT>(dn2, H));
+        const float so = pair_shape_fast<POT>(d2, H);
+        fo = __fadd_rn(fo, so);
+        if (kScaled) fd = __fadd_rn(fd, __fsub_rn(pair_shape_fast<POT>(dn2, H), so));
       }
       cnt += kScaled ? 2 : 1;
     }
@@ -344,10 +351,15 @@ __device__ __noinline__ void chain_energies(const float *xs, const Hot &H, int n
   }
   if (!kExact) {
     uo = __dmul_rn((double)H.eps4, (double)fo);
-    un = __dmul_rn((double)H.eps4, (double)fn);
+    un = __dmul_rn((double)H.eps4, (double)fd);
   }
   u_old = group_sum_d<L>(uo, gmask);
-  u_new = kScaled ? group_sum_d<L>(un, gmask) : u_old;
+  if (!kScaled) {
+    u_new = u_old;
+  } else {
+    const double x = group_sum_d<L>(un, gmask);
+    u_new = kExact ? x : __dadd_rn(u_old, x);
+  }
   pairs += __reduce_add_sync(gmask, cnt);
 }
 
