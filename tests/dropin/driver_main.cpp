@@ -3,6 +3,11 @@
 // (src/Main.cpp:36-189) with a small INPUT reader of its own (the keyword
 // rules of src/readInput.cpp:59-257), so that the drop-in can run where the
 // reference's own Main.cpp and readInput.cpp are not present.
+//
+// Built with -DJMM_DRIVER_TEAM the calls are made as the reference's driver
+// makes them: inside one OpenMP parallel region, every thread calling fad,
+// incrementStep, Step and printG, one thread (single / sections) the
+// prints and adjustments, with barriers around Step (src/Main.cpp:50-180).
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -65,6 +70,7 @@ static MCInput read_input(const char *path) {
   return inp;
 }
 
+#ifndef JMM_DRIVER_TEAM
 int main() {
   MCInput inp = read_input("INPUT");
   MCState *mcs = setupMCS(inp);
@@ -98,3 +104,60 @@ int main() {
   freeMCS(mcs);
   return 0;
 }
+#else
+#include <omp.h>
+
+int main() {
+  MCInput inp = read_input("INPUT");
+  MCState *mcs = setupMCS(inp);
+  if (!mcs) return 1;
+#pragma omp parallel default(shared)
+  {
+#pragma omp single
+    printStep(mcs);
+    unsigned long int nnn = 0;
+    double ddd = 0.5;
+    fad(mcs, &nnn, &ddd);
+    if (getRelaxFlag(mcs) > 0) relaxVolume(mcs);
+    if (!getRestartFlag(mcs)) {
+#pragma omp sections
+      {
+#pragma omp section
+        printCoords(mcs);
+#pragma omp section
+        printRho(mcs);
+#pragma omp section
+        {
+          updateThermo(mcs);
+          printThermo(mcs);
+        }
+      }
+      printG(mcs);
+    }
+    while (incrementStep(mcs)) {
+#pragma omp barrier
+      Step(mcs);
+#pragma omp barrier
+#pragma omp single
+      if (isCoordPrint(mcs)) printCoords(mcs);
+#pragma omp single
+      if (isThermoPrint(mcs)) printThermo(mcs);
+#pragma omp single
+      if (isRhoPrint(mcs)) printRho(mcs);
+#pragma omp single
+      if (isMaxDisAdjust(mcs)) maxDisAdjust(mcs);
+#pragma omp single
+      if (isMaxDVAdjust(mcs)) maxDVAdjust(mcs);
+      if (isGPrint(mcs)) printG(mcs);
+      if ((getStepNum(mcs) % 10000 == 0) && (getStepNum(mcs) < 1E6) && (getRelaxFlag(mcs) > 0))
+        relaxVolume(mcs);
+    }
+#pragma omp barrier
+  }
+  printf("\nPROGRAM COMPLETED SUCCESSFULLY!\n");
+  printE(mcs);
+  printAcc(mcs);
+  freeMCS(mcs);
+  return 0;
+}
+#endif

@@ -22,15 +22,19 @@ import numpy as np
 import pytest
 
 from tests import golden_cases as gc
+from tests import oracle_lib
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SRC = os.environ.get("JMM_REF_SRC", "/root/reference/src")
+REF_SRC = oracle_lib.reference_sources() or ""
 DRIVER = os.path.join(REPO, "tests", "dropin", "driver_main.cpp")
 
 
-def _build_driver(out_dir):
+def _build_driver(out_dir, team=False):
+    """team: the driver makes its calls from an OpenMP team as the
+    reference's driver does (src/Main.cpp:50-180)."""
     from jmmonedmc_gb300.dropin.build_dropin import build
-    return build(os.path.join(out_dir, "dropin_driver"), [DRIVER])
+    return build(os.path.join(out_dir, "dropin_driver_team" if team else "dropin_driver"), [DRIVER],
+                 extra=["-DJMM_DRIVER_TEAM"] if team else [])
 
 
 def test_reference_driver_links_against_dropin(native, tmp_path):
@@ -44,15 +48,19 @@ def test_reference_driver_links_against_dropin(native, tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("threads", [1, 4], ids=["1thread", "team4"])
 @pytest.mark.parametrize("name", gc.case_names())
-def test_dropin_writes_the_reference_files(gpu, name, tmp_path):
-    exe = _build_driver(str(tmp_path))
+def test_dropin_writes_the_reference_files(gpu, name, threads, tmp_path):
+    """threads 4: every API call made from a team of four OpenMP threads in
+    the reference driver's pattern; the drop-in runs each move once per team,
+    so the files are the same as with one thread."""
+    exe = _build_driver(str(tmp_path), team=threads > 1)
     kw, params, ref = gc.load_case(name)
     run = tmp_path / "run"
     run.mkdir()
     (run / "INPUT").write_text(str(ref["input"]))
     out = subprocess.run([exe], cwd=run, capture_output=True, text=True, timeout=300,
-                         env=dict(os.environ, OMP_NUM_THREADS="1"))
+                         env=dict(os.environ, OMP_NUM_THREADS=str(threads)))
     assert out.returncode == 0, out.stderr
     harmonic = kw["POT"] == "HARMONIC"
     ours = (run / "thermo.dat.mcs").read_text().splitlines()
