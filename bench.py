@@ -24,7 +24,6 @@ import argparse
 import json
 import math
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -66,7 +65,16 @@ def parse_args():
                     help="large workload: particles per domain")
     ap.add_argument("--sample-every", type=int, default=10,
                     help="grad workload: sweeps between gradient samples")
+    ap.add_argument("--no-sub-workloads", action="store_true",
+                    help="batched NPT workload at one GPU: leave out the compact records of the "
+                         "uneven, gradient and large-chain workloads")
     args = ap.parse_args()
+    return apply_workload_defaults(args)
+
+
+def apply_workload_defaults(args):
+    """Sizes of the chosen workload where the command line left the batched
+    NPT workload's defaults."""
     if args.workload == "uneven":
         if args.chains == 4096:
             args.chains = 1024
@@ -293,45 +301,81 @@ def cpu_reference_sample(chains, seconds, seed):
 
 # ---- roofline inputs -----------------------------------------------------------
 
+FIGURES = os.path.join(REPO, "profiles", "figures.json")
+
+
+def profile_figures(kernel):
+    """The ncu figures of one kernel (profiles/figures.json, written from the
+    committed ncu summaries), or {}."""
+    if not os.path.exists(FIGURES):
+        return {}
+    with open(FIGURES) as f:
+        return json.load(f).get(kernel, {})
+
+
 def profile_traffic(args, pair_evals_per_launch, sweeps):
-    """DRAM bytes per launch of the chain kernel from the committed ncu summary
+    """DRAM bytes per launch of the chain kernel from its ncu figures
     (measured on a smaller launch and scaled by the launch's sweeps)."""
-    path = os.path.join(REPO, "profiles", "chains_kernel_batched_npt.md")
-    if not os.path.exists(path):
+    fig = profile_figures("chains_kernel_batched_npt")
+    if "dram_bytes_per_chain_sweep" not in fig:
         return None
-    with open(path) as f:
-        text = f.read()
-    m = re.search(r"dram_bytes_per_chain_sweep:\s*([0-9.eE+-]+)", text)
-    m0 = re.search(r"dram_bytes_per_chain_launch_fixed:\s*([0-9.eE+-]+)", text)
-    if not m:
-        return None
-    per = float(m.group(1))
-    fixed = float(m0.group(1)) if m0 else 0.0
-    return args.chains * (per * sweeps + fixed)
+    return args.chains * (fig["dram_bytes_per_chain_sweep"] * sweeps
+                          + fig.get("dram_bytes_per_chain_launch_fixed", 0.0))
 
 
-def issue_roofline(profile, moves_per_s, clocks, dev):
+def issue_roofline(kernel, moves_per_s, clocks, dev):
     """Warp instructions issued per second by the dominant kernel against the
     issue limit (4 schedulers per SM, one warp instruction each per clock):
-    the kernel's instructions per attempted move, from its committed ncu
-    summary, times the timed moves/s of one GPU."""
+    the kernel's instructions per attempted move, from its ncu figures, times
+    the timed moves/s of one GPU."""
     import torch
-    path = os.path.join(REPO, "profiles", profile)
-    if not os.path.exists(path):
-        return None
-    with open(path) as f:
-        m = re.search(r"warp_instructions_per_move:\s*([0-9.eE+-]+)", f.read())
+    fig = profile_figures(kernel)
     mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
-    if not m or not mhz:
+    if "warp_instructions_per_move" not in fig or not mhz:
         return None
-    per_move = float(m.group(1))
+    per_move = float(fig["warp_instructions_per_move"])
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     peak = sms * 4 * float(mhz) * 1e6
     achieved = per_move * moves_per_s
     return {"achieved": achieved, "peak": peak, "unit": "warp instructions/s",
             "frac": achieved / peak, "instructions_per_move": per_move,
-            "source": f"instructions per move from profiles/{profile} (ncu); peak = 4 issue "
-                      f"slots per SM per clock x {sms} SMs x the sampled SM clock"}
+            "source": f"instructions per move from the ncu capture in {fig.get('summary')} "
+                      f"(profiles/figures.json); peak = 4 issue slots per SM per clock x {sms} "
+                      "SMs x the sampled SM clock"}
+
+
+def in_cutoff_neighbours(x_all, sizes, rc, periodic_l=None):
+    """Mean number of partners within the cut-off (|x_j - x_i| <= rc, either
+    side) per particle, over every chain of a sample of ordered positions
+    (x_all back to back, chain k holding sizes[k]): the k of the algorithmic
+    work unit, in-cut-off pairs per moved particle."""
+    import numpy as np
+    total_pairs, total_particles, off = 0, 0, 0
+    for k, n in enumerate(sizes):
+        x = np.asarray(x_all[off:off + n], dtype=np.float64)
+        off += n
+        r = rc[k] if hasattr(rc, "__len__") else rc
+        right = np.searchsorted(x, x + r, side="right") - np.arange(1, n + 1)
+        total_pairs += int(right.sum())
+        total_particles += n
+    return 2.0 * total_pairs / max(1, total_particles)
+
+
+def algorithmic_pairs(before, after, x_all, chains):
+    """Pair evaluations the moves of the timed region need (the algorithmic
+    work unit): a displacement evaluates its k in-cut-off partners at the old
+    and the trial position (2k), a volume move the N k / 2 in-cut-off pairs
+    at the new box length; k per chain from its positions after the run."""
+    ks, off = [], 0
+    for c in chains:
+        n = int(c.n)
+        ks.append(in_cutoff_neighbours(x_all[off:off + n], [n], float(c.cutoff)))
+        off += n
+    total = 0.0
+    for c, k, d_att, v_att in zip(chains, ks, after["disp_att"] - before["disp_att"],
+                                  after["vol_att"] - before["vol_att"]):
+        total += k * (2.0 * float(d_att) + 0.5 * int(c.n) * float(v_att))
+    return total, sum(ks) / max(1, len(ks))
 
 
 # ---- the large-chain workload -------------------------------------------------------
@@ -491,11 +535,9 @@ def run_large(args, rank, world, local_rank):
     d2h = n_tot * 8 + args.chains * 120
 
     traffic = None
-    prof = os.path.join(REPO, "profiles", "domain_kernel_large_chains.md")
-    if os.path.exists(prof):
-        m = re.search(r"dram_bytes_per_particle_phase:\s*([0-9.eE+-]+)", open(prof).read())
-        if m:
-            traffic = float(m.group(1)) * args.chains * args.n / 2
+    fig = profile_figures("domain_kernel_large_chains")
+    if "dram_bytes_per_particle_phase" in fig:
+        traffic = float(fig["dram_bytes_per_particle_phase"]) * args.chains * args.n / 2
     launches_per_step = 3 * S
     launch_ms = total_ms / (args.steps * 2 * S)  # the two domain launches of a sweep dominate
     pairs_per_launch = pairs / (args.steps * 2 * S)
@@ -527,7 +569,7 @@ def run_large(args, rank, world, local_rank):
             "pair_evals_per_launch": pairs_per_launch,
             "flop_per_pair": FLOP_PER_PAIR,
             "mufu_rcp_frac": pairs_per_launch / (launch_ms * 1e-3) / (rcp_peak.value * 1e12),
-            "issue": issue_roofline("domain_kernel_large_chains.md",
+            "issue": issue_roofline("domain_kernel_large_chains",
                                     moves_all / world / (total_ms * 1e-3), clocks, dev),
             "kernel": "domain_kernel (one colour phase of one sweep)",
         },
@@ -765,8 +807,10 @@ def run_ours(args, rank, world, local_rank):
     if args.no_autotune:
         lanes, spr, cpb = 0, 0, 0
     else:
-        # trials of about a millisecond each, so that block sizes whose
-        # difference is a few per cent are told apart
+        # one untimed step first (the GPU at its clocks, the chains off the
+        # lattice), then trials of about a millisecond each, the best of three
+        # runs per shape and the three fastest shapes timed again
+        b.run(args.sweeps_per_step)
         lanes, spr, cpb = b.autotune(trial_sweeps=20 if args.workload == "npt" else 5)
     class_names = {abi.JMM_POT_LJCUT: "ljcut", abi.JMM_POT_SOFTSPHERE: "softsphere",
                    abi.JMM_POT_GAUSS: "gauss"}
@@ -817,6 +861,7 @@ def run_ours(args, rank, world, local_rank):
     for k, c in enumerate(chains):
         x_host[x_off:x_off + c.n] = b.positions(k)
         x_off += c.n
+    alg_pairs, k_mean = algorithmic_pairs(before, after, x_host, chains)
     lbox = after["l"].copy()
     for k, c in enumerate(chains):
         c.l0 = float(lbox[k])
@@ -849,7 +894,11 @@ def run_ours(args, rank, world, local_rank):
     plain = plain_rate(chains[0], args) if args.workload == "npt" and rank == 0 else None
 
     launch_ms = total_ms / args.steps
-    flop_per_launch = pairs / args.steps * FLOP_PER_PAIR
+    # the algorithmic pair evaluations (in-cut-off partners), and the window
+    # slots the kernel evaluates (4W per kept displacement, in-cut-off pairs
+    # of the volume moves)
+    alg_per_launch = alg_pairs / args.steps
+    flop_per_launch = alg_per_launch * FLOP_PER_PAIR
     achieved = flop_per_launch / (launch_ms * 1e-3) / 1e12
     traffic = profile_traffic(args, pairs / args.steps, S) if args.workload == "npt" else None
     line = {
@@ -878,12 +927,19 @@ def run_ours(args, rank, world, local_rank):
             "traffic": traffic,
             "peak_source": "measured live by jmm_measure_peaks (FP32 FMA kernel; "
                            "MEASURED_PEAKS.json holds no FP32 figure)",
-            "pair_evals_per_launch": pairs / args.steps,
+            "pair_evals_per_launch": alg_per_launch,
+            "pair_evals_basis": (f"algorithmic: k = {k_mean:.3f} in-cut-off partners per "
+                                 "particle (mean over chains, positions after the timed "
+                                 "region); 2k pair energies per displacement (old and trial "
+                                 "position), N k / 2 per volume move"),
+            "in_cutoff_partners_k": k_mean,
             "flop_per_pair": FLOP_PER_PAIR,
-            "mufu_rcp_frac": (pairs / args.steps) / (launch_ms * 1e-3) / (rcp_peak.value * 1e12),
-            "pair_evals_per_s": (pairs / args.steps) / (launch_ms * 1e-3),
-            "smem": smem_roofline(pairs / args.steps, launch_ms),
-            "issue": issue_roofline("chains_kernel_batched_npt.md",
+            "mufu_rcp_frac": alg_per_launch / (launch_ms * 1e-3) / (rcp_peak.value * 1e12),
+            "pair_evals_per_s": alg_per_launch / (launch_ms * 1e-3),
+            "window_slots_per_launch": pairs / args.steps,
+            "window_slot_use": alg_per_launch / max(1.0, pairs / args.steps),
+            "smem": smem_roofline(alg_per_launch, launch_ms),
+            "issue": issue_roofline("chains_kernel_batched_npt",
                                     moves_all / world / (total_ms * 1e-3), clocks, dev)
             if args.workload == "npt" else None,
             "kernel": "jmm::batch::chains_kernel",
@@ -943,6 +999,22 @@ def plain_rate(chain, args, steps=20000):
 
 # ---- the reference arm -----------------------------------------------------------
 
+def reference_config(args, cores):
+    """What the reference arm runs: the reference's own move set on the GPU
+    arm's chains, not the GPU arm's moves."""
+    d = config_dict(args, {"parallelism": f"host cores x{cores}"})
+    d["gpu_arm_workload"] = d["workload"]
+    vol = ("linear dL volume moves (max dL = 0.01 N / 0.6) drawn with probability 1/(N+1) "
+           "per step, each an O(N^2) full re-sum (fav)" if args.workload == "npt"
+           else "constant L (NLT)")
+    d["workload"] = (
+        "the reference's move loop (src/jmmMCState.cpp Step / qad2 / fav: FP64, per-pair state, "
+        "all N-1 partners per displacement, " + vol + "; LJcut 3.0 for every chain) on the GPU "
+        "arm's chains (N, T, P), one chain per host core; oracle/plain_oracle.c, which replays "
+        "the reference build's trajectories bit for bit")
+    return d
+
+
 def run_reference(args):
     cfg, chains = workload(args, 0)
     cores = os.cpu_count() or 1
@@ -972,12 +1044,37 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (same chains as the GPU arm)",
-        "config": config_dict(args, {"parallelism": f"host cores x{cores}"}),
+        "config": reference_config(args, cores),
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": samples[-1]["sample"]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+
+
+SUB_WORKLOADS = ("uneven", "grad", "large")
+SUB_KEYS = ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "dtype", "e2e",
+            "roofline", "cpu_baseline", "clocks", "gpu_launches", "sequential", "gradients")
+
+
+def sub_workload_records(args, local_rank):
+    """Compact records of the uneven, gradient and large-chain workloads at
+    their own full sizes, for the one-GPU line: 3 timed steps after 3 warm-up
+    steps (each workload's own step: 500, 200 and 20 sweeps), one e2e step,
+    a 1 s CPU sample."""
+    out = {}
+    for wl in SUB_WORKLOADS:
+        sub = argparse.Namespace(**vars(args))
+        sub.workload, sub.chains, sub.n, sub.sweeps_per_step = wl, 4096, 256, 1000
+        apply_workload_defaults(sub)
+        sub.steps, sub.warmup, sub.e2e_steps, sub.cpu_seconds = 3, 3, 1, 1.0
+        runner = {"large": run_large, "grad": run_grad}.get(wl, run_ours)
+        line = runner(sub, 0, 1, local_rank)
+        rec = {k: line[k] for k in SUB_KEYS if k in line}
+        rec["workload"] = line["config"]["workload"]
+        rec["sweeps_per_step"] = sub.sweeps_per_step
+        out[wl] = rec
+    return out
 
 
 def main():
@@ -997,6 +1094,8 @@ def main():
         torch.distributed.init_process_group("nccl")
     runner = {"large": run_large, "grad": run_grad}.get(args.workload, run_ours)
     line = runner(args, rank, world, local_rank)
+    if world == 1 and args.workload == "npt" and not args.no_sub_workloads:
+        line["workloads"] = sub_workload_records(args, local_rank)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -177,20 +177,43 @@ def test_clock_record_empty(tmp_path):
     assert _sampler_with(tmp_path, [""]).stop()["reasons"] == ["no samples"]
 
 
-def test_profile_traffic_from_committed_summary(monkeypatch):
+def test_profile_traffic_from_committed_figures(monkeypatch):
     """DRAM bytes per launch = chains x (bytes per chain sweep x sweeps +
-    fixed bytes per chain), read from the committed chain-kernel summary."""
+    fixed bytes per chain), from the chain kernel's ncu figures."""
     a = args_for(monkeypatch)
+    fig = bench.profile_figures("chains_kernel_batched_npt")
     t = bench.profile_traffic(a, None, 1000)
     assert t is not None and t > 0
-    assert t == pytest.approx(a.chains * (0.0 * 1000 + 1270))
+    assert t == pytest.approx(a.chains * (fig["dram_bytes_per_chain_sweep"] * 1000
+                                          + fig["dram_bytes_per_chain_launch_fixed"]))
 
 
-@pytest.mark.parametrize("profile", ["chains_kernel_batched_npt.md",
-                                     "domain_kernel_large_chains.md"])
-def test_issue_roofline_from_committed_summary(monkeypatch, profile):
-    """Issue-slot roofline: instructions per move from the committed ncu
-    summary x moves/s against 4 issue slots per SM per clock."""
+def test_figures_name_committed_summaries():
+    """Every kernel in profiles/figures.json names a committed ncu summary."""
+    with open(bench.FIGURES) as f:
+        figures = json.load(f)
+    assert figures
+    for kernel, fig in figures.items():
+        assert os.path.exists(os.path.join(REPO, fig["summary"])), kernel
+        assert fig["warp_instructions_per_move"] > 0
+
+
+def test_in_cutoff_neighbours():
+    """k: partners within the cut-off per particle, both sides, inclusive."""
+    import numpy as np
+    x = np.array([0.0, 1.0, 2.0, 3.5, 10.0])
+    # rc = 2: pairs (0,1) (0,2) (1,2) (2,3) -> 4 pairs, k = 8 / 5
+    assert bench.in_cutoff_neighbours(x, [5], 2.0) == pytest.approx(1.6)
+    # two chains back to back, per-chain cut-offs: rc = 1 adds (0,1) (1,2)
+    both = np.concatenate([x, x])
+    assert bench.in_cutoff_neighbours(both, [5, 5], [2.0, 1.0]) == pytest.approx(12.0 / 10)
+
+
+@pytest.mark.parametrize("profile", ["chains_kernel_batched_npt",
+                                     "domain_kernel_large_chains"])
+def test_issue_roofline_from_committed_figures(monkeypatch, profile):
+    """Issue-slot roofline: instructions per move from the kernel's ncu
+    figures x moves/s against 4 issue slots per SM per clock."""
     import torch
 
     class Props:
@@ -203,7 +226,7 @@ def test_issue_roofline_from_committed_summary(monkeypatch, profile):
     assert r["frac"] == pytest.approx(r["instructions_per_move"] * 2.0e10 / r["peak"])
     assert 0 < r["frac"] < 1.2
     assert bench.issue_roofline(profile, 1.0, {}, 0) is None  # no clock record
-    assert bench.issue_roofline("no_such_profile.md", 1.0, {"sm_mhz": 1.0}, 0) is None
+    assert bench.issue_roofline("no_such_kernel", 1.0, {"sm_mhz": 1.0}, 0) is None
 
 
 def test_smem_roofline():
