@@ -499,7 +499,9 @@ int jmm_rng_words(uint64_t seed, uint64_t block0, uint32_t chain, uint64_t count
  * sized for N <= 256 (2.35 MB per GPU, held until exit): larger N fails with
  * JMM_ERR_INVALID, and calls that overlap on the GPU race on that array.
  * The first call on a device looks the array's address up; make it before
- * any stream capture. */
+ * any stream capture.  JMM_ERR_INVALID also for a box length that is not
+ * finite and positive, and for r or out that are not device (or managed)
+ * memory of the current device. */
 int jmm_plain_full_energy_noalloc(const jmm_params *params, const double *r, uint64_t n,
                                   double l, double *out, void *stream);
 

@@ -138,6 +138,27 @@ extern "C" int jmm_plain_full_energy_noalloc(const jmm_params *params, const dou
   JMM_CHECK_ARG(params->potential == JMM_POT_LJCUT || params->potential == JMM_POT_LJ ||
                     params->potential == JMM_POT_HARMONIC,
                 "potential must be LJcut, LJ or HARMONIC");
+  JMM_CHECK_ARG(isfinite(l) && l > 0.0, "the box length must be finite and positive");
+  // r and out must be device (or managed) memory of the current device: a
+  // host or another device's pointer is refused here rather than faulting in
+  // the kernel (querying attributes allocates nothing)
+  int dev = 0;
+  JMM_CUDA(cudaGetDevice(&dev));
+  for (const void *ptr : {(const void *)r, (const void *)out}) {
+    cudaPointerAttributes at;
+    const cudaError_t e = cudaPointerGetAttributes(&at, ptr);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return jmm::fail(JMM_ERR_INVALID, "jmm_plain_full_energy_noalloc: %p is not device memory",
+                       ptr);
+    }
+    const bool ok = (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) &&
+                    at.device == dev;
+    if (!ok)
+      return jmm::fail(JMM_ERR_INVALID,
+                       "jmm_plain_full_energy_noalloc: %p is not device memory of device %d", ptr,
+                       dev);
+  }
   double *terms = nullptr;
   int rc = terms_address(&terms);
   if (rc) return rc;

@@ -66,3 +66,17 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_native, "_lib", None)
     with pytest.raises(ImportError):
         _native.load()
+
+
+def test_noalloc_refuses_bad_box_before_any_device_work(native):
+    """The allocation-free entry point checks its scalar arguments on the
+    host first: a box length that is not finite and positive is refused
+    without touching the (here absent) device or the pointers."""
+    fn = native.jmm_plain_full_energy_noalloc
+    fn.argtypes = [C.POINTER(abi.Params), C.c_void_p, C.c_uint64, C.c_double, C.c_void_p,
+                   C.c_void_p]
+    fn.restype = C.c_int
+    params = abi.make_params(n=16, l=32.0)
+    fake = C.c_void_p(256)  # never dereferenced: the check comes first
+    for l in (float("nan"), 0.0, -2.0, float("inf")):
+        assert fn(C.byref(params), fake, 16, l, fake, None) == abi.JMM_ERR_INVALID

@@ -64,6 +64,10 @@ def test_noalloc_full_energy_matches_existing_path(gpu):
         abi.make_params(n=64, l=64 / 0.6, t=0.8, potential=abi.JMM_POT_LJ, nbn=3, max_step=0.3,
                         seed=9),
         abi.make_params(n=MAX_N, l=MAX_N / 0.7, t=1.2, cutoff=2.5, max_step=0.2, seed=5),
+        # HARMONIC with a neighbour limit (the golden npt10_harmonic_nbn1 kind):
+        # its virial divides by L; both paths leave phi[2..8] at 0
+        abi.make_params(n=10, ensemble=abi.JMM_NPT, potential=abi.JMM_POT_HARMONIC, p=1.0,
+                        t=1.0, cutoff=2.0, nbn=1, max_step=0.3, max_dl=0.5, seed=7),
     ]
     for params in cases:  # consecutive calls share the staging array
         r, l = _chain_positions(params, 3000)
@@ -81,3 +85,23 @@ def test_noalloc_rejects_sizes_beyond_its_array(gpu):
     rc = _entry(lib)(C.byref(params), r.data_ptr(), MAX_N + 1, 400.0, out.data_ptr(), None)
     assert rc == abi.JMM_ERR_INVALID
     assert b"exceeds" in lib.jmm_last_error()
+
+
+def test_noalloc_refuses_host_memory_and_bad_box(gpu):
+    """Pinned host buffers (which a kernel could read, so the check is what
+    refuses them) and a box length that is not finite and positive are
+    refused before any launch."""
+    import torch
+    lib = _native.load()
+    params = abi.make_params(n=16, l=32.0)
+    r_dev = torch.linspace(-15.0, 15.0, 16, dtype=torch.float64, device="cuda")
+    out_dev = torch.empty(9, dtype=torch.float64, device="cuda")
+    r_host = r_dev.cpu().pin_memory()
+    out_host = torch.empty(9, dtype=torch.float64).pin_memory()
+    for r, out in ((r_host, out_dev), (r_dev, out_host)):
+        rc = _entry(lib)(C.byref(params), r.data_ptr(), 16, 32.0, out.data_ptr(), None)
+        assert rc == abi.JMM_ERR_INVALID
+        assert b"device memory" in lib.jmm_last_error()
+    for l in (float("nan"), 0.0, -1.0, float("inf")):
+        rc = _entry(lib)(C.byref(params), r_dev.data_ptr(), 16, l, out_dev.data_ptr(), None)
+        assert rc == abi.JMM_ERR_INVALID
