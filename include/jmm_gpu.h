@@ -273,7 +273,20 @@ typedef struct jmm_batch_config {
                                 before it extends its window: 0 = max(4, G/2);
                                 8 with the shapes 2x16, 4x8 and 8x4, 3 with
                                 2x16                                           */
-  uint32_t reserved;         /* 0                                               */
+  uint32_t split_n;          /* 0, or at least 64: constant-L chains between
+                                walls with split_n or more particles run
+                                split, one block of up to 8 warps per chain:
+                                per sweep the chain is cut into domains of
+                                B = max(32, 32 ceil(N / 480)) particles from a
+                                random offset, and the domains of one colour
+                                make their steps at once, one warp each, then
+                                the other colour (detailed balance as the
+                                large chains' alternating-domain sweep); each
+                                domain runs 4 lanes x 8 steps per round with a
+                                window of 4, or 8 / 16 where the class's
+                                window is wider.  A split chain's statistics
+                                sample once per sweep (samples count sweeps).
+                                NPT chains and rings always run whole.         */
 } jmm_batch_config;
 
 /* Per-chain state and statistics, FP64 (also the device-side record). */

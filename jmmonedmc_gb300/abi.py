@@ -172,7 +172,7 @@ class BatchConfig(C.Structure):
         ("init", C.c_int32),
         ("jitter", C.c_double),
         ("window", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("split_n", C.c_uint32),
     ]
 
 
@@ -232,7 +232,8 @@ def make_chain(n, potential=JMM_POT_LJCUT, ensemble=JMM_NLT, eps=1.0, sigma=1.0,
 def make_batch_config(seed=1, boundary=JMM_BOUNDARY_WALLS, vol_move=JMM_VOLMOVE_LNL,
                       vol_schedule=JMM_VOLSCHED_SWEEP, precision=JMM_PREC_FAST,
                       resum_sweeps=100, lanes_per_chain=0, steps_per_round=0,
-                      chains_per_block=0, init=JMM_INIT_LATTICE, jitter=0.0, window=0):
+                      chains_per_block=0, init=JMM_INIT_LATTICE, jitter=0.0, window=0,
+                      split_n=0):
     c = BatchConfig()
     c.seed = seed
     c.boundary = boundary
@@ -246,6 +247,7 @@ def make_batch_config(seed=1, boundary=JMM_BOUNDARY_WALLS, vol_move=JMM_VOLMOVE_
     c.init = init
     c.jitter = jitter
     c.window = window
+    c.split_n = split_n
     return c
 
 

@@ -67,6 +67,38 @@ ChainsKernel pick_kernel(uint32_t g, uint32_t s, uint32_t w, bool exact, int pot
 
 constexpr int kPots[3] = {JMM_POT_LJCUT, JMM_POT_SOFTSPHERE, JMM_POT_GAUSS};
 
+// Split chains (split_kernel): 4 lanes x 8 steps per round per domain, a
+// window of 4, 8 or 16 neighbours per side.
+template <bool E, int WIN>
+ChainsKernel pick_split_pot(int pot) {
+  switch (pot) {
+    case JMM_POT_LJCUT: return split_kernel<4, 8, JMM_POT_LJCUT, E, WIN>;
+    case JMM_POT_SOFTSPHERE: return split_kernel<4, 8, JMM_POT_SOFTSPHERE, E, WIN>;
+    case JMM_POT_GAUSS: return split_kernel<4, 8, JMM_POT_GAUSS, E, WIN>;
+    default: return nullptr;
+  }
+}
+
+ChainsKernel pick_split(uint32_t w, bool exact, int pot) {
+  switch (w) {
+    case 4: return exact ? pick_split_pot<true, 4>(pot) : pick_split_pot<false, 4>(pot);
+    case 8: return exact ? pick_split_pot<true, 8>(pot) : pick_split_pot<false, 8>(pot);
+    case 16: return exact ? pick_split_pot<true, 16>(pot) : pick_split_pot<false, 16>(pot);
+    default: return nullptr;
+  }
+}
+
+// A chain that runs split: the batch asks for it (split_n) and the chain has
+// constant L between walls and at least split_n particles.
+bool is_split(const jmm_batch_config &cfg, const jmm_chain_desc &c) {
+  return cfg.split_n > 0 && c.n >= cfg.split_n && c.ensemble == JMM_NLT &&
+         cfg.boundary == JMM_BOUNDARY_WALLS;
+}
+
+// The window of a potential class's split chains from the class's window:
+// 8 or 16 where the class needs more than 4 neighbours per side, else 4.
+uint32_t split_window(uint32_t w) { return w > 8 ? 16u : (w > 4 ? 8u : 4u); }
+
 // The chains of one potential: a contiguous range of launch slots with its
 // own blocks and shared-memory size.
 // A launch shape: G window lanes x S steps per round, chains per block, W
@@ -81,7 +113,11 @@ struct PotClass {
   uint32_t first, count;
   uint32_t n_blocks;
   size_t smem;
+  bool split = false;   // split chains: one block of `warps` warps per chain
+  uint32_t warps = 0;
 };
+
+constexpr int kMaxClasses = 6;  // three potentials, each whole and split
 
 uint64_t pad4(uint64_t n) { return (n + 3) & ~uint64_t(3); }
 
@@ -106,8 +142,8 @@ struct jmm_batch {
   cudaStream_t stream = nullptr;
   std::map<uint64_t, cudaGraphExec_t> graphs;  // n_sweeps -> instantiated run
   std::vector<PotClass> classes;
-  cudaStream_t side[3] = {nullptr, nullptr, nullptr};  // concurrent classes in a graph
-  cudaEvent_t fork = nullptr, join[3] = {nullptr, nullptr, nullptr};
+  cudaStream_t side[kMaxClasses] = {};  // concurrent classes in a graph
+  cudaEvent_t fork = nullptr, join[kMaxClasses] = {};
   // energy gradients and their sampled statistics
   jmm_chain_desc *d_desc = nullptr;     // user order
   uint64_t *d_xoff = nullptr;           // user order
@@ -135,7 +171,7 @@ static void batch_free(jmm_batch *b) {
   drop_graphs(b);
   cudaFree(b->d_block);  // every device array of the batch
   cudaFree(b->d_hist);
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < kMaxClasses; ++k) {
     if (b->side[k]) cudaStreamDestroy(b->side[k]);
     if (b->join[k]) cudaEventDestroy(b->join[k]);
   }
@@ -172,8 +208,71 @@ static int apply_layout(jmm_batch *b, const Shape shapes[3]) {
   std::vector<ChainParams> prm(b->n_chains);
   std::vector<PotClass> classes;
   uint32_t slot0 = 0;
+  // the chain parameters every launch takes
+  auto fill = [&](uint32_t slot, uint32_t s_off) {
+    const uint32_t id = b->order[slot];
+    const jmm_chain_desc &c = b->chains[id];
+    ChainParams &P = prm[slot];
+    memset(&P, 0, sizeof(P));
+    P.id = id;
+    P.n = c.n;
+    P.pot = (uint32_t)c.potential;
+    P.ensemble = (uint32_t)c.ensemble;
+    P.steps_per_sweep = c.ensemble == JMM_NPT ? c.n + 1 : c.n;
+    P.s_off = s_off;
+    P.x_off = b->x_off[id];
+    P.eps4 = c.potential == JMM_POT_LJCUT ? (float)(4.0 * c.eps) : (float)c.eps;
+    P.sigma2 = (float)(c.sigma * c.sigma);
+    P.inv_sigma2 = (float)(1.0 / (c.sigma * c.sigma));
+    P.rc2 = (float)(c.cutoff * c.cutoff);
+    P.rc = (float)c.cutoff;
+    P.beta = (float)(1.0 / c.t);
+    P.beta_d = 1.0 / c.t;
+    P.p = c.p;
+    P.two_max_step = (float)(2.0 * c.max_step);
+    P.vol_step = (float)c.vol_step;
+  };
   for (int pi = 0; pi < 3; ++pi) {
     const int pot = kPots[pi];
+    // split chains of this potential: the leading ones in launch order, one
+    // block each, as many warps as the largest one's colour has domains
+    {
+      PotClass sc;
+      sc.pot = pot;
+      sc.shape = Shape{4, 8, 1, split_window(shapes[pi].w ? shapes[pi].w
+                                                            : (uint32_t)window_of((int)shapes[pi].g))};
+      sc.first = slot0;
+      sc.count = 0;
+      sc.split = true;
+      sc.warps = 1;
+      sc.smem = 0;
+      while (slot0 + sc.count < b->n_chains) {
+        const jmm_chain_desc &c = b->chains[b->order[slot0 + sc.count]];
+        if (c.potential != pot || !is_split(b->cfg, c)) break;
+        const uint32_t dom = split_domain_size(c.n);
+        const uint32_t per_colour = (c.n / dom + 2u + 1u) / 2u;
+        sc.warps = std::max(sc.warps, std::min(kSplitWarps, per_colour));
+        fill(slot0 + sc.count, 0);
+        prm[slot0 + sc.count].dom = dom;
+        sc.count++;
+      }
+      if (sc.count) {
+        for (uint32_t k = 0; k < sc.count; ++k)
+          sc.smem = std::max(sc.smem,
+                             (size_t)split_smem_bytes(prm[sc.first + k].n, sc.warps));
+        // the kernel's own static shared memory (per-warp tallies) comes on top
+        if (sc.smem + 1024 > kMaxSmem)
+          return fail(JMM_ERR_INVALID, "a split chain needs %zu bytes of shared memory (max %zu)",
+                      sc.smem, kMaxSmem - 1024);
+        sc.n_blocks = sc.count;
+        ChainsKernel kf = pick_split(sc.shape.w, exact, pot);
+        if (sc.smem > 48 * 1024)
+          JMM_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sc.smem));
+        classes.push_back(sc);
+        slot0 += sc.count;
+      }
+    }
     const uint32_t g = shapes[pi].g, spr = shapes[pi].spr, cpb = shapes[pi].cpb;
     const uint32_t win = shapes[pi].w ? shapes[pi].w : (uint32_t)window_of((int)g);
     if (!pick_kernel(g, spr, win, false, JMM_POT_LJCUT, false))
@@ -203,28 +302,8 @@ static int apply_layout(jmm_batch *b, const Shape shapes[3]) {
       for (uint32_t k = 0; k < cpb; ++k) {
         const uint32_t local = blk * cpb + k;
         if (local >= pc.count) break;
-        const uint32_t id = b->order[pc.first + local];
-        const jmm_chain_desc &c = b->chains[id];
-        ChainParams &P = prm[pc.first + local];
-        memset(&P, 0, sizeof(P));
-        P.id = id;
-        P.n = c.n;
-        P.pot = (uint32_t)c.potential;
-        P.ensemble = (uint32_t)c.ensemble;
-        P.steps_per_sweep = c.ensemble == JMM_NPT ? c.n + 1 : c.n;
-        P.s_off = (uint32_t)s_off;
-        P.x_off = b->x_off[id];
-        P.eps4 = c.potential == JMM_POT_LJCUT ? (float)(4.0 * c.eps) : (float)c.eps;
-        P.sigma2 = (float)(c.sigma * c.sigma);
-        P.inv_sigma2 = (float)(1.0 / (c.sigma * c.sigma));
-        P.rc2 = (float)(c.cutoff * c.cutoff);
-        P.rc = (float)c.cutoff;
-        P.beta = (float)(1.0 / c.t);
-        P.beta_d = 1.0 / c.t;
-        P.p = c.p;
-        P.two_max_step = (float)(2.0 * c.max_step);
-        P.vol_step = (float)c.vol_step;
-        s_off += pad4(c.n + 2 * kGhost);
+        fill(pc.first + local, (uint32_t)s_off);
+        s_off += pad4(b->chains[b->order[pc.first + local]].n + 2 * kGhost);
       }
       pc.smem = std::max(pc.smem, (size_t)s_off * sizeof(float));
     }
@@ -248,7 +327,7 @@ static int apply_layout(jmm_batch *b, const Shape shapes[3]) {
     if (!b->shapes[pi].w) b->shapes[pi].w = (uint32_t)window_of((int)shapes[pi].g);
   }
   for (const PotClass &pc : b->classes) {
-    if (pc.count > most) {
+    if (!pc.split && pc.count > most) {
       most = pc.count;
       b->g = pc.shape.g;
       b->spr = pc.shape.spr;
@@ -308,6 +387,12 @@ static int launch_class(jmm_batch *b, size_t k, uint64_t n_sweeps, cudaStream_t 
   kc.n_chains = pc.count;
   const bool per = b->cfg.boundary == JMM_BOUNDARY_PERIODIC;
   const bool exact = b->cfg.precision == JMM_PREC_EXACT;
+  if (pc.split) {
+    ChainsKernel kf = pick_split(pc.shape.w, exact, pc.pot);
+    kf<<<pc.n_blocks, 32 * pc.warps, pc.smem, st>>>(b->d_params + pc.first, b->d_res, b->d_x, kc);
+    JMM_CUDA(cudaGetLastError());
+    return JMM_OK;
+  }
   const uint32_t threads = pc.shape.g * pc.shape.spr * pc.shape.cpb;
   ChainsKernel kf = pick_kernel(pc.shape.g, pc.shape.spr, pc.shape.w, exact, pc.pot, per);
   kf<<<pc.n_blocks, threads, pc.smem, st>>>(b->d_params + pc.first, b->d_res, b->d_x, kc);
@@ -359,6 +444,8 @@ static int validate(const jmm_batch_config *cfg, const jmm_chain_desc *chains, u
                 "unknown volume schedule");
   JMM_CHECK_ARG(cfg->precision == JMM_PREC_FAST || cfg->precision == JMM_PREC_EXACT,
                 "unknown precision");
+  JMM_CHECK_ARG(cfg->split_n == 0 || cfg->split_n >= 64,
+                "split_n must be 0 (no split chains) or at least 64");
   if (cfg->lanes_per_chain) {
     const uint32_t g = cfg->lanes_per_chain;
     const uint32_t spr = cfg->steps_per_round ? cfg->steps_per_round : (g <= 32 ? 32 / g : 1);
@@ -504,11 +591,13 @@ static int batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chain
   std::iota(b->order.begin(), b->order.end(), 0u);
   std::stable_sort(b->order.begin(), b->order.end(), [&](uint32_t a, uint32_t c) {
     if (chains[a].potential != chains[c].potential) return chains[a].potential < chains[c].potential;
+    const bool sa = is_split(*cfg, chains[a]), sc = is_split(*cfg, chains[c]);
+    if (sa != sc) return sa;
     return chains[a].n > chains[c].n;
   });
 
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
-  for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+  for (int k = 0; k < kMaxClasses && e == cudaSuccess; ++k) {
     e = cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming);
   }

@@ -73,6 +73,7 @@ struct ChainParams {
   float rc;
   float grid;                // domain sweeps: position grid step 2^-k, displacements
                              // snapped to it; 0 (unused) for whole chains
+  uint32_t dom;              // split chains: domain size B; 0 for whole chains
   double beta_d, p;
 };
 
@@ -419,8 +420,13 @@ __host__ __device__ constexpr unsigned leader_bits(int g, int s) {
 }
 
 // One chain for one launch: n_sweeps sweeps in speculative rounds of S steps.
-template <int G, int S, int POT, bool PER, bool kExact, bool HALO = false, int WIN = window_of(G)>
-__device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result *__restrict__ res,
+// rp is the chain's record (state and statistics); P.id keys its Philox
+// stream.  HALO: the chain is one domain of a longer chain, whose neighbouring
+// particles fill the kGhost slots on each side; SNAP: trial displacements are
+// snapped to the position grid P.grid (large chains' integer positions).
+template <int G, int S, int POT, bool PER, bool kExact, bool HALO = false, int WIN = window_of(G),
+          bool SNAP = HALO>
+__device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result *__restrict__ rp,
                                           float *__restrict__ xg, float *xs, uint32_t *ring,
                                           const KernelCfg &cfg, int cl, unsigned gmask) {
   constexpr int W = WIN;            // neighbours looked at on each side
@@ -468,7 +474,6 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
   H.beta = P.beta;
   H.two_max_step = P.two_max_step;
 
-  jmm_chain_result *rp = res + P.id;
   const bool npt = P.ensemble == JMM_NPT;
   const bool per_sweep = cfg.vol_schedule == JMM_VOLSCHED_SWEEP;
   double L_box = rp->l;
@@ -482,7 +487,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
   g.nseg = 0;
   constexpr bool kShares = !kExact && S > 1;
   float sd_loc = 0.0f, sd2_loc = 0.0f;  // this lane's shares (kShares)
-  const float inv_grid = HALO ? __frcp_rn(P.grid) : 0.0f;
+  const float inv_grid = SNAP ? __frcp_rn(P.grid) : 0.0f;
   const uint32_t spsw = P.steps_per_sweep;
   const uint64_t step0 = rp->steps;
   uint32_t sweep_pos = (uint32_t)(step0 % spsw);
@@ -516,7 +521,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
             nm_e = n;  // the sweep's volume step
         }
         float md_e = __fmul_rn(__fsub_rn(u1, 0.5f), H.two_max_step);
-        if (HALO) md_e = __fmul_rn(rintf(__fmul_rn(md_e, inv_grid)), P.grid);  // exact: 2^k scales
+        if (SNAP) md_e = __fmul_rn(rintf(__fmul_rn(md_e, inv_grid)), P.grid);  // exact: 2^k scales
         ring_rec[e] = make_uint4((uint32_t)nm_e, __float_as_uint(nm_e == n ? u1 : md_e),
                                  __float_as_uint(threshold_of<kExact>(w.w[2])), 0u);
       }
@@ -795,7 +800,198 @@ __global__ void __maxnreg__(G * S == 32 ? 72 : 128) chains_kernel(const ChainPar
   __syncwarp(gmask);
   set_ghosts<PER>(xs, (int)P.n, (float)res[P.id].l, cl, L);
   __syncwarp(gmask);
-  run_chain<G, S, POT, PER, kExact, false, WIN>(P, res, xg, xs, ring, cfg, cl, gmask);
+  run_chain<G, S, POT, PER, kExact, false, WIN>(P, res + P.id, xg, xs, ring, cfg, cl, gmask);
+}
+
+// ---- split chains: one chain's sweep over several warps ---------------------
+//
+// A long constant-L chain between walls runs as one block of M warps.  Per
+// sweep its index range is cut into domains of B particles from a random
+// offset o in [0, B) -- domain d = [o + (d-1)B, o + dB) clipped to [0, N) --
+// and the domains of one colour (d even or d odd; which colour first drawn
+// per sweep) make their steps at the same time, one warp each, on the
+// chain's positions in shared memory, then the other colour, with a block
+// barrier between.  A domain is the batched step loop (run_chain with HALO)
+// on its own particles, its 16 neighbours on each side frozen for the phase.
+// Two active domains are separated by a frozen interior domain of B >= 32
+// particles, and a domain runs only if the 16th frozen neighbour on each
+// interior side lies beyond the cut-off from the first (else it is skipped
+// and the chain flagged JMM_ERR_INVALID), so active domains share no pair: a
+// phase is a product of independent Metropolis chains on the conditional
+// distribution of each domain given the rest, which leaves the Boltzmann
+// distribution invariant; the random offset and colour make the layout
+// itself random.  Domains of one phase share no pair, so the order in which
+// they run does not change a bit of the result.
+//
+// Domain [lo, hi) of a sweep takes the chain's Philox blocks steps + lo + 1
+// .. steps + hi (steps counted before the sweep), so a sweep draws the N
+// blocks a whole sweep would, and the layout comes from the fourth word
+// (unused by a step) of block steps + 1: offset from its high bits, colour
+// from its lowest.  Each domain's energy change is summed in FP32 over its
+// steps; after the sweep the chain's FP64 energy takes the domains' changes
+// in index order, and the statistics sample the energy once per sweep
+// (samples count sweeps).  Constant-L chains re-sum every resum_sweeps
+// sweeps over the whole chain (32 lanes of warp 0).
+
+constexpr uint32_t kSplitWarps = 8;  // warps of a split chain's block, at most
+
+// B for a chain of n particles: a multiple of 32 of at least 2 kGhost, and
+// at least n / 15, so that a sweep has at most 16 non-empty domains and a
+// colour at most kSplitWarps.
+__host__ __device__ constexpr uint32_t split_domain_size(uint32_t n) {
+  return 32u * ((n + 479u) / 480u) < 2u * (uint32_t)kGhost ? 2u * (uint32_t)kGhost
+                                                          : 32u * ((n + 479u) / 480u);
+}
+
+// Shared memory of a split chain's block: per warp a step ring and a domain
+// record, the domains' energy changes, then the positions with their ghosts.
+__host__ __device__ constexpr uint64_t split_smem_bytes(uint32_t n, uint32_t warps) {
+  return (uint64_t)warps * (kRingWords * 4u + sizeof(jmm_chain_result)) +
+         8u * (uint64_t)(n / split_domain_size(n) + 2u) + 4u * ((uint64_t)n + 2u * kGhost);
+}
+
+template <int G, int S, int POT, bool kExact, int WIN>
+__global__ void __maxnreg__(72) split_kernel(const ChainParams *__restrict__ prm,
+                                             jmm_chain_result *__restrict__ res,
+                                             float *__restrict__ xg, KernelCfg cfg) {
+  static_assert(G * S == 32, "one warp per domain");
+  extern __shared__ __align__(16) float smem[];
+  __shared__ unsigned long long tally[kSplitWarps][4];  // accepted, attempted, pairs, overflows
+  __shared__ uint32_t tally_err[kSplitWarps];
+  if (blockIdx.x >= cfg.n_chains) return;
+  const uint32_t nwarps = blockDim.x >> 5, warp = threadIdx.x >> 5;
+  const int cl = threadIdx.x & 31;
+  const ChainParams P = prm[blockIdx.x];
+  const int n = (int)P.n;
+  const uint32_t B = P.dom;
+  uint32_t *ring = reinterpret_cast<uint32_t *>(smem) + warp * kRingWords;
+  jmm_chain_result *drec =
+      reinterpret_cast<jmm_chain_result *>(reinterpret_cast<uint32_t *>(smem) + nwarps * kRingWords);
+  double *dde = reinterpret_cast<double *>(drec + nwarps);  // n / B + 2 domains at most
+  float *xs = reinterpret_cast<float *>(dde + (n / (int)B + 2)) + kGhost;
+  jmm_chain_result *rp = res + P.id;
+  const double L = rp->l;
+  const float lf = (float)L;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = xg[P.x_off + i];
+  if (warp == 0) set_ghosts<false>(xs, n, lf, cl, 32);
+  unsigned long long acc = 0, att = 0, pairs = 0, ovf = 0;
+  uint32_t err = 0;
+  uint64_t steps = rp->steps;
+  double e = rp->e;  // thread 0's running energy
+  const double rho = __ddiv_rn((double)n, L);
+  KernelCfg dcfg = cfg;  // one pass over a domain, no re-summation inside
+  dcfg.n_sweeps = 1;
+  dcfg.resum_sweeps = 0;
+  ChainParams Pd = P;
+  Pd.ensemble = JMM_NLT;
+  uint32_t since_resum = 0;
+  __syncthreads();
+  for (uint64_t sw = 0; sw < cfg.n_sweeps; ++sw) {
+    const Words4 lw = step_words(cfg.seed, steps + 1, P.id);
+    const int off = (int)word_to_index(lw.w[3], (uint64_t)B);
+    const uint32_t first = lw.w[3] & 1u;
+    const int n_dom = (n - off + (int)B - 1) / (int)B + 1;
+    for (int phase = 0; phase < 2; ++phase) {
+      const int colour = (int)((first + (uint32_t)phase) & 1u);
+      for (int d = colour + 2 * (int)warp; d < n_dom; d += 2 * (int)nwarps) {
+        const int lo = max(0, off + (d - 1) * (int)B);
+        const int hi = min(n, off + d * (int)B);
+        double de_d = 0.0;
+        if (hi > lo) {
+          // the 16th frozen neighbour beyond each interior edge lies beyond
+          // the cut-off (where the chain goes on past the halo)
+          bool fits = true;
+          if (lo >= kGhost) fits = fits && __fsub_rn(xs[lo - 1], xs[lo - kGhost]) > P.rc;
+          if (hi + kGhost <= n) fits = fits && __fsub_rn(xs[hi + kGhost - 1], xs[hi]) > P.rc;
+          if (!fits) {
+            err |= JMM_ERR_INVALID;
+          } else {
+            jmm_chain_result *dr = drec + warp;
+            if (cl == 0) {
+              memset(dr, 0, sizeof(jmm_chain_result));
+              dr->l = L;
+              dr->steps = steps + (uint64_t)lo;
+            }
+            __syncwarp();
+            Pd.n = (uint32_t)(hi - lo);
+            Pd.steps_per_sweep = (uint32_t)(hi - lo);
+            run_chain<G, S, POT, false, kExact, true, WIN, false>(Pd, dr, nullptr, xs + lo, ring,
+                                                                  dcfg, cl, 0xffffffffu);
+            __syncwarp();
+            de_d = dr->e;
+            acc += dr->disp_acc;
+            att += dr->disp_att;
+            pairs += dr->pair_evals;
+            ovf += dr->window_overflows;
+            err |= dr->error;
+            __syncwarp();
+          }
+        }
+        if (cl == 0) dde[d] = de_d;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      for (int d = 0; d < n_dom; ++d) e = __dadd_rn(e, dde[d]);
+      rp->sum_e = __dadd_rn(rp->sum_e, e);
+      rp->sum_e2 = __dadd_rn(rp->sum_e2, __dmul_rn(e, e));
+      rp->sum_l = __dadd_rn(rp->sum_l, L);
+      rp->sum_l2 = __dadd_rn(rp->sum_l2, __dmul_rn(L, L));
+      rp->sum_le = __dadd_rn(rp->sum_le, __dmul_rn(L, e));
+      rp->sum_rho = __dadd_rn(rp->sum_rho, rho);
+      rp->sum_rho2 = __dadd_rn(rp->sum_rho2, __dmul_rn(rho, rho));
+      rp->samples += 1;
+    }
+    steps += (uint64_t)n;
+    if (cfg.resum_sweeps > 0 && ++since_resum >= (uint32_t)cfg.resum_sweeps) {
+      since_resum = 0;
+      if (warp == 0) {
+        Hot H;
+        H.eps4 = P.eps4;
+        H.sigma2 = P.sigma2;
+        H.inv_sigma2 = P.inv_sigma2;
+        H.rc2 = P.rc2;
+        H.beta = P.beta;
+        H.two_max_step = P.two_max_step;
+        double uo, un;
+        uint64_t rpairs = 0;
+        uint32_t rerr = 0;
+        chain_energies<32, POT, false, kExact, false>(xs, H, n, cl, 0xffffffffu, lf, 1.0f, lf, uo,
+                                                      un, rpairs, rerr);
+        if (cl == 0) {
+          const double drift = fabs(__dsub_rn(e, uo));
+          if (drift > rp->max_drift) rp->max_drift = drift;
+          e = uo;
+          pairs += rpairs;
+          err |= rerr;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) xg[P.x_off + i] = xs[i];
+  if (cl == 0) {
+    tally[warp][0] = acc;
+    tally[warp][1] = att;
+    tally[warp][2] = pairs;
+    tally[warp][3] = ovf;
+    tally_err[warp] = err;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t e_all = rp->error;
+    for (uint32_t w = 0; w < nwarps; ++w) {
+      rp->disp_acc += tally[w][0];
+      rp->disp_att += tally[w][1];
+      rp->pair_evals += tally[w][2];
+      rp->window_overflows += (uint32_t)tally[w][3];
+      e_all |= tally_err[w];
+    }
+    if (!isfinite(e)) e_all |= JMM_ERR_NUMERIC;
+    rp->e = e;
+    rp->steps = steps;
+    rp->error = e_all;
+  }
 }
 
 // Fresh FP64 energies of every chain (32 lanes per chain).

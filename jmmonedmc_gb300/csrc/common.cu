@@ -19,6 +19,9 @@ void clear_error() { g_last_error[0] = '\0'; }
 
 int cuda_status(cudaError_t e, const char *what, const char *file, int line) {
   int code = (e == cudaErrorMemoryAllocation) ? JMM_ERR_NOMEM : JMM_ERR_CUDA;
+  // a failed call leaves its (non-sticky) error as the runtime's last error:
+  // clear it, so that a later launch check does not report it again
+  cudaGetLastError();
   return fail(code, "%s failed at %s:%d: %s (%s)", what, file, line, cudaGetErrorName(e),
               cudaGetErrorString(e));
 }

@@ -194,7 +194,8 @@ __global__ void __maxnreg__(72)
   if (cl == 0) rp->l = (left_wall || right_wall) ? __dmul_rn(2.0, (double)q_to_f(H, ch.grid)) : 2e30;
   __syncwarp();
   const ChainParams P = domain_params(ch, ch.rec0 + d, (uint32_t)n);
-  run_chain<kG, kS, POT, false, false, true, WIN>(P, rec, nullptr, xs, ring, cfg, cl, 0xffffffffu);
+  run_chain<kG, kS, POT, false, false, true, WIN>(P, rec + P.id, nullptr, xs, ring, cfg, cl,
+                                                  0xffffffffu);
   __syncwarp();
   const float inv_grid = __frcp_rn(ch.grid);
   for (int i = cl; i < n; i += 32) qc[i] = O + __float2ll_rn(__fmul_rn(xs[i], inv_grid));

@@ -231,6 +231,86 @@ static double threshold64(uint32_t w) {
 }
 
 /* One launch of n_sweeps for one chain. */
+/* One displacement step of the FP32 chain (the EXACT kernel's arithmetic):
+ * particle nm of xs[0..n) with the step's Philox words w, G window lanes of
+ * W neighbours per side; moves the particle when accepted and returns the
+ * accepted energy change (0 when rejected).  Counts accepted moves, window
+ * extensions and window pair slots. */
+static float disp32(float *xs, int n, int nm, const uint32_t w[4], const chain_prm *P,
+                    int periodic, float lf, float half_l, uint32_t G, uint32_t W, uint64_t *pairs,
+                    uint32_t *err, jmm_chain_result *R) {
+  const float u1 = (float)(w[1] >> 8) * (1.0f / 16777216.0f);
+  const float thr = threshold32(w[2]);
+  const float md = (u1 - 0.5f) * P->two_max_step;
+  const float xo = xs[nm];
+  const float xn = xo + md;
+  float left, right;
+  if (periodic) {
+    left = nm > 0 ? xs[nm - 1] : xs[n - 1] - lf;
+    right = nm + 1 < n ? xs[nm + 1] : xs[0] + lf;
+  } else {
+    left = nm > 0 ? xs[nm - 1] : -INFINITY;
+    right = nm + 1 < n ? xs[nm + 1] : INFINITY;
+  }
+  int ok = (xn > left) && (xn < right);
+  if (!periodic) ok = ok && !(fabsf(xn) > half_l);
+  if (!ok) return 0.0f;
+  /* lane w of the G lanes of a step: side -1 for w < G/2; offsets
+   * kb, kb + G/2, ... (kb = w % (G/2) + 1) up to the window W,
+   * summed in offset order, then the butterfly over the G lanes */
+  const int H2 = (int)G / 2;
+  const int KPL = (int)W / H2;
+  float de = 0.0f;
+  for (int chunk = 0;; ++chunk) {
+    float v[32] = {0};
+    int any_sat = 0;
+    for (uint32_t gl = 0; gl < G; ++gl) {
+      const int side = (int)gl < H2 ? -1 : 1;
+      const int kb = (int)gl % H2 + 1;
+      float tl = 0.0f;
+      for (int q = 0; q < KPL; ++q) {
+        const int k = chunk * (int)W + kb + q * H2;
+        int j = nm + side * k;
+        int valid = 1;
+        float shift = 0.0f;
+        if (!periodic) {
+          valid = j >= 0 && j < n;
+        } else if (j < 0) {
+          j += n;
+          shift = -lf;
+        } else if (j >= n) {
+          j -= n;
+          shift = lf;
+        }
+        float tq = 0.0f;
+        if (valid) {
+          const float xj = xs[j] + shift;
+          const float dnw = side > 0 ? xj - xn : xn - xj;
+          const float dol = side > 0 ? xj - xo : xo - xj;
+          const float dn2 = dnw * dnw, do2 = dol * dol;
+          tq = pair_e32(dn2, P) - pair_e32(do2, P);
+          if (k == (chunk + 1) * (int)W && (dn2 <= P->rc2 || do2 <= P->rc2)) any_sat = 1;
+        }
+        tl = q == 0 ? tq : tl + tq;
+      }
+      v[gl] = tl;
+    }
+    de = de + butterfly32(v, G);
+    *pairs += 4 * W;
+    if (!any_sat) break;
+    if (chunk == 0) R->window_overflows += 1;
+    if (periodic && 2 * (chunk + 2) * (int)W > n - 1) {
+      *err = JMM_ERR_INVALID;
+      break;
+    }
+  }
+  const int acc = (de <= 0.0f) || (de * P->beta < thr);
+  if (!acc) return 0.0f;
+  xs[nm] = xn;
+  R->disp_acc += 1;
+  return de;
+}
+
 static void run_chain(jmmo_batch *b, uint32_t c, uint64_t n_sweeps) {
   const jmm_batch_config *cfg = &b->cfg;
   const chain_prm Pv = make_prm(&b->chains[c], c);
@@ -276,80 +356,7 @@ static void run_chain(jmmo_batch *b, uint32_t c, uint64_t n_sweeps) {
     if (!vol) {
       R->disp_att += 1;
       if (!fp64) {
-        const float u1 = (float)(w[1] >> 8) * (1.0f / 16777216.0f);
-        const float thr = threshold32(w[2]);
-        const float md = (u1 - 0.5f) * P->two_max_step;
-        const float xo = xs[nm];
-        const float xn = xo + md;
-        float left, right;
-        if (periodic) {
-          left = nm > 0 ? xs[nm - 1] : xs[n - 1] - lf;
-          right = nm + 1 < n ? xs[nm + 1] : xs[0] + lf;
-        } else {
-          left = nm > 0 ? xs[nm - 1] : -INFINITY;
-          right = nm + 1 < n ? xs[nm + 1] : INFINITY;
-        }
-        int ok = (xn > left) && (xn < right);
-        if (!periodic) ok = ok && !(fabsf(xn) > half_l);
-        float de_acc = 0.0f;
-        if (ok) {
-          /* lane w of the G lanes of a step: side -1 for w < G/2; offsets
-           * kb, kb + G/2, ... (kb = w % (G/2) + 1) up to the window W,
-           * summed in offset order, then the butterfly over the G lanes */
-          const int H2 = (int)G / 2;
-          const int KPL = (int)W / H2;
-          float de = 0.0f;
-          for (int chunk = 0;; ++chunk) {
-            float v[32] = {0};
-            int any_sat = 0;
-            for (uint32_t gl = 0; gl < G; ++gl) {
-              const int side = (int)gl < H2 ? -1 : 1;
-              const int kb = (int)gl % H2 + 1;
-              float tl = 0.0f;
-              for (int q = 0; q < KPL; ++q) {
-                const int k = chunk * (int)W + kb + q * H2;
-                int j = nm + side * k;
-                int valid = 1;
-                float shift = 0.0f;
-                if (!periodic) {
-                  valid = j >= 0 && j < n;
-                } else if (j < 0) {
-                  j += n;
-                  shift = -lf;
-                } else if (j >= n) {
-                  j -= n;
-                  shift = lf;
-                }
-                float tq = 0.0f;
-                if (valid) {
-                  const float xj = xs[j] + shift;
-                  const float dnw = side > 0 ? xj - xn : xn - xj;
-                  const float dol = side > 0 ? xj - xo : xo - xj;
-                  const float dn2 = dnw * dnw, do2 = dol * dol;
-                  tq = pair_e32(dn2, P) - pair_e32(do2, P);
-                  if (k == (chunk + 1) * (int)W && (dn2 <= P->rc2 || do2 <= P->rc2)) any_sat = 1;
-                }
-                tl = q == 0 ? tq : tl + tq;
-              }
-              v[gl] = tl;
-            }
-            de = de + butterfly32(v, G);
-            pairs += 4 * W;
-            if (!any_sat) break;
-            if (chunk == 0) R->window_overflows += 1;
-            if (periodic && 2 * (chunk + 2) * (int)W > n - 1) {
-              err = JMM_ERR_INVALID;
-              break;
-            }
-          }
-          const int acc = (de <= 0.0f) || (de * P->beta < thr);
-          if (acc) {
-            xs[nm] = xn;
-            de_acc = de;
-            R->disp_acc += 1;
-          }
-        }
-        g.delta = g.delta + de_acc;
+        g.delta = g.delta + disp32(xs, n, nm, w, P, periodic, lf, half_l, G, W, &pairs, &err, R);
       } else {
         const double u1 = (double)(w[1] >> 8) * (1.0 / 16777216.0);
         const double thr = threshold64(w[2]);
@@ -507,6 +514,109 @@ static void run_chain(jmmo_batch *b, uint32_t c, uint64_t n_sweeps) {
   R->error = err;
 }
 
+/* ---- split chains (jmm_batch_config.split_n) -------------------------------
+ * The GPU runs a long constant-L chain between walls as alternating domains:
+ * per sweep, domains of B particles from a random offset, the domains of one
+ * colour at once, then the other.  Domains of one phase share no pair, so
+ * replaying them one after another in index order gives the GPU's result
+ * bit for bit: each domain's steps are the EXACT kernel's displacement steps
+ * on the chain's positions (G = 4 lanes, the split window), its Philox
+ * blocks those of the chain's steps lo + 1 .. hi of the sweep, its energy
+ * change an FP32 sum over its steps; the chain's FP64 energy takes the
+ * domains' changes in index order and is sampled once per sweep. */
+static uint32_t split_domain_size(uint32_t n) {
+  const uint32_t b = 32u * ((n + 479u) / 480u);
+  return b < 32u ? 32u : b;
+}
+
+static int is_split(const jmmo_batch *b, const jmm_chain_desc *c) {
+  return !b->fp64 && b->cfg.split_n > 0 && c->n >= b->cfg.split_n && c->ensemble == JMM_NLT &&
+         b->cfg.boundary == JMM_BOUNDARY_WALLS;
+}
+
+static void run_split32(jmmo_batch *b, uint32_t c, uint64_t n_sweeps) {
+  const jmm_batch_config *cfg = &b->cfg;
+  const chain_prm Pv = make_prm(&b->chains[c], c);
+  const chain_prm *P = &Pv;
+  const int n = (int)P->n;
+  float *xs = b->xf[c];
+  jmm_chain_result *R = &b->res[c];
+  const uint32_t W0 = cfg->window ? cfg->window : (b->g <= 8 ? 4u : b->g / 2u);
+  const uint32_t W = W0 > 8 ? 16u : (W0 > 4 ? 8u : 4u);
+  const uint32_t B = split_domain_size((uint32_t)n);
+  const double L = R->l;
+  const float lf = (float)L, half_l = (float)(L * 0.5);
+  const double rho = (double)n / L;
+  uint64_t steps = R->steps, pairs = R->pair_evals;
+  uint32_t err = R->error, since_resum = 0;
+  double e = R->e;
+  double *dde = (double *)calloc((size_t)n / B + 2, sizeof(double));
+  for (uint64_t sw = 0; sw < n_sweeps; ++sw) {
+    uint32_t lw[4];
+    jmmo_step_words(cfg->seed, steps + 1, P->id, lw);
+    const int off = (int)jmmo_word_to_index(lw[3], B);
+    const uint32_t first = lw[3] & 1u;
+    const int n_dom = (n - off + (int)B - 1) / (int)B + 1;
+    for (int phase = 0; phase < 2; ++phase) {
+      const int colour = (int)((first + (uint32_t)phase) & 1u);
+      for (int d = colour; d < n_dom; d += 2) {
+        const int lo = off + (d - 1) * (int)B < 0 ? 0 : off + (d - 1) * (int)B;
+        const int hi = off + d * (int)B > n ? n : off + d * (int)B;
+        dde[d] = 0.0;
+        if (hi <= lo) continue;
+        int fits = 1;
+        if (lo >= 16) fits = fits && (xs[lo - 1] - xs[lo - 16]) > P->rc;
+        if (hi + 16 <= n) fits = fits && (xs[hi + 15] - xs[hi]) > P->rc;
+        if (!fits) {
+          err |= JMM_ERR_INVALID;
+          continue;
+        }
+        float delta = 0.0f;
+        const int nd = hi - lo;
+        for (int t = 0; t < nd; ++t) {
+          uint32_t w[4];
+          jmmo_step_words(cfg->seed, steps + (uint64_t)lo + (uint64_t)t + 1, P->id, w);
+          const int nm = lo + (int)jmmo_word_to_index(w[0], (uint64_t)nd);
+          R->disp_att += 1;
+          delta = delta + disp32(xs, n, nm, w, P, 0, lf, half_l, 4, W, &pairs, &err, R);
+        }
+        dde[d] = (double)delta;
+      }
+    }
+    for (int d = 0; d < n_dom; ++d) e = e + dde[d];
+    R->sum_e = R->sum_e + e;
+    R->sum_e2 = R->sum_e2 + e * e;
+    R->sum_l = R->sum_l + L;
+    R->sum_l2 = R->sum_l2 + L * L;
+    R->sum_le = R->sum_le + L * e;
+    R->sum_rho = R->sum_rho + rho;
+    R->sum_rho2 = R->sum_rho2 + rho * rho;
+    R->samples += 1;
+    steps += (uint64_t)n;
+    if (cfg->resum_sweeps > 0 && ++since_resum >= cfg->resum_sweeps) {
+      since_resum = 0;
+      double uo, un;
+      energies32(xs, P, 32, 0, lf, 0, 1.0f, lf, &uo, &un, &pairs, &err);
+      const double drift = fabs(e - uo);
+      if (drift > R->max_drift) R->max_drift = drift;
+      e = uo;
+    }
+  }
+  free(dde);
+  R->e = e;
+  R->steps = steps;
+  R->pair_evals = pairs;
+  if (!isfinite(e)) err |= JMM_ERR_NUMERIC;
+  R->error = err;
+}
+
+static void run_any(jmmo_batch *b, uint32_t c, uint64_t n_sweeps) {
+  if (is_split(b, &b->chains[c]))
+    run_split32(b, c, n_sweeps);
+  else
+    run_chain(b, c, n_sweeps);
+}
+
 /* ---- API ------------------------------------------------------------------- */
 
 static double chain_energy(jmmo_batch *b, uint32_t c) {
@@ -574,13 +684,13 @@ void jmmo_batch_destroy(jmmo_batch *b) {
 }
 
 int jmmo_batch_run(jmmo_batch *b, uint64_t n_sweeps) {
-  for (uint32_t c = 0; c < b->n_chains; ++c) run_chain(b, c, n_sweeps);
+  for (uint32_t c = 0; c < b->n_chains; ++c) run_any(b, c, n_sweeps);
   return JMM_OK;
 }
 
 int jmmo_batch_run_chain(jmmo_batch *b, uint32_t chain, uint64_t n_sweeps) {
   if (chain >= b->n_chains) return JMM_ERR_INVALID;
-  run_chain(b, chain, n_sweeps);
+  run_any(b, chain, n_sweeps);
   return JMM_OK;
 }
 

@@ -122,3 +122,34 @@ def test_uneven_batch_classes_match_fp64(gpu, fixture):
             print(f"  pot={pot} rho={rho} T={t} {r[0]:6s} {r[1]:.6g} ({r[2]:.2g})  "
                   f"{r[3]:.6g} ({r[4]:.2g})  z={r[5]:+.2f}")
     _judge(rows, "GPU FAST vs batched FP64, soft sphere and Gaussian core")
+
+
+def test_split_chains_match_fp64(gpu, fixture):
+    """The same NVT states run split (split_n = 64: every N = 128 chain cut
+    into domains of 32, alternating colours, sampled once per sweep) against
+    the FP64 restatement's whole chains."""
+    proto = fixture["protocol"]["nvt"]
+    cut = {int(k): v for k, v in fixture["protocol"]["nvt_cutoff"].items()}
+    states = fixture["protocol"]["nvt_states"]
+    n = proto["n"]
+    chains = [abi.make_chain(n, potential=pot, ensemble=abi.JMM_NLT, cutoff=cut[pot], t=t,
+                             rho=rho, max_step=proto["max_step"])
+              for pot, rho, t in states for _ in range(REPLICAS)]
+    cfg = abi.make_batch_config(seed=2028, precision=abi.JMM_PREC_FAST, resum_sweeps=100,
+                                split_n=64)
+    with ChainBatch(cfg, chains) as b:
+        b.run(proto["equil"])
+        b.reset_stats()
+        b.run(proto["prod"])
+        res = b.results()
+    assert not np.any(res["error"])
+    assert np.all(res["samples"] == proto["prod"])  # one sample per sweep
+    rows = []
+    print("\nGPU FAST split vs batched FP64 (NVT): potential, rho, T, observable, GPU (se), "
+          "CPU (se), z")
+    for (pot, rho, t), g, st in zip(states, _tables(res, len(states), n), fixture["nvt"]):
+        for r in es.compare(g, st["batched_fp64"], ("u", "var_u")):
+            rows.append(r)
+            print(f"  pot={pot} rho={rho} T={t} {r[0]:6s} {r[1]:.6g} ({r[2]:.2g})  "
+                  f"{r[3]:.6g} ({r[4]:.2g})  z={r[5]:+.2f}")
+    _judge(rows, "GPU FAST split chains vs batched FP64")
