@@ -65,6 +65,10 @@ def parse_args():
                     help="large workload: particles per domain")
     ap.add_argument("--sample-every", type=int, default=10,
                     help="grad workload: sweeps between gradient samples")
+    ap.add_argument("--split-n", type=int, default=None,
+                    help="batched workloads: constant-L chains of at least this many particles "
+                         "run split over a block's warps in alternating domains (0 = none; "
+                         "default 512 for the uneven workload, 0 otherwise)")
     ap.add_argument("--no-sub-workloads", action="store_true",
                     help="batched NPT workload at one GPU: leave out the compact records of the "
                          "uneven, gradient and large-chain workloads")
@@ -75,6 +79,8 @@ def parse_args():
 def apply_workload_defaults(args):
     """Sizes of the chosen workload where the command line left the batched
     NPT workload's defaults."""
+    if getattr(args, "split_n", None) is None:
+        args.split_n = 512 if args.workload == "uneven" else 0
     if args.workload == "uneven":
         if args.chains == 4096:
             args.chains = 1024
@@ -111,7 +117,8 @@ def uneven_workload(args, seed):
         chains.append(abi.make_chain(n, potential=pot, ensemble=abi.JMM_NLT, eps=1.0, sigma=1.0,
                                      cutoff=rc, t=0.5 + 1.5 * ut[c], rho=0.3 + 0.6 * ur[c],
                                      max_step=0.3))
-    cfg = abi.make_batch_config(seed=seed, precision=abi.JMM_PREC_FAST, resum_sweeps=100)
+    cfg = abi.make_batch_config(seed=seed, precision=abi.JMM_PREC_FAST, resum_sweeps=100,
+                                split_n=getattr(args, "split_n", 0) or 0)
     return cfg, chains
 
 
@@ -140,10 +147,14 @@ def config_dict(args, extra=None):
     if args.workload == "grad":
         return grad_config(args, extra)
     if args.workload == "uneven":
+        split = getattr(args, "split_n", 0) or 0
         d = {"workload": (f"uneven batch: {args.chains} chains, N ~ U{{32..2048}}, rho ~ "
                           "U(0.3,0.9), potential cycling LJ rc=3 / soft sphere rc=2.5 / Gaussian "
                           "core rc=4 (eps=sigma=1), T ~ U(0.5,2.0), NVT, hard walls, max "
-                          "displacement 0.3"),
+                          "displacement 0.3"
+                          + (f"; chains of N >= {split} split over a block's warps in "
+                             "alternating domains (sampled once per sweep)" if split else "")),
+             "split_n": split,
              "chains": args.chains, "sweeps_per_step": args.sweeps_per_step,
              "l2": "flushed between timed steps (256 MiB device write)",
              "precision": "FP32 pair energies, FP64 running totals and accumulators"}
@@ -874,7 +885,8 @@ def run_ours(args, rank, world, local_rank):
                                     lanes_per_chain=lanes if one_class else 0,
                                     steps_per_round=spr if one_class else 0,
                                     chains_per_block=cpb if one_class else 0,
-                                    window=next(iter(b.shapes().values()))[3] if one_class else 0)
+                                    window=next(iter(b.shapes().values()))[3] if one_class else 0,
+                                    split_n=cfg.split_n)
     # the chain descriptions as the C call takes them, built once like the
     # pinned positions; each step continues from the last one's box lengths
     desc = chain_array(chains)
@@ -1066,6 +1078,7 @@ def sub_workload_records(args, local_rank):
     for wl in SUB_WORKLOADS:
         sub = argparse.Namespace(**vars(args))
         sub.workload, sub.chains, sub.n, sub.sweeps_per_step = wl, 4096, 256, 1000
+        sub.split_n = None
         apply_workload_defaults(sub)
         sub.steps, sub.warmup, sub.e2e_steps, sub.cpu_seconds = 3, 3, 1, 1.0
         runner = {"large": run_large, "grad": run_grad}.get(wl, run_ours)

@@ -286,3 +286,16 @@ def test_own_arm_without_a_gpu_fails_loudly():
     p = _run_bench(["--steps", "1", "--warmup", "3", "--chains", "64"], timeout=120)
     assert p.returncode != 0
     assert not any(ln.strip().startswith("{") for ln in p.stdout.splitlines())
+
+
+def test_uneven_workload_splits_long_chains_by_default(monkeypatch):
+    """The uneven workload runs its chains of N >= 512 split (the batched
+    config's split_n); --split-n 0 runs every chain whole; other workloads
+    split nothing unless asked."""
+    a = args_for(monkeypatch, "--workload", "uneven")
+    cfg, _ = bench.uneven_workload(a, 1)
+    assert a.split_n == 512 and cfg.split_n == 512
+    assert bench.config_dict(a)["split_n"] == 512
+    a = args_for(monkeypatch, "--workload", "uneven", "--split-n", "0")
+    assert bench.uneven_workload(a, 1)[0].split_n == 0
+    assert args_for(monkeypatch).split_n == 0
