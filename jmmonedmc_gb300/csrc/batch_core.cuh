@@ -254,7 +254,8 @@ __device__ __forceinline__ float pair_energy_h(float d2, const Hot &H) {
 }
 
 // The pair energy over its strength (eps4): the FAST step loop sums these
-// and scales the chain's energy change once.
+// and scales the chain's energy change once.  LJ's (s^6)^2 - s^6 is one fused
+// multiply-add here (FAST only).
 template <int POT>
 __device__ __forceinline__ float pair_shape_fast(float d2, const Hot &H) {
   float e;
@@ -263,7 +264,7 @@ __device__ __forceinline__ float pair_shape_fast(float d2, const Hot &H) {
   } else {
     const float inv2 = __fmul_rn(H.sigma2, rcp32<false>(d2));
     const float inv6 = __fmul_rn(__fmul_rn(inv2, inv2), inv2);
-    e = (POT == JMM_POT_SOFTSPHERE) ? __fmul_rn(inv6, inv6) : __fmul_rn(inv6, __fsub_rn(inv6, 1.0f));
+    e = (POT == JMM_POT_SOFTSPHERE) ? __fmul_rn(inv6, inv6) : __fmaf_rn(inv6, inv6, -inv6);
   }
   return d2 <= H.rc2 ? e : 0.0f;
 }

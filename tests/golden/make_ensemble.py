@@ -22,6 +22,15 @@ blocking errors of E/N, rho and L from its chunk averages
 (tests/ensemble_stats.py).  Run by hand (about 30 minutes on 8 cores):
 
     python tests/golden/make_ensemble.py [--jobs 8]
+
+The large-chain workload's state (N = 2^20, LJ 12-6 truncated at 2.5,
+density 0.7, T = 1.2, hard walls, displacements up to 0.3, lattice start)
+is a section of its own, eight chains of the FP64 restatement (sequential
+single-particle Metropolis with the cut-off window, the reference's move
+loop cannot hold N = 2^20); each keeps its mean E/N and acceptance ratio
+over the production sweeps (about 6 minutes on 8 cores):
+
+    python tests/golden/make_ensemble.py --parts large
 """
 import argparse
 import json
@@ -41,6 +50,7 @@ NVT = dict(n=128, max_step=0.3, equil=1000, prod=4000, chunk=100, batch_replicas
 SOFT, GAUSS = 3, 4  # JMM_POT_SOFTSPHERE, JMM_POT_GAUSS
 NVT_CUTOFF = {SOFT: 2.5, GAUSS: 4.0}
 NVT_STATES = [(pot, rho, t) for pot in (SOFT, GAUSS) for rho in (0.3, 0.9) for t in (0.5, 2.0)]
+LARGE = dict(n=1 << 20, rho=0.7, t=1.2, cutoff=2.5, max_step=0.3, equil=100, prod=300, chains=8)
 
 
 def _setup():
@@ -106,6 +116,27 @@ def batch_task(kind, idx, state):
     return kind, idx, _replica_table(chunks, q["n"])
 
 
+def large_task(k):
+    """One chain of the large-chain workload through the FP64 restatement."""
+    _setup()
+    from jmmonedmc_gb300 import abi
+    from tests import oracle_lib
+    q = LARGE
+    chain = abi.make_chain(q["n"], potential=abi.JMM_POT_LJCUT, ensemble=abi.JMM_NLT,
+                           cutoff=q["cutoff"], t=q["t"], rho=q["rho"], max_step=q["max_step"])
+    cfg = abi.make_batch_config(seed=900 + k, precision=abi.JMM_PREC_EXACT, resum_sweeps=0)
+    b = oracle_lib.OracleBatch(cfg, [chain], fp64=True)
+    b.run(q["equil"])
+    r0 = b.results()
+    b.run(q["prod"])
+    r1 = b.results()
+    b.close()
+    s = float(r1["samples"][0] - r0["samples"][0])
+    u = float(r1["sum_e"][0] - r0["sum_e"][0]) / s / q["n"]
+    acc = float(r1["disp_acc"][0] - r0["disp_acc"][0]) / float(r1["disp_att"][0] - r0["disp_att"][0])
+    return k, u, acc
+
+
 def plain_task(idx, r, t, p, max_dl):
     """One replica of the reference's move loop (FP64 restatement)."""
     _setup()
@@ -138,11 +169,27 @@ def plain_task(idx, r, t, p, max_dl):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
+    ap.add_argument("--parts", default="grid,large",
+                    help="grid (the NPT and NVT states), large (the large chains), or both; "
+                         "a part not made keeps the file's existing section")
     args = ap.parse_args()
+    parts = set(args.parts.split(","))
     _setup()
     import numpy as np
     t0 = time.time()
     ctx = mp.get_context("spawn")
+    if "grid" not in parts:
+        with open(OUT) as f:
+            out = json.load(f)
+        with ctx.Pool(args.jobs) as pool:
+            res = pool.map(large_task, range(LARGE["chains"]))
+        out["protocol"]["large"] = LARGE
+        out["large"] = {"u": [u for _, u, _ in sorted(res)], "acc": [a for _, _, a in sorted(res)]}
+        with open(OUT, "w") as f:
+            json.dump(out, f, indent=None, separators=(",", ":"))
+            f.write("\n")
+        print(f"wrote the large section of {OUT} in {time.time() - t0:.0f} s")
+        return
     out = {"protocol": {"npt": NPT, "npt_states": NPT_STATES, "nvt": NVT,
                         "nvt_cutoff": {str(k): v for k, v in NVT_CUTOFF.items()},
                         "nvt_states": NVT_STATES},
@@ -172,6 +219,11 @@ def main():
             merged = [{key: np.concatenate([rep[c][key] for rep in order])
                        for key in order[0][c]} for c in range(len(order[0]))]
             out["npt"][k]["reference_algorithm"] = _replica_table(merged, NPT["n"])
+        if "large" in parts:
+            res = pool.map(large_task, range(LARGE["chains"]))
+            out["protocol"]["large"] = LARGE
+            out["large"] = {"u": [u for _, u, _ in sorted(res)],
+                            "acc": [a for _, _, a in sorted(res)]}
     with open(OUT, "w") as f:
         json.dump(out, f, indent=None, separators=(",", ":"))
         f.write("\n")

@@ -217,3 +217,40 @@ def test_narrow_halo_is_flagged_and_sequential_handles_it(gpu):
     _check_positions(seq.positions(0), l)
     np.testing.assert_allclose(r["e"], seq.energies(), rtol=1e-6)
     seq.close()
+
+
+def test_full_size_ensemble_matches_fp64_fixture(gpu):
+    """The large-chain workload at its full size (64 chains x N = 2^20, LJ
+    rc 2.5, rho 0.7, T 1.2, displacements up to 0.3, domains of 1024) against
+    eight chains of the FP64 CPU restatement of the same state
+    (tests/golden/ensemble_states.json, section "large": sequential
+    single-particle Metropolis, the reference's move loop cannot hold 2^20):
+    per-chain means of E/N and the acceptance ratio over sweeps 100-400 from
+    the lattice, within 3 combined standard errors of the chain spreads plus
+    2e-5 (FP32 pair terms)."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                           "ensemble_states.json")) as f:
+        fix = json.load(f)
+    q = fix["protocol"]["large"]
+    n = q["n"]
+    chains = [abi.make_chain(n, rho=q["rho"], t=q["t"], cutoff=q["cutoff"], max_step=q["max_step"])
+              for _ in range(64)]
+    h = LargeChains(_cfg(41, resum=0), chains, domain_size=1024)
+    h.run(q["equil"], "domains")
+    h.reset_stats()
+    r0 = h.results()
+    h.run(q["prod"], "domains")
+    r = h.results()
+    h.close()
+    assert np.all(r["error"] == 0)
+    u = r["sum_e"] / r["samples"] / n
+    acc = (r["accepted"] - r0["accepted"]) / (r["moves"] - r0["moves"])
+    for name, g, c in (("E/N", u, np.array(fix["large"]["u"])),
+                       ("acceptance", acc, np.array(fix["large"]["acc"]))):
+        se = np.sqrt(g.var(ddof=1) / len(g) + c.var(ddof=1) / len(c))
+        z = (g.mean() - c.mean()) / se
+        print(f"N = 2^20 {name}: GPU domains {g.mean():.6f} (se {g.std(ddof=1) / 8:.1e}), "
+              f"FP64 CPU {c.mean():.6f}, z = {z:+.2f}")
+        assert abs(g.mean() - c.mean()) < 3 * se + 2e-5, (name, g.mean(), c.mean(), se)
