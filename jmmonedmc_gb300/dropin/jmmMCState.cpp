@@ -412,8 +412,13 @@ int qav(struct MCState *mcs) {
 int fav(struct MCState *mcs) { return qav(mcs); }
 int qavLJ(struct MCState *mcs) { return qav(mcs); }
 
+// The barrier (src/jmmMCState.cpp:1742) keeps the step number unchanged until
+// every thread of the team has finished the previous step's print tests
+// (the driver evaluates isGPrint from all threads outside any single); without
+// it a fast thread's increment sends a slow one into a different construct.
 unsigned long int incrementStep(struct MCState *mcs) {
   unsigned long int out = 0;
+#pragma omp barrier
 #pragma omp single copyprivate(out)
   {
     if (mcs->sn != mcs->numSteps) {
