@@ -532,6 +532,12 @@ def run_large(args, rank, world, local_rank):
     for k in range(args.chains):
         x_host[k * args.n:(k + 1) * args.n] = h.positions(k)
     h.close()
+    # k from the first four chains' positions after the timed region (NVT:
+    # 2k pair energies per displacement)
+    k_sample = min(4, args.chains)
+    k_mean = in_cutoff_neighbours(x_host[:k_sample * args.n], [args.n] * k_sample,
+                                  float(chains[0].cutoff))
+    alg_pairs = 2.0 * k_mean * moves
     e2e_times, e2e_moves = [], 0
     for j in range(args.e2e_steps):
         torch.cuda.synchronize(dev)
@@ -551,7 +557,7 @@ def run_large(args, rank, world, local_rank):
         traffic = float(fig["dram_bytes_per_particle_phase"]) * args.chains * args.n / 2
     launches_per_step = 3 * S
     launch_ms = total_ms / (args.steps * 2 * S)  # the two domain launches of a sweep dominate
-    pairs_per_launch = pairs / (args.steps * 2 * S)
+    pairs_per_launch = alg_pairs / (args.steps * 2 * S)
     achieved = pairs_per_launch * FLOP_PER_PAIR / (launch_ms * 1e-3) / 1e12
     line = {
         "metric": LARGE_METRIC,
@@ -578,6 +584,11 @@ def run_large(args, rank, world, local_rank):
             "peak_source": "measured live by jmm_measure_peaks (FP32 FMA kernel; "
                            "MEASURED_PEAKS.json holds no FP32 figure)",
             "pair_evals_per_launch": pairs_per_launch,
+            "pair_evals_basis": (f"algorithmic: k = {k_mean:.3f} in-cut-off partners per "
+                                 f"particle (first {k_sample} chains, positions after the timed "
+                                 "region); 2k pair energies per displacement"),
+            "in_cutoff_partners_k": k_mean,
+            "window_slots_per_launch": pairs / (args.steps * 2 * S),
             "flop_per_pair": FLOP_PER_PAIR,
             "mufu_rcp_frac": pairs_per_launch / (launch_ms * 1e-3) / (rcp_peak.value * 1e12),
             "issue": issue_roofline("domain_kernel_large_chains",
@@ -726,6 +737,7 @@ def run_grad(args, rank, world, local_rank):
     n_tot = sum(int(c.n) for c in chains)
     x_host = torch.empty(n_tot, dtype=torch.float32, pin_memory=True).numpy()
     x_host[:] = np.concatenate([b.positions(k) for k in range(len(chains))])
+    alg_pairs, k_mean = algorithmic_pairs(before, after, x_host, chains)
     desc = chain_array(chains)
     chain_view(desc)["l0"] = b.results()["l"]  # the box lengths of these positions
     e2e_times, e2e_moves = [], 0
@@ -744,7 +756,7 @@ def run_grad(args, rank, world, local_rank):
            "how": "ChainBatch from pinned host positions (jmm_batch_create_at), run_sampled, "
                   "results and grad_stats read back, all inside the timed region"}
     launch_ms = total_ms / args.steps
-    achieved = pairs / args.steps * FLOP_PER_PAIR / (launch_ms * 1e-3) / 1e12
+    achieved = alg_pairs / args.steps * FLOP_PER_PAIR / (launch_ms * 1e-3) / 1e12
     line = {
         "metric": GRAD_METRIC,
         "value": moves_all / (total_ms * 1e-3),
@@ -769,7 +781,12 @@ def run_grad(args, rank, world, local_rank):
             "frac": achieved / fp32_peak.value, "traffic": None,
             "peak_source": "measured live by jmm_measure_peaks (FP32 FMA kernel; "
                            "MEASURED_PEAKS.json holds no FP32 figure)",
-            "pair_evals_per_launch": pairs / args.steps, "flop_per_pair": FLOP_PER_PAIR,
+            "pair_evals_per_launch": alg_pairs / args.steps,
+            "pair_evals_basis": (f"algorithmic: k = {k_mean:.3f} in-cut-off partners per "
+                                 "particle (mean over chains); 2k pair energies per "
+                                 "displacement, N k / 2 per volume move"),
+            "in_cutoff_partners_k": k_mean,
+            "window_slots_per_launch": pairs / args.steps, "flop_per_pair": FLOP_PER_PAIR,
             "kernel": "jmm::batch::chains_kernel (the gradient kernel runs between)"},
         "e2e": e2e,
         "gpu_launches": args.steps * (1 + S // every),
@@ -1086,6 +1103,8 @@ def sub_workload_records(args, local_rank):
         rec = {k: line[k] for k in SUB_KEYS if k in line}
         rec["workload"] = line["config"]["workload"]
         rec["sweeps_per_step"] = sub.sweeps_per_step
+        if "class_shapes" in line["config"]:
+            rec["class_shapes"] = line["config"]["class_shapes"]
         out[wl] = rec
     return out
 

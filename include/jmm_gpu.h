@@ -297,7 +297,10 @@ typedef struct jmm_chain_result {
   uint64_t samples;      /* steps accumulated since the last reset             */
   double sum_e, sum_e2, sum_l, sum_l2, sum_le, sum_rho, sum_rho2;
   uint64_t disp_acc, disp_att, vol_acc, vol_att;
-  uint64_t pair_evals;   /* pair energies evaluated                            */
+  uint64_t pair_evals;   /* pair slots evaluated: 4 x window per displacement
+                          * and per window extension; 2 per pair within the
+                          * cut-off at the old or new length of a volume move,
+                          * 1 per in-cut-off pair of a re-sum                */
   double max_drift;      /* largest |running E - fresh FP64 sum| at a re-sum   */
   uint32_t error;        /* JMM_ERR_* seen by the kernel, 0 = none             */
   uint32_t window_overflows; /* moves whose neighbour window was extended      */

@@ -36,6 +36,7 @@
 // quantities, rounded in another order).
 #pragma once
 #include <math.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "../../include/jmm_gpu.h"
@@ -218,6 +219,45 @@ __device__ __forceinline__ void fold(Seg &g, jmm_chain_result *__restrict__ rp, 
   g.nseg = 0;
 }
 
+static_assert(offsetof(jmm_chain_result, sum_rho2) - offsetof(jmm_chain_result, sum_e) ==
+                  6 * sizeof(double),
+              "the seven sums are consecutive doubles");
+
+// FAST precision: lanes 0-6 of the chain fold one sum each (sum_e ..
+// sum_rho2, consecutive doubles of the record) as one product and a term,
+// a * b + c, from the segment's sum of E, lin = nd e0 + sd, and of E^2,
+// e0 (lin + sd) + sd2; lane 0 adds the sample count.
+__device__ __forceinline__ void fold_spread(Seg &g, jmm_chain_result *__restrict__ rp, int cl,
+                                            double l, double rho) {
+  const double nd = (double)g.nseg, sdd = (double)g.sd;
+  const double lin = fma(nd, g.e0, sdd);
+  if (cl < 7) {
+    const double ndx = nd * (cl == 3 ? l : rho);
+    const double a = cl == 1 ? g.e0 : (cl == 4 ? lin : ((cl == 3 || cl == 6) ? ndx : nd));
+    const double b = cl == 0 ? g.e0 : (cl == 1 ? lin + sdd : (cl <= 4 ? l : rho));
+    const double c = cl == 0 ? sdd : (cl == 1 ? (double)g.sd2 : 0.0);
+    double *sum = &rp->sum_e + cl;
+    *sum = *sum + fma(a, b, c);
+  }
+  if (cl == 0) rp->samples += g.nseg;
+  g.e0 = __dadd_rn(g.e0, (double)g.delta);
+  g.delta = 0.0f;
+  g.sd = 0.0f;
+  g.sd2 = 0.0f;
+  g.nseg = 0;
+}
+
+// The fold of a chain of L lanes: spread over seven lanes in FAST precision,
+// by the first lane in EXACT (the order the oracle replays).
+template <int L, bool kExact>
+__device__ __forceinline__ void fold_run(Seg &g, jmm_chain_result *__restrict__ rp, int cl,
+                                         double l, double rho) {
+  if (kExact || L < 8)
+    fold(g, rp, cl == 0, l, rho);
+  else
+    fold_spread(g, rp, cl, l, rho);
+}
+
 __device__ __forceinline__ void note_drift(jmm_chain_result *__restrict__ rp, bool writer,
                                            double drift) {
   if (writer && drift > rp->max_drift) rp->max_drift = drift;
@@ -351,10 +391,20 @@ __device__ __noinline__ void chain_energies(const float *xs, const Hot &H, int n
       if (kScaled) un = __dadd_rn(un, (double)en);
     }
   }
-  if (!kExact) {
-    uo = __dmul_rn((double)H.eps4, (double)fo);
-    un = __dmul_rn((double)H.eps4, (double)fd);
+  if (!kExact && kScaled && L >= 2) {
+    // both FAST sums over the lanes in one FP64 butterfly: after the first
+    // exchange even lanes carry sums of shapes, odd lanes of differences
+    const bool odd = gl & 1;
+    double r = __dadd_rn(odd ? (double)fd : (double)fo,
+                         __shfl_xor_sync(gmask, odd ? (double)fo : (double)fd, 1, L));
+#pragma unroll
+    for (int m = 2; m < L; m <<= 1) r = __dadd_rn(r, __shfl_xor_sync(gmask, r, m, L));
+    u_old = __dmul_rn((double)H.eps4, __shfl_sync(gmask, r, 0, L));
+    u_new = __dadd_rn(u_old, __dmul_rn((double)H.eps4, __shfl_sync(gmask, r, 1, L)));
+    pairs += __reduce_add_sync(gmask, cnt);
+    return;
   }
+  if (!kExact) uo = __dmul_rn((double)H.eps4, (double)fo);
   u_old = group_sum_d<L>(uo, gmask);
   if (!kScaled) {
     u_new = u_old;
@@ -495,7 +545,10 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
   uint32_t sweeps_since_resum = 0;
   uint32_t err = rp->error;
   uint64_t pairs = rp->pair_evals;
-  uint32_t ok_loc = 0;  // window chunks of this lane's kept steps (4 W pair energies each)
+  // window pair slots: 4 W for every kept displacement step (its lanes
+  // evaluate the window whether or not the trial keeps its place) and for
+  // every chunk an extended window adds
+  uint32_t chunks_extra = 0;
   uint32_t d_acc = 0, d_att = 0, v_acc = 0, v_att = 0, overflows = 0;
   const uint32_t total = (uint32_t)(cfg.n_sweeps * (uint64_t)spsw);
   __syncwarp(gmask);  // every lane has read the record before lane 0 updates it
@@ -573,7 +626,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       bool acc = arg < (double)thr_0;
       if (!(lnew > 0.0)) acc = false;
       if (PER && !(lnew > 2.0 * (double)P.rc)) acc = false;
-      fold(g, rp, writer, L_box, rho_box);
+      fold_run<L, kExact>(g, rp, cl, L_box, rho_box);
       v_att += 1;
       if (acc) {
         for (int i = cl; i < n; i += L) xs[i] = __fmul_rn(xs[i], s);
@@ -623,7 +676,6 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       float de = group_sum<G>(t_lane, gmask);
       const unsigned satbits = (__ballot_sync(gmask, sat) >> lane_shift & kChainBits);
       uint32_t f = rem;
-      uint32_t extra_chunks = 0;
       if (satbits & kSlotBits) {
         // slow path: slot 0's window reaches beyond W; extend it chunk by chunk
         for (int chunk = 1;; ++chunk) {
@@ -644,7 +696,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
               sat2 = inr2 && k == (chunk + 1) * W && (dn22 <= H.rc2 || do22 <= H.rc2);
           }
           de = __fadd_rn(de, group_sum<G>(t2, gmask));
-          extra_chunks += 1;
+          chunks_extra += 1;
           if (!(((__ballot_sync(gmask, sat2) >> lane_shift & kChainBits)) & kSlotBits)) break;
           if (PER && 2 * (chunk + 2) * W > n - 1) {
             err = JMM_ERR_INVALID;
@@ -733,8 +785,6 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
         g.delta = __fadd_rn(g.delta, __shfl_sync(gmask, x, (int)(f - 1) * G, L));
       }
       __syncwarp(gmask);
-      // this slot leader's kept step with its window chunks (pair energies)
-      if (wl == 0 && (uint32_t)slot < f && ok) ok_loc += 1u + (slot == 0 ? extra_chunks : 0u);
       d_acc += __popc(accbits & committed);
       d_att += f;
       g.nseg += f;
@@ -751,20 +801,19 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
         const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
         note_drift(rp, writer, drift);
         if (kShares) gather_shares<L>(g, sd_loc, sd2_loc, gmask);
-        fold(g, rp, writer, L_box, rho_box);
+        fold_run<L, kExact>(g, rp, cl, L_box, rho_box);
         g.e0 = uo;
       }
     }
   }
   if (kShares) gather_shares<L>(g, sd_loc, sd2_loc, gmask);
-  fold(g, rp, writer, L_box, rho_box);
+  fold_run<L, kExact>(g, rp, cl, L_box, rho_box);
   if (!isfinite(g.e0)) err = JMM_ERR_NUMERIC;
-  const uint32_t ok_sum = __reduce_add_sync(gmask, ok_loc);
   if (writer) {
     rp->e = g.e0;
     rp->l = L_box;
     rp->steps = step0 + total;
-    rp->pair_evals = pairs + (uint64_t)(4 * W) * ok_sum;
+    rp->pair_evals = pairs + (uint64_t)(4 * W) * (d_att + chunks_extra);
     rp->disp_acc += d_acc;
     rp->disp_att += d_att;
     rp->vol_acc += v_acc;

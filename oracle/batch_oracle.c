@@ -235,7 +235,7 @@ static double threshold64(uint32_t w) {
  * particle nm of xs[0..n) with the step's Philox words w, G window lanes of
  * W neighbours per side; moves the particle when accepted and returns the
  * accepted energy change (0 when rejected).  Counts accepted moves, window
- * extensions and window pair slots. */
+ * extensions and window pair slots (4 W per step and per extension). */
 static float disp32(float *xs, int n, int nm, const uint32_t w[4], const chain_prm *P,
                     int periodic, float lf, float half_l, uint32_t G, uint32_t W, uint64_t *pairs,
                     uint32_t *err, jmm_chain_result *R) {
@@ -254,7 +254,12 @@ static float disp32(float *xs, int n, int nm, const uint32_t w[4], const chain_p
   }
   int ok = (xn > left) && (xn < right);
   if (!periodic) ok = ok && !(fabsf(xn) > half_l);
-  if (!ok) return 0.0f;
+  /* the step's lanes evaluate its window (4 W pair slots) whether or not
+   * the trial keeps its place */
+  if (!ok) {
+    *pairs += 4 * W;
+    return 0.0f;
+  }
   /* lane w of the G lanes of a step: side -1 for w < G/2; offsets
    * kb, kb + G/2, ... (kb = w % (G/2) + 1) up to the window W,
    * summed in offset order, then the butterfly over the G lanes */
