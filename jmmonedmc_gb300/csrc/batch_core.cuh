@@ -529,19 +529,23 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
   const bool per_sweep = cfg.vol_schedule == JMM_VOLSCHED_SWEEP;
   double L_box = rp->l;
   float lf = (float)L_box, half_l = (float)__dmul_rn(L_box, 0.5);
-  double rho_box = __ddiv_rn((double)n, L_box);  // n / L, renewed when L changes
+  // n / L, renewed when L changes; a domain (HALO) keeps no statistics of
+  // its own: its caller samples the whole chain once per sweep
+  double rho_box = HALO ? 0.0 : __ddiv_rn((double)n, L_box);
   Seg g;
   g.e0 = rp->e;
   g.delta = 0.0f;
   g.sd = 0.0f;
   g.sd2 = 0.0f;
   g.nseg = 0;
-  constexpr bool kShares = !kExact && S > 1;
+  constexpr bool kShares = !kExact && S > 1 && !HALO;
   float sd_loc = 0.0f, sd2_loc = 0.0f;  // this lane's shares (kShares)
   const float inv_grid = SNAP ? __frcp_rn(P.grid) : 0.0f;
   const uint32_t spsw = P.steps_per_sweep;
   const uint64_t step0 = rp->steps;
-  uint32_t sweep_pos = (uint32_t)(step0 % spsw);
+  // a domain's pass is one sweep of its particles from wherever its caller's
+  // step count stands (where rounds end does not change a step's outcome)
+  uint32_t sweep_pos = HALO ? 0u : (uint32_t)(step0 % spsw);
   uint32_t sweeps_since_resum = 0;
   uint32_t err = rp->error;
   uint64_t pairs = rp->pair_evals;
@@ -766,8 +770,10 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
           const float d_s = __shfl_sync(gmask, de_acc, s2 * G, L);
           if ((uint32_t)s2 < f) {
             g.delta = __fadd_rn(g.delta, d_s);
-            g.sd = __fadd_rn(g.sd, g.delta);
-            g.sd2 = __fmaf_rn(g.delta, g.delta, g.sd2);
+            if (!HALO) {
+              g.sd = __fadd_rn(g.sd, g.delta);
+              g.sd2 = __fmaf_rn(g.delta, g.delta, g.sd2);
+            }
           }
         }
       } else {
@@ -779,9 +785,11 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
           if (slot >= o) x = __fadd_rn(x, y);
         }
         // the slot leaders of kept steps add their step's share
-        const float v = ((uint32_t)slot < f && wl == 0) ? __fadd_rn(g.delta, x) : 0.0f;
-        sd_loc = __fadd_rn(sd_loc, v);
-        sd2_loc = __fmaf_rn(v, v, sd2_loc);
+        if (!HALO) {
+          const float v = ((uint32_t)slot < f && wl == 0) ? __fadd_rn(g.delta, x) : 0.0f;
+          sd_loc = __fadd_rn(sd_loc, v);
+          sd2_loc = __fmaf_rn(v, v, sd2_loc);
+        }
         g.delta = __fadd_rn(g.delta, __shfl_sync(gmask, x, (int)(f - 1) * G, L));
       }
       __syncwarp(gmask);
@@ -807,7 +815,10 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
     }
   }
   if (kShares) gather_shares<L>(g, sd_loc, sd2_loc, gmask);
-  fold_run<L, kExact>(g, rp, cl, L_box, rho_box);
+  if (HALO)
+    g.e0 = __dadd_rn(g.e0, (double)g.delta);
+  else
+    fold_run<L, kExact>(g, rp, cl, L_box, rho_box);
   if (!isfinite(g.e0)) err = JMM_ERR_NUMERIC;
   if (writer) {
     rp->e = g.e0;
@@ -880,7 +891,8 @@ __global__ void __maxnreg__(G * S == 32 ? 72 : 128) chains_kernel(const ChainPar
 // from its lowest.  Each domain's energy change is summed in FP32 over its
 // steps; after the sweep the chain's FP64 energy takes the domains' changes
 // in index order, and the statistics sample the energy once per sweep
-// (samples count sweeps).  Constant-L chains re-sum every resum_sweeps
+// (samples count sweeps; thread 0 takes a sweep's sample while the other
+// warps start the next sweep).  Constant-L chains re-sum every resum_sweeps
 // sweeps over the whole chain (32 lanes of warp 0).
 
 constexpr uint32_t kSplitWarps = 8;  // warps of a split chain's block, at most
@@ -894,10 +906,11 @@ __host__ __device__ constexpr uint32_t split_domain_size(uint32_t n) {
 }
 
 // Shared memory of a split chain's block: per warp a step ring and a domain
-// record, the domains' energy changes, then the positions with their ghosts.
+// record, the domains' energy changes of two sweeps, then the positions with
+// their ghosts.
 __host__ __device__ constexpr uint64_t split_smem_bytes(uint32_t n, uint32_t warps) {
   return (uint64_t)warps * (kRingWords * 4u + sizeof(jmm_chain_result)) +
-         8u * (uint64_t)(n / split_domain_size(n) + 2u) + 4u * ((uint64_t)n + 2u * kGhost);
+         16u * (uint64_t)(n / split_domain_size(n) + 2u) + 4u * ((uint64_t)n + 2u * kGhost);
 }
 
 template <int G, int S, int POT, bool kExact, int WIN>
@@ -917,8 +930,11 @@ __global__ void __maxnreg__(72) split_kernel(const ChainParams *__restrict__ prm
   uint32_t *ring = reinterpret_cast<uint32_t *>(smem) + warp * kRingWords;
   jmm_chain_result *drec =
       reinterpret_cast<jmm_chain_result *>(reinterpret_cast<uint32_t *>(smem) + nwarps * kRingWords);
-  double *dde = reinterpret_cast<double *>(drec + nwarps);  // n / B + 2 domains at most
-  float *xs = reinterpret_cast<float *>(dde + (n / (int)B + 2)) + kGhost;
+  // the domains' energy changes (n / B + 2 domains at most), one buffer per
+  // sweep parity: thread 0 adds a sweep's changes while the next sweep runs
+  const int dstride = n / (int)B + 2;
+  double *dde = reinterpret_cast<double *>(drec + nwarps);
+  float *xs = reinterpret_cast<float *>(dde + 2 * dstride) + kGhost;
   jmm_chain_result *rp = res + P.id;
   const double L = rp->l;
   const float lf = (float)L;
@@ -935,13 +951,36 @@ __global__ void __maxnreg__(72) split_kernel(const ChainParams *__restrict__ prm
   ChainParams Pd = P;
   Pd.ensemble = JMM_NLT;
   uint32_t since_resum = 0;
+  // thread 0: the chain's energy after a sweep (its domains' changes in
+  // index order) into the per-sweep samples
+  int pend_dom = 0;         // domains of the sweep whose sample is pending (0: none)
+  const double *pend_dde = dde;
+  auto sample = [&]() {
+    for (int d = 0; d < pend_dom; ++d) e = __dadd_rn(e, pend_dde[d]);
+    rp->sum_e = __dadd_rn(rp->sum_e, e);
+    rp->sum_e2 = __dadd_rn(rp->sum_e2, __dmul_rn(e, e));
+    rp->sum_l = __dadd_rn(rp->sum_l, L);
+    rp->sum_l2 = __dadd_rn(rp->sum_l2, __dmul_rn(L, L));
+    rp->sum_le = __dadd_rn(rp->sum_le, __dmul_rn(L, e));
+    rp->sum_rho = __dadd_rn(rp->sum_rho, rho);
+    rp->sum_rho2 = __dadd_rn(rp->sum_rho2, __dmul_rn(rho, rho));
+    rp->samples += 1;
+  };
   __syncthreads();
   for (uint64_t sw = 0; sw < cfg.n_sweeps; ++sw) {
     const Words4 lw = step_words(cfg.seed, steps + 1, P.id);
     const int off = (int)word_to_index(lw.w[3], (uint64_t)B);
     const uint32_t first = lw.w[3] & 1u;
     const int n_dom = (n - off + (int)B - 1) / (int)B + 1;
+    double *dd = dde + (sw & 1u) * dstride;
     for (int phase = 0; phase < 2; ++phase) {
+      // the previous sweep's sample, by thread 0 ahead of its first domain
+      // (the other warps go on; the previous sweep's buffer stays untouched
+      // until the sweep after this one)
+      if (phase == 0 && pend_dom > 0) {
+        if (threadIdx.x == 0) sample();
+        pend_dom = 0;
+      }
       const int colour = (int)((first + (uint32_t)phase) & 1u);
       for (int d = colour + 2 * (int)warp; d < n_dom; d += 2 * (int)nwarps) {
         const int lo = max(0, off + (d - 1) * (int)B);
@@ -957,8 +996,12 @@ __global__ void __maxnreg__(72) split_kernel(const ChainParams *__restrict__ prm
             err |= JMM_ERR_INVALID;
           } else {
             jmm_chain_result *dr = drec + warp;
+            static_assert(sizeof(jmm_chain_result) % 8 == 0 && sizeof(jmm_chain_result) <= 256,
+                          "a record is at most 32 eight-byte words");
+            if (cl < (int)(sizeof(jmm_chain_result) / 8))
+              reinterpret_cast<unsigned long long *>(dr)[cl] = 0ull;
+            __syncwarp();
             if (cl == 0) {
-              memset(dr, 0, sizeof(jmm_chain_result));
               dr->l = L;
               dr->steps = steps + (uint64_t)lo;
             }
@@ -977,24 +1020,18 @@ __global__ void __maxnreg__(72) split_kernel(const ChainParams *__restrict__ prm
             __syncwarp();
           }
         }
-        if (cl == 0) dde[d] = de_d;
+        if (cl == 0) dd[d] = de_d;
       }
       __syncthreads();
     }
-    if (threadIdx.x == 0) {
-      for (int d = 0; d < n_dom; ++d) e = __dadd_rn(e, dde[d]);
-      rp->sum_e = __dadd_rn(rp->sum_e, e);
-      rp->sum_e2 = __dadd_rn(rp->sum_e2, __dmul_rn(e, e));
-      rp->sum_l = __dadd_rn(rp->sum_l, L);
-      rp->sum_l2 = __dadd_rn(rp->sum_l2, __dmul_rn(L, L));
-      rp->sum_le = __dadd_rn(rp->sum_le, __dmul_rn(L, e));
-      rp->sum_rho = __dadd_rn(rp->sum_rho, rho);
-      rp->sum_rho2 = __dadd_rn(rp->sum_rho2, __dmul_rn(rho, rho));
-      rp->samples += 1;
-    }
+    pend_dom = n_dom;
+    pend_dde = dd;
     steps += (uint64_t)n;
     if (cfg.resum_sweeps > 0 && ++since_resum >= (uint32_t)cfg.resum_sweeps) {
       since_resum = 0;
+      // the sample first, then the fresh sum replaces the running energy
+      if (threadIdx.x == 0) sample();
+      pend_dom = 0;
       if (warp == 0) {
         Hot H;
         H.eps4 = P.eps4;
@@ -1016,9 +1053,10 @@ __global__ void __maxnreg__(72) split_kernel(const ChainParams *__restrict__ prm
           err |= rerr;
         }
       }
+      __syncthreads();  // the re-sum reads every position before the next sweep moves any
     }
-    __syncthreads();
   }
+  if (pend_dom > 0 && threadIdx.x == 0) sample();
   for (int i = threadIdx.x; i < n; i += blockDim.x) xg[P.x_off + i] = xs[i];
   if (cl == 0) {
     tally[warp][0] = acc;
