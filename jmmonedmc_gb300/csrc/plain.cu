@@ -80,7 +80,7 @@ struct Args {
   uint64_t n, nn, npairs, num_trial_types;
   int32_t potential, nbn;
   int32_t use_qavlj;
-  int32_t stage_old;  // qad2 stages the stored pair terms in shared memory (N <= 1495)
+  int32_t stage_old;  // qad2 stages the stored pair terms in shared memory (where they fit)
   double cutoff, t, p;
   uint64_t seed, eci;
   // rho(x) and g(x) histograms, bins [0, rhonb) density, then gns x gnb
@@ -404,9 +404,9 @@ __device__ __forceinline__ void hist_touch(const Args &a, uint64_t b, uint64_t T
 // qagrho: particle ctl.nm moved by ctl.md, a.r[nm] already holds the new
 // position (the old one is formed as r[nm] - md, as the reference does).
 // Phase 0 flushes every bin the move touches, phase 1 changes the counts.
-__device__ void qagrho(const Args &a, const Ctl &ctl) {
+__device__ void qagrho(const Args &a, Scalars *S, const Ctl &ctl) {
   const uint64_t n = a.n, nm = ctl.nm, nm1 = n - 1;
-  const uint64_t T = a.s->hist_ticks;
+  const uint64_t T = S->hist_ticks;
   const double xn = a.r[nm];
   const double xo = __dsub_rn(xn, ctl.md);
   const long long rb1 = rho_bin(a, xo), rb2 = rho_bin(a, xn);
@@ -440,8 +440,8 @@ __device__ void qagrho(const Args &a, const Ctl &ctl) {
 // bin's sum has been brought up to the current accumulation.  A negative
 // separation (particles that passed each other) gives a negative bin, which
 // the reference writes out of bounds; here it is not counted.
-__device__ void fgrho(const Args &a) {
-  const uint64_t n = a.n, T = a.s->hist_ticks;
+__device__ void fgrho(const Args &a, Scalars *S) {
+  const uint64_t n = a.n, T = S->hist_ticks;
   const uint64_t total = a.rhonb + (uint64_t)a.gns * a.gnb;
   for (uint64_t b = threadIdx.x; b < total; b += blockDim.x) {
     a.h_acc[b] += (long long)a.h_val[b] * (long long)(T - a.h_last[b]);
@@ -469,15 +469,15 @@ __device__ void fgrho(const Args &a) {
 }
 
 // ugrho: one accumulation.
-__device__ __forceinline__ void ugrho(const Args &a) {
-  if (threadIdx.x == 0) a.s->hist_ticks += 1;
+__device__ __forceinline__ void ugrho(const Args &a, Scalars *S) {
+  if (threadIdx.x == 0) S->hist_ticks += 1;
 }
 
 // ---- the moves --------------------------------------------------------------
 
 // qad2: displacement of particle ctl.nm by (rn - 0.5) * 2 * maxStep.
-__device__ void qad2(const Args &a, Ctl &ctl, double *s_new, double *s_rij, const jmm_draw *rp) {
-  Scalars *S = a.s;
+__device__ void qad2(const Args &a, Scalars *S, Ctl &ctl, double *s_new, double *s_rij,
+                     const jmm_draw *rp) {
   const uint64_t n = a.n, nm = ctl.nm, nm1 = n - 1;
   if (threadIdx.x == 0) {
     const double md = __dmul_rn(__dmul_rn(__dsub_rn(ctl.rn, 0.5), 2.0), S->max_step);
@@ -590,20 +590,19 @@ __device__ void qad2(const Args &a, Ctl &ctl, double *s_new, double *s_rij, cons
     }
   }
   __syncthreads();
-  if (ctl.accept && a.hist_on) qagrho(a, ctl);  // src/jmmMCState.cpp:1431
+  if (ctl.accept && a.hist_on) qagrho(a, S, ctl);  // src/jmmMCState.cpp:1431
 }
 
 // qad2 with its histogram accumulation, which the reference makes whatever
 // the outcome, the wall rejection included (src/jmmMCState.cpp:1453).
-__device__ void qad2_step(const Args &a, Ctl &ctl, double *s_new, double *s_rij,
+__device__ void qad2_step(const Args &a, Scalars *S, Ctl &ctl, double *s_new, double *s_rij,
                           const jmm_draw *rp) {
-  qad2(a, ctl, s_new, s_rij, rp);
-  if (a.hist_on) ugrho(a);
+  qad2(a, S, ctl, s_new, s_rij, rp);
+  if (a.hist_on) ugrho(a, S);
 }
 
 // fav: full-energy volume move, linear dl uniform in +-maxdl.
-__device__ void fav(const Args &a, Ctl &ctl, const jmm_draw *rp) {
-  Scalars *S = a.s;
+__device__ void fav(const Args &a, Scalars *S, Ctl &ctl, const jmm_draw *rp) {
   const uint64_t n = a.n;
   if (threadIdx.x == 0) {
     const double dl = __dmul_rn(__dmul_rn(__dsub_rn(ctl.rn, 0.5), 2.0), S->max_dl);
@@ -656,8 +655,7 @@ __device__ void fav(const Args &a, Ctl &ctl, const jmm_draw *rp) {
 // qavLJ with a nine-entry phi buffer.  The reference's six-entry buffer
 // (src/jmmMCState.cpp:1651) overflows and aborts there; nothing here is
 // pinned to it.
-__device__ void qav_lj(const Args &a, Ctl &ctl, const jmm_draw *rp) {
-  Scalars *S = a.s;
+__device__ void qav_lj(const Args &a, Scalars *S, Ctl &ctl, const jmm_draw *rp) {
   const uint64_t n = a.n;
   __shared__ double lrat1_s;
   if (threadIdx.x == 0) {
@@ -720,15 +718,14 @@ __device__ void qav_lj(const Args &a, Ctl &ctl, const jmm_draw *rp) {
   }
   __syncthreads();
   if (a.hist_on) {  // fgrho on acceptance, ugrho always (src/jmmMCState.cpp:1717, :1726)
-    if (ctl.accept) fgrho(a);
-    ugrho(a);
+    if (ctl.accept) fgrho(a, S);
+    ugrho(a, S);
   }
 }
 
 // ECheck: full FP64 re-sum of E from the positions; on |dE| > 1e-4 rebuild
 // every pair and total.
-__device__ void echeck(const Args &a, Ctl &ctl) {
-  Scalars *S = a.s;
+__device__ void echeck(const Args &a, Scalars *S, Ctl &ctl) {
   const uint64_t n = a.n;
   full_terms(a, a.r, false, S->l);
   __syncthreads();
@@ -782,11 +779,20 @@ __device__ void echeck(const Args &a, Ctl &ctl) {
 
 // ---- kernels ------------------------------------------------------------------
 
+static_assert(sizeof(Scalars) % 8 == 0, "Scalars copies as 8-byte words");
+
+// The chain's scalars live in shared memory for the launch (copied in at the
+// start, back at the end), so that thread 0's serial part of a step (draws,
+// the decision, counters, totals) waits on no global-memory round trip.
 __global__ void __launch_bounds__(kThreads, 1)
     steps_kernel(Args a, uint64_t n_steps, const jmm_draw *replay, jmm_step_record *log) {
   extern __shared__ double smem[];
   __shared__ Ctl ctl;
-  Scalars *S = a.s;
+  __shared__ Scalars s_sh;
+  for (uint32_t k = threadIdx.x; k < sizeof(Scalars) / 8; k += blockDim.x)
+    reinterpret_cast<uint64_t *>(&s_sh)[k] = reinterpret_cast<const uint64_t *>(a.s)[k];
+  __syncthreads();
+  Scalars *S = &s_sh;
   const uint64_t nm1 = a.n - 1;
   double *s_new = smem;
   double *s_rij = smem + 9 * nm1;
@@ -808,17 +814,17 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();
     if (ctl.nm < a.n) {
-      qad2_step(a, ctl, s_new, s_rij, rp);
+      qad2_step(a, S, ctl, s_new, s_rij, rp);
     } else if (ctl.nm == a.n) {
       if (a.use_qavlj)
-        qav_lj(a, ctl, rp);
+        qav_lj(a, S, ctl, rp);
       else
-        fav(a, ctl, rp);
+        fav(a, S, ctl, rp);
     } else if (threadIdx.x == 0) {
       S->error = JMM_ERR_INVALID;  // trial type beyond N: "unknown trial type"
     }
     __syncthreads();
-    if (a.eci && (S->sn % a.eci) == 0) echeck(a, ctl);
+    if (a.eci && (S->sn % a.eci) == 0) echeck(a, S, ctl);
     if (threadIdx.x < 12) update_thermo_lane(S, a.n, threadIdx.x);
     if (threadIdx.x == 0) {
       if (log) {
@@ -839,6 +845,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();
   }
+  for (uint32_t k = threadIdx.x; k < sizeof(Scalars) / 8; k += blockDim.x)
+    reinterpret_cast<uint64_t *>(a.s)[k] = reinterpret_cast<const uint64_t *>(&s_sh)[k];
 }
 
 __global__ void __launch_bounds__(kThreads, 1) fad_kernel(Args a, uint64_t nm, double d) {
@@ -882,7 +890,7 @@ __global__ void __launch_bounds__(kThreads, 1) fad_kernel(Args a, uint64_t nm, d
 
 __global__ void __launch_bounds__(kThreads, 1) echeck_kernel(Args a) {
   __shared__ Ctl ctl;
-  echeck(a, ctl);
+  echeck(a, a.s, ctl);
 }
 
 // One trial of a given kind outside Step: qad2 of particle nm with trial
@@ -902,11 +910,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   __syncthreads();
   if (kind == JMM_KIND_DISPLACEMENT)
-    qad2_step(a, ctl, smem, smem + 9 * nm1, nullptr);
+    qad2_step(a, a.s, ctl, smem, smem + 9 * nm1, nullptr);
   else if (a.use_qavlj)
-    qav_lj(a, ctl, nullptr);
+    qav_lj(a, a.s, ctl, nullptr);
   else
-    fav(a, ctl, nullptr);
+    fav(a, a.s, ctl, nullptr);
   if (threadIdx.x == 0 && rec) {
     Scalars *S = a.s;
     rec->sn = S->sn;
@@ -1077,8 +1085,8 @@ __global__ void __launch_bounds__(kThreads, 1) hist_init_kernel(Args a) {
   }
   if (threadIdx.x == 0) a.s->hist_ticks = 0;
   __syncthreads();
-  fgrho(a);
-  ugrho(a);
+  fgrho(a, a.s);
+  ugrho(a, a.s);
 }
 
 // Sums of bins [b0, b0 + nb) since the last take, as the reference's int
@@ -1178,10 +1186,21 @@ extern "C" int jmm_plain_create(const jmm_params *prm, jmm_plain **out) {
   a.p = prm->p;
   a.seed = prm->seed;
   a.eci = prm->eci;
-  // s_new (9 quantities) and s_rij per partner; and, where it fits, the
-  // stored old terms too, so that qad2's in-order sums read shared memory
-  // instead of one strided HBM load per term
-  a.stage_old = 19 * (n - 1) * sizeof(double) <= 227 * 1024 ? 1 : 0;
+  // s_new (9 quantities) and s_rij per partner; and, where it fits beside
+  // the kernels' own static shared memory, the stored old terms too, so that
+  // qad2's in-order sums read shared memory instead of one strided load per
+  // term
+  size_t static_smem = 0;
+  {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, steps_kernel) == cudaSuccess && fa.sharedSizeBytes > static_smem)
+      static_smem = fa.sharedSizeBytes;
+    if (cudaFuncGetAttributes(&fa, move_kernel) == cudaSuccess && fa.sharedSizeBytes > static_smem)
+      static_smem = fa.sharedSizeBytes;
+    cudaGetLastError();
+  }
+  const size_t room = 227 * 1024 - static_smem;
+  a.stage_old = 19 * (n - 1) * sizeof(double) <= room ? 1 : 0;
   h->smem_bytes = (a.stage_old ? 19 : 10) * (n - 1) * sizeof(double);
 
   int rc = JMM_OK;
