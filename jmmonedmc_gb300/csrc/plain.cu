@@ -105,8 +105,12 @@ struct Ctl {
   double part[2][9];  // qad2: the partner sums over i < nm and over i > nm
   uint64_t ncomp;     // pairs compacted for a full sum
   uint32_t wsum[32];  // per-warp counts of the compaction scan
+  // qad2 with its old terms staged: bit p of the partner slots, set where any
+  // of the partner's eighteen terms (new and stored) is not +0.0
+  uint32_t nz[48];
   int32_t wall, accept, kind, outcome, reset, pad;
 };
+constexpr uint64_t kNzSlots = 32 * 48;
 
 // ---- pair potentials (FP64, the reference's operand order) --------------
 
@@ -497,35 +501,69 @@ __device__ void qad2(const Args &a, Scalars *S, Ctl &ctl, double *s_new, double 
   if (ctl.wall) return;
   const double md = ctl.md, l = S->l;
   double *s_old = s_rij + nm1;  // 9 * nm1 when a.stage_old
-  for (uint64_t p = threadIdx.x; p < nm1; p += blockDim.x) {
-    const uint64_t i = p < nm ? p : p + 1;
-    const uint64_t lo = i < nm ? i : nm, hi = i < nm ? nm : i;
-    const uint64_t ind = lo * n + hi;
-    const double rt = (i < nm) ? __dadd_rn(a.rij[ind], md) : __dsub_rn(a.rij[ind], md);
-    double phi[9];
-    if (pair_cut(a, lo, hi)) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // with the old terms staged, each warp marks its 32 partner slots whose
+  // eighteen terms are not all +0.0 as it forms them
+  const bool use_nz = a.stage_old && nm1 <= kNzSlots;
+  for (uint64_t base = threadIdx.x - lane; base < nm1; base += blockDim.x) {
+    const uint64_t p = base + lane;
+    unsigned long long bits = 0;
+    if (p < nm1) {
+      const uint64_t i = p < nm ? p : p + 1;
+      const uint64_t lo = i < nm ? i : nm, hi = i < nm ? nm : i;
+      const uint64_t ind = lo * n + hi;
+      const double rt = (i < nm) ? __dadd_rn(a.rij[ind], md) : __dsub_rn(a.rij[ind], md);
+      double phi[9];
+      if (pair_cut(a, lo, hi)) {
 #pragma unroll
-      for (int k = 0; k < 9; ++k) phi[k] = 0.0;
-    } else {
-      phi_eval(a, rt, true, l, phi);
+        for (int k = 0; k < 9; ++k) phi[k] = 0.0;
+      } else {
+        phi_eval(a, rt, true, l, phi);
+      }
+      s_rij[p] = rt;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        s_new[k * nm1 + p] = phi[k];
+        bits |= (unsigned long long)__double_as_longlong(phi[k]);
+      }
+      if (a.stage_old) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          const double v = a.q[k * a.nn + ind];
+          s_old[k * nm1 + p] = v;
+          bits |= (unsigned long long)__double_as_longlong(v);
+        }
+      }
     }
-    s_rij[p] = rt;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) s_new[k * nm1 + p] = phi[k];
-    if (a.stage_old) {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) s_old[k * nm1 + p] = a.q[k * a.nn + ind];
+    if (use_nz) {
+      const unsigned m = __ballot_sync(0xffffffffu, bits != 0);
+      if (lane == 0) ctl.nz[base / 32] = m;
     }
   }
   __syncthreads();
   // the reference's order: (sum - old) + new over the partners i < nm (lanes
   // 0-8 of warp 0) and, as a separate sum, over i > nm (lanes 0-8 of warp 1):
   // two dependent FP64 chains, which overlap only in different warps.  The
-  // 32 lanes of the warp test 32 partners at a time (any of the eighteen
-  // terms other than +0.0) and the nine summing lanes add the marked ones
-  // in index order; the others would add +0.0 twice.
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (warp < 2) {
+  // nine summing lanes add the partners marked above (any of the eighteen
+  // terms other than +0.0) in index order; the others would add +0.0 twice.
+  // Without the marks the 32 lanes of the warp test 32 partners at a time.
+  if (warp < 2 && use_nz) {
+    const uint64_t p0 = warp == 0 ? 0 : nm, p1 = warp == 0 ? nm : nm1;
+    double sp = 0.0;
+    if (lane < 9) {
+      for (uint64_t w = p0 / 32; w * 32 < p1; ++w) {
+        unsigned m = ctl.nz[w];
+        if (w * 32 < p0) m &= ~0u << (unsigned)(p0 - w * 32);
+        if (p1 - w * 32 < 32) m &= (1u << (unsigned)(p1 - w * 32)) - 1u;
+        for (; m; m &= m - 1u) {
+          const uint64_t pp = w * 32 + (uint64_t)(__ffs(m) - 1);
+          sp = __dadd_rn(__dsub_rn(sp, s_old[(uint64_t)lane * nm1 + pp]),
+                         s_new[(uint64_t)lane * nm1 + pp]);
+        }
+      }
+      ctl.part[warp][lane] = sp;
+    }
+  } else if (warp < 2) {
     const uint64_t p0 = warp == 0 ? 0 : nm, p1 = warp == 0 ? nm : nm1;
     // stored term k of partner slot p
     auto old_term = [&](int k, uint64_t p) -> double {
