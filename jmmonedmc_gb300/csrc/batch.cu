@@ -1082,7 +1082,7 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
   // state is restored before each run, the first run warms the code path and
   // the best of the next three counts (a single short run can land on a
   // clock ramp).
-  auto trial = [&](int cls, float *ms_out) -> int {
+  auto trial = [&](int cls, float *ms_out, uint32_t sweeps) -> int {
     float best_run = 1e30f;
     for (int rep = 0; rep < 4; ++rep) {
       float ms = 0.0f;
@@ -1093,10 +1093,10 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
       cudaEventRecord(t0, b->stream);
       int rc = JMM_OK;
       if (cls < 0) {
-        rc = launch(b, trial_sweeps, b->stream);
+        rc = launch(b, sweeps, b->stream);
       } else {
         for (size_t k = 0; k < b->classes.size(); ++k)
-          if (b->classes[k].pot == kPots[cls]) rc = launch_class(b, k, trial_sweeps, b->stream);
+          if (b->classes[k].pot == kPots[cls]) rc = launch_class(b, k, sweeps, b->stream);
       }
       cudaEventRecord(t1, b->stream);
       if (rc) return rc;
@@ -1136,7 +1136,7 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
           continue;
         }
         float ms = 0.0f;
-        rc = trial(per_class ? pi : -1, &ms);
+        rc = trial(per_class ? pi : -1, &ms, trial_sweeps);
         if (rc) break;
         timed.emplace_back(ms, sh);
       }
@@ -1152,7 +1152,7 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
         continue;
       }
       float ms = 0.0f;
-      rc = trial(per_class ? pi : -1, &ms);
+      rc = trial(per_class ? pi : -1, &ms, trial_sweeps);
       if (rc == JMM_OK && ms < best_ms) {
         best_ms = ms;
         for (int q = 0; q < 3; ++q) best[q] = timed[c].second[q];
@@ -1161,14 +1161,16 @@ extern "C" int jmm_batch_autotune(jmm_batch *b, uint32_t trial_sweeps, uint32_t 
   }
   if (per_class && rc == JMM_OK && b->classes.size() > 1) {
     // the classes were timed alone but run side by side: keep the per-class
-    // defaults where they run the whole batch faster than the tuned shapes
+    // defaults unless the tuned shapes run the whole batch at least 3 %
+    // faster, timed over ten times the trial sweeps (short side-by-side runs
+    // of several class kernels did not rank the two sets as long runs do)
     Shape dflt[3];
     default_shapes(b, dflt);
     float t_best = 1e30f, t_dflt = 1e30f;
-    if (apply_layout(b, best) == JMM_OK) rc = trial(-1, &t_best);
-    if (rc == JMM_OK && apply_layout(b, dflt) == JMM_OK) rc = trial(-1, &t_dflt);
+    if (apply_layout(b, best) == JMM_OK) rc = trial(-1, &t_best, 10 * trial_sweeps);
+    if (rc == JMM_OK && apply_layout(b, dflt) == JMM_OK) rc = trial(-1, &t_dflt, 10 * trial_sweeps);
     clear_error();
-    if (rc == JMM_OK && t_dflt < t_best)
+    if (rc == JMM_OK && t_dflt < 1.03f * t_best)
       for (int q = 0; q < 3; ++q) best[q] = dflt[q];
   }
   cudaMemcpy(b->d_x, x_save, b->total_floats * sizeof(float), cudaMemcpyDeviceToDevice);
