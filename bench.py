@@ -37,6 +37,11 @@ if REPO not in sys.path:
 METRIC = "attempted MC moves/s (batched chains, FP32 pairs / FP64 totals)"
 UNIT = "moves/s"
 FLOP_PER_PAIR = 9  # d, r^2, inv2 scale, inv6 (2), inv6-1, products (2), select
+# FP32 FLOP of one pair energy by potential (each also one MUFU op: the
+# reciprocal, or exp for the Gaussian core): LJ 12-6 and soft sphere as
+# above (soft sphere: inv6^2 in place of inv6 (inv6 - 1)); Gaussian core:
+# d, r^2, r^2 / sigma^2, exp argument, scale, select, accumulate
+FLOP_PER_PAIR_BY_POT = {0: 9, 1: 9, 2: 7}  # JMM_POT_LJCUT, _SOFTSPHERE, _GAUSS
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -382,11 +387,13 @@ def algorithmic_pairs(before, after, x_all, chains):
         n = int(c.n)
         ks.append(in_cutoff_neighbours(x_all[off:off + n], [n], float(c.cutoff)))
         off += n
-    total = 0.0
+    total = flop = 0.0
     for c, k, d_att, v_att in zip(chains, ks, after["disp_att"] - before["disp_att"],
                                   after["vol_att"] - before["vol_att"]):
-        total += k * (2.0 * float(d_att) + 0.5 * int(c.n) * float(v_att))
-    return total, sum(ks) / max(1, len(ks))
+        pairs = k * (2.0 * float(d_att) + 0.5 * int(c.n) * float(v_att))
+        total += pairs
+        flop += pairs * FLOP_PER_PAIR_BY_POT.get(int(c.potential), FLOP_PER_PAIR)
+    return total, sum(ks) / max(1, len(ks)), flop
 
 
 # ---- the large-chain workload -------------------------------------------------------
@@ -737,7 +744,7 @@ def run_grad(args, rank, world, local_rank):
     n_tot = sum(int(c.n) for c in chains)
     x_host = torch.empty(n_tot, dtype=torch.float32, pin_memory=True).numpy()
     x_host[:] = np.concatenate([b.positions(k) for k in range(len(chains))])
-    alg_pairs, k_mean = algorithmic_pairs(before, after, x_host, chains)
+    alg_pairs, k_mean, alg_flop = algorithmic_pairs(before, after, x_host, chains)
     desc = chain_array(chains)
     chain_view(desc)["l0"] = b.results()["l"]  # the box lengths of these positions
     e2e_times, e2e_moves = [], 0
@@ -889,7 +896,7 @@ def run_ours(args, rank, world, local_rank):
     for k, c in enumerate(chains):
         x_host[x_off:x_off + c.n] = b.positions(k)
         x_off += c.n
-    alg_pairs, k_mean = algorithmic_pairs(before, after, x_host, chains)
+    alg_pairs, k_mean, alg_flop = algorithmic_pairs(before, after, x_host, chains)
     lbox = after["l"].copy()
     for k, c in enumerate(chains):
         c.l0 = float(lbox[k])
@@ -927,7 +934,7 @@ def run_ours(args, rank, world, local_rank):
     # slots the kernel evaluates (4W per kept displacement, in-cut-off pairs
     # of the volume moves)
     alg_per_launch = alg_pairs / args.steps
-    flop_per_launch = alg_per_launch * FLOP_PER_PAIR
+    flop_per_launch = alg_flop / args.steps  # 9 FLOP per LJ or soft-sphere pair, 7 per Gaussian
     achieved = flop_per_launch / (launch_ms * 1e-3) / 1e12
     traffic = profile_traffic(args, pairs / args.steps, S) if args.workload == "npt" else None
     line = {
@@ -962,7 +969,8 @@ def run_ours(args, rank, world, local_rank):
                                  "region); 2k pair energies per displacement (old and trial "
                                  "position), N k / 2 per volume move"),
             "in_cutoff_partners_k": k_mean,
-            "flop_per_pair": FLOP_PER_PAIR,
+            "flop_per_pair": alg_flop / max(alg_pairs, 1.0),
+            "flop_per_pair_by_potential": {"ljcut": 9, "softsphere": 9, "gauss": 7},
             "mufu_rcp_frac": alg_per_launch / (launch_ms * 1e-3) / (rcp_peak.value * 1e12),
             "pair_evals_per_s": alg_per_launch / (launch_ms * 1e-3),
             "window_slots_per_launch": pairs / args.steps,
