@@ -41,7 +41,12 @@ FLOP_PER_PAIR = 9  # d, r^2, inv2 scale, inv6 (2), inv6-1, products (2), select
 # reciprocal, or exp for the Gaussian core): LJ 12-6 and soft sphere as
 # above (soft sphere: inv6^2 in place of inv6 (inv6 - 1)); Gaussian core:
 # d, r^2, r^2 / sigma^2, exp argument, scale, select, accumulate
-FLOP_PER_PAIR_BY_POT = {0: 9, 1: 9, 2: 7}  # JMM_POT_LJCUT, _SOFTSPHERE, _GAUSS
+
+
+def flop_per_pair_of(potential):
+    from jmmonedmc_gb300 import abi
+    return {abi.JMM_POT_LJCUT: 9, abi.JMM_POT_LJ: 9, abi.JMM_POT_SOFTSPHERE: 9,
+            abi.JMM_POT_GAUSS: 7}.get(int(potential), FLOP_PER_PAIR)
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -392,7 +397,7 @@ def algorithmic_pairs(before, after, x_all, chains):
                                   after["vol_att"] - before["vol_att"]):
         pairs = k * (2.0 * float(d_att) + 0.5 * int(c.n) * float(v_att))
         total += pairs
-        flop += pairs * FLOP_PER_PAIR_BY_POT.get(int(c.potential), FLOP_PER_PAIR)
+        flop += pairs * flop_per_pair_of(c.potential)
     return total, sum(ks) / max(1, len(ks)), flop
 
 

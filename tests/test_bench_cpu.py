@@ -209,6 +209,24 @@ def test_in_cutoff_neighbours():
     assert bench.in_cutoff_neighbours(both, [5, 5], [2.0, 1.0]) == pytest.approx(12.0 / 10)
 
 
+def test_algorithmic_pairs_weigh_each_potential():
+    """2k pair energies per displacement, N k / 2 per volume move; 9 FP32
+    FLOP per LJ or soft-sphere pair, 7 per Gaussian-core pair."""
+    import numpy as np
+    from jmmonedmc_gb300 import abi
+    x = np.array([0.0, 1.0, 2.0, 3.5, 10.0])  # k = 1.6 at rc 2
+    chains = [abi.make_chain(5, potential=abi.JMM_POT_LJCUT, cutoff=2.0),
+              abi.make_chain(5, potential=abi.JMM_POT_SOFTSPHERE, cutoff=2.0),
+              abi.make_chain(5, potential=abi.JMM_POT_GAUSS, cutoff=2.0)]
+    before = {"disp_att": np.zeros(3), "vol_att": np.zeros(3)}
+    after = {"disp_att": np.array([10.0, 10.0, 10.0]), "vol_att": np.array([2.0, 0.0, 0.0])}
+    pairs, k, flop = bench.algorithmic_pairs(before, after, np.concatenate([x, x, x]), chains)
+    per = [1.6 * (2 * 10 + 0.5 * 5 * 2), 1.6 * 20, 1.6 * 20]
+    assert k == pytest.approx(1.6)
+    assert pairs == pytest.approx(sum(per))
+    assert flop == pytest.approx(9 * per[0] + 9 * per[1] + 7 * per[2])
+
+
 @pytest.mark.parametrize("profile", ["chains_kernel_batched_npt",
                                      "domain_kernel_large_chains"])
 def test_issue_roofline_from_committed_figures(monkeypatch, profile):
