@@ -661,15 +661,20 @@ def grad_workload(args, seed):
               for k in range(args.chains)]
     cfg = abi.make_batch_config(seed=seed, vol_move=abi.JMM_VOLMOVE_LNL,
                                 vol_schedule=abi.JMM_VOLSCHED_SWEEP, resum_sweeps=10,
-                                precision=abi.JMM_PREC_FAST)
+                                precision=abi.JMM_PREC_FAST,
+                                split_n=getattr(args, "split_n", 0) or 0)
     return cfg, chains
 
 
 def grad_config(args, extra=None):
+    split = getattr(args, "split_n", 0) or 0
     d = {"workload": (f"differentiation: {args.chains} chains x N={args.n}, LJ 12-6 eps=sigma=1 "
                       "rc=3, rho=0.7 lattice start, T=1, half NVT and half NPT (P=1, ln L "
                       "moves delta=0.02 once per sweep), max displacement 0.3; U, dU/deps, "
-                      f"dU/dsigma, dU/dL of every chain every {args.sample_every} sweeps"),
+                      f"dU/dsigma, dU/dL of every chain every {args.sample_every} sweeps"
+                      + (f"; NVT chains of N >= {split} split over a block's warps in "
+                         "alternating domains (sampled once per sweep)" if split else "")),
+         "split_n": split,
          "chains": args.chains, "particles_per_chain": args.n,
          "sweeps_per_step": args.sweeps_per_step, "sample_every": args.sample_every,
          "l2": "flushed between timed steps (256 MiB device write)",
