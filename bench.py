@@ -703,8 +703,19 @@ def run_grad(args, rank, world, local_rank):
     fp32_peak, rcp_peak = C.c_double(), C.c_double()
     _native.call("jmm_measure_peaks", C.byref(fp32_peak), C.byref(rcp_peak))
     b = ChainBatch(cfg, chains)
-    # trials of a few milliseconds each: the shapes' differences are a few per cent
-    lanes, spr, cpb = (0, 0, 0) if args.no_autotune else b.autotune(trial_sweeps=20)
+    if args.no_autotune:
+        lanes, spr, cpb = 0, 0, 0
+    else:
+        # one untimed step first, so that the trials see equilibrated chains
+        # (on the starting lattice no fourth neighbour lies within the
+        # cut-off, and a window of 3 would look best); trials of a few
+        # milliseconds each: the shapes' differences are a few per cent
+        b.run(args.sweeps_per_step)
+        lanes, spr, cpb = b.autotune(trial_sweeps=20)
+    from jmmonedmc_gb300 import abi
+    names = {abi.JMM_POT_LJCUT: "ljcut", abi.JMM_POT_SOFTSPHERE: "softsphere",
+             abi.JMM_POT_GAUSS: "gauss"}
+    class_shapes = {names[p]: "%dx%d, %d per block, window %d" % v for p, v in b.shapes().items()}
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
@@ -788,7 +799,8 @@ def run_grad(args, rank, world, local_rank):
         "dtype": "f32",
         "data": "synthetic (lattice start, seeded Philox moves)",
         "config": grad_config(args, {"lanes_per_chain": lanes, "steps_per_round": spr,
-                                     "chains_per_block": cpb, "parallelism": f"replicas{world}",
+                                     "chains_per_block": cpb, "class_shapes": class_shapes,
+                                     "parallelism": f"replicas{world}",
                                      "wall_s_timed": wall}),
         "gradient_samples_per_s": samples / (total_ms * 1e-3),
         "without_gradients": {"value": moves / (plain_ms * 1e-3), "unit": UNIT,

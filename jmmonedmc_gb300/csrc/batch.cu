@@ -347,6 +347,8 @@ static void default_shapes(const jmm_batch *b, Shape sh[3]) {
   // per side at the densest).  Windows of 4 or 8 per side take 8 steps per
   // round, or 16 where the class holds a chain of 1024 or more particles (a
   // class lasts as long as its longest chain, whose rounds rarely conflict).
+  // The window comes from every chain of the class (split chains take the
+  // class's window too), the round shape from the chains that run whole.
   for (int pi = 0; pi < 3; ++pi) {
     double need = 0.0;
     uint32_t n_max = 0;
@@ -355,7 +357,7 @@ static void default_shapes(const jmm_batch *b, Shape sh[3]) {
       const double side = c.potential == JMM_POT_GAUSS ? 1.5 * c.n / c.l0 * c.cutoff
                                                        : c.cutoff / (0.85 * c.sigma);
       need = std::max(need, side);
-      n_max = std::max(n_max, c.n);
+      if (!is_split(b->cfg, c)) n_max = std::max(n_max, c.n);
     }
     const uint32_t gg = need > 8.0 ? 32u : (n_max >= 1024 ? 2u : 4u);
     const uint32_t ss = 32 / gg;
