@@ -247,13 +247,22 @@ __device__ __forceinline__ void fold_spread(Seg &g, jmm_chain_result *__restrict
   g.nseg = 0;
 }
 
+// The spread fold as a call of its own: the step loops of two-lane slots
+// (2 x 16) keep fewer registers live with it out of line.
+static __device__ __noinline__ void fold_spread_call(Seg &g, jmm_chain_result *__restrict__ rp,
+                                                     int cl, double l, double rho) {
+  fold_spread(g, rp, cl, l, rho);
+}
+
 // The fold of a chain of L lanes: spread over seven lanes in FAST precision,
 // by the first lane in EXACT (the order the oracle replays).
-template <int L, bool kExact>
+template <int L, bool kExact, bool kOutOfLine = false>
 __device__ __forceinline__ void fold_run(Seg &g, jmm_chain_result *__restrict__ rp, int cl,
                                          double l, double rho) {
   if (kExact || L < 8)
     fold(g, rp, cl == 0, l, rho);
+  else if (kOutOfLine)
+    fold_spread_call(g, rp, cl, l, rho);
   else
     fold_spread(g, rp, cl, l, rho);
 }
@@ -337,7 +346,9 @@ __device__ __forceinline__ float threshold_of(uint32_t w) {
 // U_new - U_old is the FP64 sum of the per-pair differences, and
 // U_new = U_old + du (a caller's U_new - U_old gives du back to within an
 // ulp of U).
-template <int L, int POT, bool PER, bool kExact, bool kScaled>
+// kPair: FAST sums U_old and U_new - U_old in one butterfly (below); the
+// step loops of two-lane slots (2 x 16) run faster with two separate ones.
+template <int L, int POT, bool PER, bool kExact, bool kScaled, bool kPair = true>
 __device__ __noinline__ void chain_energies(const float *xs, const Hot &H, int n, int gl,
                                                unsigned gmask, float lf, float s, float lnf,
                                                double &u_old, double &u_new, uint64_t &pairs,
@@ -391,7 +402,7 @@ __device__ __noinline__ void chain_energies(const float *xs, const Hot &H, int n
       if (kScaled) un = __dadd_rn(un, (double)en);
     }
   }
-  if (!kExact && kScaled && L >= 2) {
+  if (!kExact && kScaled && kPair && L >= 2) {
     // both FAST sums over the lanes in one FP64 butterfly: after the first
     // exchange even lanes carry sums of shapes, odd lanes of differences
     const bool odd = gl & 1;
@@ -404,7 +415,10 @@ __device__ __noinline__ void chain_energies(const float *xs, const Hot &H, int n
     pairs += __reduce_add_sync(gmask, cnt);
     return;
   }
-  if (!kExact) uo = __dmul_rn((double)H.eps4, (double)fo);
+  if (!kExact) {
+    uo = __dmul_rn((double)H.eps4, (double)fo);
+    un = __dmul_rn((double)H.eps4, (double)fd);
+  }
   u_old = group_sum_d<L>(uo, gmask);
   if (!kScaled) {
     u_new = u_old;
@@ -620,7 +634,8 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       }
       double uo, un;
       const float lnf = (float)lnew;
-      chain_energies<L, POT, PER, kExact, true>(xs, H, n, cl, gmask, lf, s, lnf, uo, un, pairs, err);
+      chain_energies<L, POT, PER, kExact, true, (G >= 4)>(xs, H, n, cl, gmask, lf, s, lnf, uo, un,
+                                                         pairs, err);
       const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
       note_drift(rp, writer, drift);
       if (kShares) gather_shares<L>(g, sd_loc, sd2_loc, gmask);
@@ -630,7 +645,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
       bool acc = arg < (double)thr_0;
       if (!(lnew > 0.0)) acc = false;
       if (PER && !(lnew > 2.0 * (double)P.rc)) acc = false;
-      fold_run<L, kExact>(g, rp, cl, L_box, rho_box);
+      fold_run<L, kExact, (G < 4)>(g, rp, cl, L_box, rho_box);
       v_att += 1;
       if (acc) {
         for (int i = cl; i < n; i += L) xs[i] = __fmul_rn(xs[i], s);
@@ -809,7 +824,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
         const double drift = fabs(__dsub_rn(__dadd_rn(g.e0, (double)g.delta), uo));
         note_drift(rp, writer, drift);
         if (kShares) gather_shares<L>(g, sd_loc, sd2_loc, gmask);
-        fold_run<L, kExact>(g, rp, cl, L_box, rho_box);
+        fold_run<L, kExact, (G < 4)>(g, rp, cl, L_box, rho_box);
         g.e0 = uo;
       }
     }
@@ -818,7 +833,7 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
   if (HALO)
     g.e0 = __dadd_rn(g.e0, (double)g.delta);
   else
-    fold_run<L, kExact>(g, rp, cl, L_box, rho_box);
+    fold_run<L, kExact, (G < 4)>(g, rp, cl, L_box, rho_box);
   if (!isfinite(g.e0)) err = JMM_ERR_NUMERIC;
   if (writer) {
     rp->e = g.e0;
