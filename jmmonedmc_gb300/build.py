@@ -27,6 +27,7 @@ UNITS = {
     "common.cu": [],
     "plain.cu": ["-fmad=false"],
     "batch.cu": [],
+    "batch_wide.cu": [],
     "grad.cu": [],
     "noalloc.cu": ["-fmad=false"],
     "peak.cu": [],

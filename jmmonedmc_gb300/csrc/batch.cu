@@ -42,9 +42,16 @@ ChainsKernel pick_pot(int pot, bool per) {
 }
 
 // Launch shapes: G window lanes x S steps per round (G*S = 16 or 32 lanes),
-// W neighbours per side (0 = the default of G).
-ChainsKernel pick_kernel(uint32_t g, uint32_t s, uint32_t w, bool exact, int pot, bool per) {
+// W neighbours per side (0 = the default of G); `wide`: the 128-register
+// instantiation of a single-warp FAST shape (a batch with at most 16 such
+// chains per SM).
+ChainsKernel pick_kernel(uint32_t g, uint32_t s, uint32_t w, bool exact, int pot, bool per,
+                         bool wide = false) {
   if (w == 0) w = (uint32_t)window_of((int)g);
+  if (wide && !exact && g * s == 32) {
+    ChainsKernel k = pick_kernel_wide(g, s, w, pot, per);
+    if (k) return k;
+  }
 #define JMM_SHAPE(G_, S_, W_)                                                        \
   if (g == G_ && s == S_ && w == W_)                                                \
     return exact ? pick_pot<G_, S_, true, W_>(pot, per) : pick_pot<G_, S_, false, W_>(pot, per);
@@ -115,6 +122,7 @@ struct PotClass {
   size_t smem;
   bool split = false;   // split chains: one block of `warps` warps per chain
   uint32_t warps = 0;
+  bool wide = false;    // the 128-register kernel (pick_kernel)
 };
 
 constexpr int kMaxClasses = 6;  // three potentials, each whole and split
@@ -137,6 +145,7 @@ struct jmm_batch {
   float *d_x = nullptr;
   double *d_e = nullptr;
   uint32_t g = 8, spr = 4, cpb = 4, win = 4, n_blocks = 0;  // the shape of the largest class
+  uint32_t n_sm = 0;  // SMs of the batch's device
   Shape shapes[3] = {{8, 4, 4, 4}, {8, 4, 4, 4}, {8, 4, 4, 4}};  // per potential class (kPots order)
   size_t smem = 0;
   cudaStream_t stream = nullptr;
@@ -232,6 +241,16 @@ static int apply_layout(jmm_batch *b, const Shape shapes[3]) {
     P.two_max_step = (float)(2.0 * c.max_step);
     P.vol_step = (float)c.vol_step;
   };
+  // Single-warp FAST classes take the 128-register kernel when the batch's
+  // chains that run whole come to at most 16 warps per SM (a full wave at
+  // 72 registers holds 27).
+  double whole_warps = 0.0;
+  for (const jmm_chain_desc &c : b->chains) {
+    if (is_split(b->cfg, c)) continue;
+    for (int pi = 0; pi < 3; ++pi)
+      if (c.potential == kPots[pi]) whole_warps += shapes[pi].g * shapes[pi].spr / 32.0;
+  }
+  const bool wide = !exact && b->n_sm > 0 && whole_warps <= 16.0 * b->n_sm;
   for (int pi = 0; pi < 3; ++pi) {
     const int pot = kPots[pi];
     // split chains of this potential: the leading ones in launch order, one
@@ -288,6 +307,7 @@ static int apply_layout(jmm_batch *b, const Shape shapes[3]) {
     pc.shape.w = win;
     pc.first = slot0;
     pc.count = 0;
+    pc.wide = wide && g * spr == 32;
     while (slot0 + pc.count < b->n_chains && b->chains[b->order[slot0 + pc.count]].potential == pot)
       pc.count++;
     if (per) {
@@ -311,7 +331,7 @@ static int apply_layout(jmm_batch *b, const Shape shapes[3]) {
       return fail(JMM_ERR_INVALID, "a block's chains need %zu bytes of shared memory (max %zu): "
                   "lower chains_per_block", pc.smem, kMaxSmem);
     if (pc.count) {
-      ChainsKernel kf = pick_kernel(g, spr, win, exact, pot, per);
+      ChainsKernel kf = pick_kernel(g, spr, win, exact, pot, per, pc.wide);
       JMM_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem));
       classes.push_back(pc);
     }
@@ -396,7 +416,7 @@ static int launch_class(jmm_batch *b, size_t k, uint64_t n_sweeps, cudaStream_t 
     return JMM_OK;
   }
   const uint32_t threads = pc.shape.g * pc.shape.spr * pc.shape.cpb;
-  ChainsKernel kf = pick_kernel(pc.shape.g, pc.shape.spr, pc.shape.w, exact, pc.pot, per);
+  ChainsKernel kf = pick_kernel(pc.shape.g, pc.shape.spr, pc.shape.w, exact, pc.pot, per, pc.wide);
   kf<<<pc.n_blocks, threads, pc.smem, st>>>(b->d_params + pc.first, b->d_res, b->d_x, kc);
   JMM_CUDA(cudaGetLastError());
   return JMM_OK;
@@ -599,6 +619,12 @@ static int batch_create(const jmm_batch_config *cfg, const jmm_chain_desc *chain
   });
 
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) {
+    int dev = 0, n_sm = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    b->n_sm = (uint32_t)n_sm;
+  }
   for (int k = 0; k < kMaxClasses && e == cudaSuccess; ++k) {
     e = cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming);

@@ -854,11 +854,13 @@ __device__ __forceinline__ void run_chain(const ChainParams &P, jmm_chain_result
 
 // One kernel per (shape, potential, boundary, precision): the chains of one
 // potential class, L lanes each, chains_per_block chains per block.
-// A single-warp chain is held to 72 registers so that 27 of them stay
+// A single-warp chain is held to REG = 72 registers so that 27 of them stay
 // resident per SM (4096 chains on 152 SMs in one wave); chains that share a
-// warp (G*S < 32) may use 128.
-template <int G, int S, int POT, bool PER, bool kExact, int WIN>
-__global__ void __maxnreg__(G * S == 32 ? 72 : 128) chains_kernel(const ChainParams *__restrict__ prm,
+// warp (G*S < 32) may use 128, and so may single-warp chains of a batch
+// with at most 16 of them per SM (the REG = 128 instantiations,
+// csrc/batch_wide.cu), which then spill nothing.
+template <int G, int S, int POT, bool PER, bool kExact, int WIN, int REG = (G * S == 32 ? 72 : 128)>
+__global__ void __maxnreg__(REG) chains_kernel(const ChainParams *__restrict__ prm,
                                                      jmm_chain_result *__restrict__ res,
                                                      float *__restrict__ xg, KernelCfg cfg) {
   constexpr int L = G * S;
@@ -1099,6 +1101,12 @@ __global__ void __maxnreg__(64) split_kernel(const ChainParams *__restrict__ prm
     rp->error = e_all;
   }
 }
+
+typedef void (*ChainsKernelFn)(const ChainParams *, jmm_chain_result *, float *, KernelCfg);
+
+// The 128-register FAST instantiations of the single-warp shapes
+// (csrc/batch_wide.cu); nullptr for a shape that has none.
+ChainsKernelFn pick_kernel_wide(uint32_t g, uint32_t s, uint32_t w, int pot, bool per);
 
 // Fresh FP64 energies of every chain (32 lanes per chain).
 template <bool kExact>
