@@ -1119,7 +1119,7 @@ SUB_KEYS = ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "dtype"
 def sub_workload_records(args, local_rank):
     """Compact records of the uneven, gradient and large-chain workloads at
     their own full sizes, for the one-GPU line: 3 timed steps after 3 warm-up
-    steps (each workload's own step: 500, 200 and 20 sweeps), one e2e step,
+    steps (each workload's own step: 500, 200 and 20 sweeps), two e2e steps,
     a 1 s CPU sample."""
     out = {}
     for wl in SUB_WORKLOADS:
@@ -1127,7 +1127,7 @@ def sub_workload_records(args, local_rank):
         sub.workload, sub.chains, sub.n, sub.sweeps_per_step = wl, 4096, 256, 1000
         sub.split_n = None
         apply_workload_defaults(sub)
-        sub.steps, sub.warmup, sub.e2e_steps, sub.cpu_seconds = 3, 3, 1, 1.0
+        sub.steps, sub.warmup, sub.e2e_steps, sub.cpu_seconds = 3, 3, 2, 1.0
         runner = {"large": run_large, "grad": run_grad}.get(wl, run_ours)
         line = runner(sub, 0, 1, local_rank)
         rec = {k: line[k] for k in SUB_KEYS if k in line}
