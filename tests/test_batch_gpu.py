@@ -472,3 +472,29 @@ def test_autotune_per_potential_class(gpu):
         x = b.positions(k).astype(np.float64)
         e64 = oracle_lib.energy64(chains[k], x, res["l"][k])
         assert abs(fresh[k] - e64) <= 1e-6 * max(1.0, abs(e64))
+
+
+def test_wide_and_narrow_kernels_agree(gpu):
+    """A FAST batch of at most 16 whole single-warp chains per SM runs the
+    128-register chain kernel, a larger one the 72-register kernel: the same
+    code with another register budget, so a chain's record and positions
+    must be the same bit for bit either way (a chain's random stream depends
+    only on its index).  2600 chains (more than 16 per SM on 152 SMs) run
+    narrow; their first 64 alone run wide."""
+    rng = np.random.default_rng(77)
+    chains = _mixed_chains(rng, 2600, 40, 120)
+    cfg = abi.make_batch_config(seed=5, vol_move=abi.JMM_VOLMOVE_LNL,
+                                vol_schedule=abi.JMM_VOLSCHED_SWEEP, precision=abi.JMM_PREC_FAST,
+                                resum_sweeps=4, lanes_per_chain=4, steps_per_round=8,
+                                chains_per_block=4)
+    narrow, wide = ChainBatch(cfg, chains), ChainBatch(cfg, chains[:64])
+    narrow.run(12)
+    wide.run(12)
+    rn, rw = narrow.results()[:64], wide.results()
+    for f in RESULT_FIELDS:
+        a, b = rn[f], rw[f]
+        assert a.tobytes() == b.tobytes(), f
+    for k in range(64):
+        assert np.array_equal(narrow.positions(k), wide.positions(k)), k
+    narrow.close()
+    wide.close()
